@@ -1,0 +1,336 @@
+#!/usr/bin/env python3
+"""Benchmark: block-PCG throughput (RHS x iterations / s) of the LGMM solve.
+
+Workload (default ``--config precision``): the on-the-fly genotype GRM
+configuration -- N = 100,000 individuals, M = 500,000 SNPs as 2-bit PLINK
+codes (MAF ~ U(0.01, 0.5), 2% missing; ~12.5 GB in HBM), ~700,000 records
+(Poisson(6)+1 per individual, times U[0,10]), intercept + 2 covariates + time,
+right-hand sides [X y] (k = 5), components (0.6, 0.4, 0.4, 0.2, 0.2).
+Synthetic: genotypes drawn on the GPU by a counter-based generator, records
+by numpy from a fixed seed.
+
+A step is one call of the block-PCG solve (globe_pcg_dev) capped at
+``--iters`` iterations with the tolerance at 0 so every column stays active:
+it performs ``k * iters`` RHS-iterations (each = one V.P product through the
+GRM on the packed genotypes + the PCG vector updates).  ``value`` is the
+device-resident throughput; ``e2e`` is the same through globe_pcg with pinned
+host buffers (B copied in, X copied out inside the timed region).
+
+``--impl reference`` times the reference algorithm on the host cores: the
+FP32 OpenMP restatement of computeVx_multi with the reference's loop
+structure (oracle/globe_oracle.c, orc_ref_vx_f32) on a SNP subsample of the
+same workload, extrapolated to all SNPs (one PCG iteration = one V.x).
+
+Multi-GPU: the path does not shard across GPUs in this design (one GPU per
+solve); with torchrun each rank runs an independent replica and ``value`` is
+the sum over ranks divided by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PCG RHS*iters/s"
+CONFIGS = {
+    # name: N, M, record distribution, T, maf_lo, maf_hi, miss
+    "precision": dict(N=100_000, M=500_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
+                      label="N=100k indiv, M=500k 2-bit SNPs, ~700k records, k=5 RHS ([X y])"),
+    "small": dict(N=20_000, M=40_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
+                  label="N=20k indiv, M=40k SNPs, ~140k records, k=5"),
+    "c1": dict(N=2_000, M=10_000, recs=("uniform", 3, 10), T=5.0, maf_lo=0.05, maf_hi=0.5, miss=0.01,
+               label="N=2000 indiv, M=10k SNPs, ~13k records, k=5"),
+}
+VC = (0.6, 0.4, 0.4, 0.2, 0.2)
+SEED = 20261203
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_records(cfg, seed=SEED):
+    from globe_gb300 import synth
+    coh = synth.simulate_cohort(seed, cfg["N"], 0, cfg["recs"], cfg["T"], vc=VC, exact_genetic=False)
+    X = np.asfortranarray(np.column_stack([coh["cov"], coh["times"]]))
+    return coh["indiv"].astype(np.int32), X, coh["y"], cfg["N"]
+
+
+def cpu_reference_vx(indiv, X, packed_rows, maf_rows, N, k, rng):
+    """One FP32 V.x of the reference's loop structure over the given SNP rows."""
+    from oracle import oracle
+    x = rng.standard_normal((len(indiv), k)).astype(np.float32)
+    t0 = time.perf_counter()
+    oracle.ref_vx_f32(indiv, X[:, -1], packed_rows, maf_rows, VC, x, N)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(indiv, X, N, Mk, k, sample_rows, sample_maf, budget_s=12.0):
+    """Time the reference algorithm on a SNP subsample and extrapolate to Mk SNPs.
+    Returns (RHS*iters/s, description, threads)."""
+    rng = np.random.default_rng(1)
+    t_rec = cpu_reference_vx(indiv, X, sample_rows[:0], sample_maf[:0], N, k, rng)
+    ms = min(16, sample_rows.shape[0])
+    t = cpu_reference_vx(indiv, X, sample_rows[:ms], sample_maf[:ms], N, k, rng)
+    per_snp = max(t - t_rec, 1e-9) / ms
+    ms2 = int(min(sample_rows.shape[0], max(ms, budget_s / per_snp)))
+    t2 = cpu_reference_vx(indiv, X, sample_rows[:ms2], sample_maf[:ms2], N, k, rng)
+    per_snp = max(t2 - t_rec, 1e-9) / ms2
+    t_matvec = t_rec + per_snp * Mk
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    desc = ("FP32 reference-structure V.x (orc_ref_vx_f32, OpenMP) on %d of %d SNPs x %d individuals, k=%d, "
+            "record ops %.3fs; per-SNP %.3g s extrapolated to all SNPs: %.2f s per PCG iteration"
+            % (ms2, Mk, N, k, t_rec, per_snp, t_matvec))
+    return k / t_matvec, desc, threads
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def run_reference(args, cfg):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    from globe_gb300 import synth
+    from oracle import oracle
+    oracle.build()
+    indiv, X, y, N = make_records(cfg)
+    k = 5
+    rng = np.random.default_rng(2)
+    nsample = 4096 if cfg["N"] >= 50_000 else min(cfg["M"], 4096)
+    G = synth.simulate_genotypes(rng, nsample, N, cfg["maf_lo"], cfg["maf_hi"], cfg["miss"])
+    packed = synth.pack_genotypes(G)
+    alt, miss, maf, _, keep = oracle.bed_stats(packed, N)
+    rows, mafk = packed[keep], maf[keep]
+    Mk = int(round(cfg["M"] * keep.mean()))
+    per_step_budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, desc, threads = cpu_baseline(indiv, X, N, Mk, k, rows, mafk, budget_s=per_step_budget)
+        if s >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {"metric": METRIC, "value": value, "unit": "RHS*iters/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * k / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.config, "shape": cfg["label"], "seed": SEED},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "RHS*iters/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "RHS*iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args, cfg):
+    import torch
+
+    import globe_gb300 as G
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+    prec = G.PREC_MIXED if args.precision == "mixed" else G.PREC_FP64
+    ctx = G.Context(device)
+    indiv, X, y, N = make_records(cfg)
+    ctx.load_records(indiv, X, y, N)
+    Nrec = len(indiv)
+    bps = (N + 3) // 4
+    stride = (bps + 15) // 16 * 16
+    M = cfg["M"]
+    raw = torch.empty((M, stride), dtype=torch.uint8, device="cuda")
+    ctx.synth_bed_dev(raw.data_ptr(), M, N, stride, SEED + 7919 * rank, cfg["maf_lo"], cfg["maf_hi"], cfg["miss"])
+    Mk = ctx.load_bed_dev(raw.data_ptr(), M, stride)
+    # a host copy of some kept-looking rows for the CPU baseline (rank 0)
+    sample_rows = raw[: min(M, 4096)].cpu().numpy()[:, :bps].copy() if rank == 0 else None
+    del raw
+    torch.cuda.empty_cache()
+    ctx.set_vc(G.as_float_vc(VC))
+    k = 5
+    B = torch.empty((k, Nrec), dtype=torch.float64, device="cuda")      # column-major Nrec x k
+    B[: k - 1] = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    B[k - 1] = torch.from_numpy(y).cuda()
+    Xs = torch.zeros_like(B)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    opts = dict(tol=0.0, maxit=args.iters, rule=G.RULE_AIREML, x0mode=G.X0_ZERO, precision=prec)
+
+    def step_dev():
+        return ctx.pcg_dev(B.data_ptr(), Xs.data_ptr(), k, **opts)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step_dev()
+    barrier()
+    clocks = ClockSampler(device)
+    clocks.start()
+    ctx.prof_enable(True)
+    launches0 = ctx.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    rhs_iters = 0
+    for _ in range(args.steps):
+        rhs_iters += step_dev()["rhs_iters"]
+    ev1.record(stream)
+    barrier()
+    launches = ctx.kernel_launches() - launches0
+    t_ms = ev0.elapsed_time(ev1)
+    prof = {kind: ctx.prof_query(kind) for kind in (G._lib.PROF_GRM, G._lib.PROF_GRM_PASS1, G._lib.PROF_GRM_PASS2,
+                                                    G._lib.PROF_PCG_ITER)}
+    ctx.prof_enable(False)
+    clk = clocks.stop()
+    t_max = t_ms
+    total_units = rhs_iters
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        uu = torch.tensor([rhs_iters], device="cuda", dtype=torch.float64)
+        dist.all_reduce(uu, op=dist.ReduceOp.SUM)
+        t_max, total_units = float(tt.item()), float(uu.item())
+    value = total_units / (t_max / 1000.0)
+
+    # e2e through the public API with pinned host buffers
+    hB = torch.empty((k, Nrec), dtype=torch.float64, pin_memory=True)
+    hB.copy_(B.cpu())
+    hX = torch.empty_like(hB).pin_memory()
+    nB, nX = hB.numpy(), hX.numpy()
+    Bf, Xf = nB.T, nX.T          # Fortran-ordered views (Nrec x k)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_units = 0
+    for _ in range(args.steps):
+        Xout, info = ctx.pcg(Bf, out=Xf, **opts)
+        e2e_units += info["rhs_iters"]
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": e2e_units / t_e2e, "unit": "RHS*iters/s", "h2d_bytes_per_step": int(8 * Nrec * k),
+           "d2h_bytes_per_step": int(8 * Nrec * k)}
+
+    # roofline of the dominant GRM kernel (one genotype pass per launch)
+    hbm, bf16, peak_src = load_peaks()
+    n1, ms1 = prof[G._lib.PROF_GRM_PASS1]
+    n2, ms2 = prof[G._lib.PROF_GRM_PASS2]
+    dom = ("k_geno_p2", n2, ms2) if ms2 >= ms1 else ("k_geno_p1", n1, ms1)
+    bytes_per_launch = Mk * bps + (N + Mk) * k * 8
+    avg_s = dom[2] / 1000.0 / max(dom[1], 1)
+    achieved = bytes_per_launch / avg_s / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get("%s:%s:%s" % (args.config, args.precision, dom[0]))
+    ngrm, msgrm = prof[G._lib.PROF_GRM]
+    niter, msiter = prof[G._lib.PROF_PCG_ITER]
+    roof = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_source": peak_src, "traffic": traffic,
+            "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_s * 1000.0, "launches": dom[1],
+            "grm_product_share_of_iteration": (msgrm / msiter) if msiter else None}
+    line = {"metric": METRIC, "value": value, "unit": "RHS*iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == G.PREC_FP64 else "mixed",
+            "data": "synthetic (GPU counter-based genotypes, seeded numpy records)",
+            "config": {"workload": args.config, "shape": cfg["label"], "precision": args.precision,
+                       "iters_per_step": args.iters, "kept_snps": Mk, "records": Nrec,
+                       "l2": "inputs larger than L2 (packed genotypes %.1f GB)" % (Mk * stride / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches)}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle
+        alt, miss, maf, _, keep = oracle.bed_stats(sample_rows, N)
+        v, desc, threads = cpu_baseline(indiv, X, N, Mk, k, sample_rows[keep], maf[keep])
+        line["cpu_baseline"] = {"value": v, "unit": "RHS*iters/s", "cores": threads, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="precision")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--iters", type=int, default=2, help="PCG iterations per step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,13 @@
+"""GB300-native GLOBE: the longitudinal genomic mixed-model solve of
+ahmadazim/GLOBE (runPCGsolver / runAIREML) on one GPU.
+
+The compute path is libglobe_gb300.so (hand-written sm_103a CUDA behind the C
+ABI in include/globe.h); this package is its host-side binding.
+"""
+from ._lib import GlobeError, PREC_FP64, PREC_MIXED, RULE_AIREML, RULE_PCGSOLVER, X0_GIVEN, X0_PRECOND, X0_ZERO
+from .api import (Context, as_float_vc, read_bed, read_grm, read_records, read_vector, run_aireml,
+                  run_pcg_solver, save_vector, trust_region_step)
+
+__all__ = ["Context", "GlobeError", "PREC_FP64", "PREC_MIXED", "RULE_AIREML", "RULE_PCGSOLVER", "X0_GIVEN",
+           "X0_PRECOND", "X0_ZERO", "as_float_vc", "read_bed", "read_grm", "read_records", "read_vector",
+           "run_aireml", "run_pcg_solver", "save_vector", "trust_region_step"]

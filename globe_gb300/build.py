@@ -1,0 +1,76 @@
+"""In-tree build of libglobe_gb300.so and the runPCGsolver / runAIREML programs.
+
+nvcc compiles every translation unit for sm_103a only (one -gencode), in
+parallel, into ``globe_gb300/_build``; the shared library lands in
+``globe_gb300/`` and the command-line programs in ``globe_gb300/bin``.
+"""
+import glob
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+BIN = os.path.join(HERE, "bin")
+LIB = os.path.join(HERE, "libglobe_gb300.so")
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", os.path.join(ROOT, "include"), "-I", SRC,
+          "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
+LIB_SOURCES = ["api.cu", "k_bed.cu", "k_records.cu", "k_grm_geno.cu", "k_grm_dense.cu", "solver.cu",
+               "aireml.cpp", "io.cpp"]
+CLI = {"runPCGsolver": "cli_pcg.cpp", "runAIREML": "cli_aireml.cpp"}
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers():
+    return glob.glob(os.path.join(SRC, "*.cuh")) + glob.glob(os.path.join(SRC, "*.hpp")) + \
+        [os.path.join(ROOT, "include", "globe.h")]
+
+
+def _compile(src):
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    if not _newer(obj, [src] + _headers()):
+        return obj
+    extra = ARCH if src.endswith(".cu") else ["-x", "cu"] + ARCH if False else []
+    cmd = [NVCC] + COMMON + (ARCH if src.endswith(".cu") else []) + ["-c", src, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-6000:]))
+    if r.stderr.strip():
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def build(verbose=True):
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(BIN, exist_ok=True)
+    srcs = [os.path.join(SRC, s) for s in LIB_SOURCES]
+    with ThreadPoolExecutor(max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
+        objs = list(ex.map(_compile, srcs))
+    if _newer(LIB, objs):
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+        subprocess.check_call(cmd)
+    for name, src in CLI.items():
+        s = os.path.join(SRC, src)
+        exe = os.path.join(BIN, name)
+        if os.path.exists(s) and _newer(exe, [s, LIB] + _headers()):
+            cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), s, "-o", exe,
+                   "-L", HERE, "-lglobe_gb300", "-Wl,-rpath,$ORIGIN/.."]
+            subprocess.check_call(cmd)
+    if verbose:
+        print("built", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build()

@@ -1,0 +1,468 @@
+// api.cu -- context, memory and input loading of the C ABI (include/globe.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace globe {
+
+static thread_local std::string g_create_err;
+
+int set_err(globe_ctx* ctx, int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    else g_create_err = buf;
+    return code;
+}
+
+int cuda_err(globe_ctx* ctx, cudaError_t e, const char* what) {
+    return set_err(ctx, e == cudaErrorMemoryAllocation ? GLOBE_ERR_NOMEM : GLOBE_ERR_CUDA, "%s: %s (%s)", what,
+                   cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+int dalloc_bytes(globe_ctx* ctx, void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, GLOBE_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    ctx->dev_bytes += (int64_t)bytes;
+    ctx->allocs.emplace_back(*p, bytes);
+    return GLOBE_OK;
+}
+
+void dfree(globe_ctx* ctx, void* p) {
+    if (!p) return;
+    for (auto it = ctx->allocs.begin(); it != ctx->allocs.end(); ++it)
+        if (it->first == p) {
+            ctx->dev_bytes -= (int64_t)it->second;
+            ctx->allocs.erase(it);
+            break;
+        }
+    cudaFree(p);
+}
+
+int wslot(globe_ctx* ctx, int id, size_t bytes, void** out) {
+    Slot& s = ctx->ws[id];
+    if (s.bytes < bytes) {
+        if (s.p) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(s.p);
+            ctx->dev_bytes -= (int64_t)s.bytes;
+            s.p = nullptr;
+            s.bytes = 0;
+        }
+        size_t want = bytes + bytes / 4 + 256;
+        cudaError_t e = cudaMalloc(&s.p, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            s.p = nullptr;
+            return set_err(ctx, GLOBE_ERR_NOMEM, "workspace cudaMalloc(%zu bytes) failed: %s", want,
+                           cudaGetErrorString(e));
+        }
+        s.bytes = want;
+        ctx->dev_bytes += (int64_t)want;
+    }
+    *out = s.p;
+    return GLOBE_OK;
+}
+
+int after_launch(globe_ctx* ctx, const char* name) {
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(ctx, e, name);
+    return GLOBE_OK;
+}
+
+static void prof_flush(globe_ctx* ctx) {
+    cudaStreamSynchronize(ctx->stream);
+    for (size_t i = 0; i < ctx->prof_used; ++i) {
+        auto& e = ctx->prof_pool[i];
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+            ctx->prof_count[e.kind] += 1;
+            ctx->prof_ms[e.kind] += ms;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    ctx->prof_used = 0;
+}
+
+int prof_begin(globe_ctx* ctx, int kind) {
+    if (!ctx->prof_on || kind < 0 || kind >= GLOBE_PROF_KINDS) return -1;
+    if (ctx->prof_used >= 4096) prof_flush(ctx);
+    if (ctx->prof_used == ctx->prof_pool.size()) {
+        globe_ctx::ProfEv e{kind, nullptr, nullptr};
+        if (cudaEventCreate(&e.a) != cudaSuccess || cudaEventCreate(&e.b) != cudaSuccess) {
+            cudaGetLastError();
+            return -1;
+        }
+        ctx->prof_pool.push_back(e);
+    }
+    int h = (int)ctx->prof_used++;
+    ctx->prof_pool[h].kind = kind;
+    cudaEventRecord(ctx->prof_pool[h].a, ctx->stream);
+    return h;
+}
+
+void prof_end(globe_ctx* ctx, int h) {
+    if (h < 0) return;
+    cudaEventRecord(ctx->prof_pool[h].b, ctx->stream);
+}
+
+static void free_cohort(globe_ctx* ctx) {
+    auto& c = ctx->coh;
+    for (void* p : {(void*)c.X, (void*)c.y, (void*)c.bstart, (void*)c.bind, (void*)c.rind, (void*)c.bn,
+                    (void*)c.bt, (void*)c.btt})
+        dfree(ctx, p);
+    c = Cohort();
+    for (void* p : {(void*)ctx->vinv_X, (void*)ctx->vinv_r, (void*)ctx->uhat, (void*)ctx->f_theta}) dfree(ctx, p);
+    ctx->vinv_X = ctx->vinv_r = ctx->uhat = ctx->f_theta = nullptr;
+    ctx->mme_ok = ctx->fth_ok = false;
+    ctx->precond_ok = false;
+}
+
+static void free_genetic(globe_ctx* ctx) {
+    auto& g = ctx->gen;
+    for (void* p : {(void*)g.geno, (void*)g.zs, (void*)g.f, (void*)g.inv, (void*)g.grm, (void*)g.gdiag})
+        dfree(ctx, p);
+    g = Genetic();
+    ctx->precond_ok = false;
+    ctx->mme_ok = ctx->fth_ok = false;
+}
+
+}  // namespace globe
+
+using namespace globe;
+
+extern "C" {
+
+int globe_create(globe_ctx** out, int device) {
+    if (!out) return set_err(nullptr, GLOBE_ERR_ARG, "globe_create: null output pointer");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return set_err(nullptr, GLOBE_ERR_CUDA, "no CUDA device available (%s)",
+                       e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+    if (device < 0 || device >= n) return set_err(nullptr, GLOBE_ERR_ARG, "device %d out of range [0,%d)", device, n);
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return set_err(nullptr, GLOBE_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+    globe_ctx* ctx = new globe_ctx();
+    ctx->device = device;
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return set_err(nullptr, GLOBE_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    ctx->hpin_n = 1 << 14;
+    e = cudaMallocHost(&ctx->hpin, sizeof(double) * ctx->hpin_n);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return set_err(nullptr, GLOBE_ERR_CUDA, "cudaMallocHost: %s", cudaGetErrorString(e));
+    }
+    *out = ctx;
+    return GLOBE_OK;
+}
+
+void globe_destroy(globe_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& a : ctx->allocs) cudaFree(a.first);
+    for (auto& s : ctx->ws)
+        if (s.p) cudaFree(s.p);
+    if (ctx->hpin) cudaFreeHost(ctx->hpin);
+    for (auto& e : ctx->prof_pool) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* globe_last_error(const globe_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+int globe_get_stream(globe_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return GLOBE_ERR_ARG;
+    *stream = (void*)ctx->stream;
+    return GLOBE_OK;
+}
+
+int globe_synchronize(globe_ctx* ctx) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GLOBE_OK;
+}
+
+int64_t globe_device_bytes(const globe_ctx* ctx) { return ctx ? ctx->dev_bytes : 0; }
+int64_t globe_kernel_launches(const globe_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int globe_prof_enable(globe_ctx* ctx, int on) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    prof_flush(ctx);
+    for (int k = 0; k < GLOBE_PROF_KINDS; ++k) {
+        ctx->prof_count[k] = 0;
+        ctx->prof_ms[k] = 0.0;
+    }
+    ctx->prof_on = on != 0;
+    return GLOBE_OK;
+}
+
+int globe_prof_query(globe_ctx* ctx, int kind, int64_t* count, double* ms) {
+    if (!ctx || kind < 0 || kind >= GLOBE_PROF_KINDS) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    prof_flush(ctx);
+    if (count) *count = ctx->prof_count[kind];
+    if (ms) *ms = ctx->prof_ms[kind];
+    return GLOBE_OK;
+}
+
+int globe_get_dims(const globe_ctx* ctx, int64_t* Nrec, int32_t* N, int32_t* p, int64_t* kept) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (Nrec) *Nrec = ctx->coh.Nrec;
+    if (N) *N = ctx->coh.N;
+    if (p) *p = ctx->coh.p;
+    if (kept) *kept = ctx->gen.src == GSRC_GENO ? ctx->gen.Mk : 0;
+    return GLOBE_OK;
+}
+
+int globe_load_records(globe_ctx* ctx, int64_t Nrec, int32_t N, int32_t p, const int32_t* indiv,
+                       const double* X, const double* y) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (Nrec < 1 || N < 1 || p < 0 || !indiv || !X || !y)
+        return set_err(ctx, GLOBE_ERR_ARG, "globe_load_records: invalid sizes or null pointers");
+    if (Nrec > INT32_MAX) return set_err(ctx, GLOBE_ERR_ARG, "globe_load_records: Nrec exceeds 2^31-1");
+    // blocks = runs of one individual; each individual must form exactly one run
+    std::vector<int32_t> bstart, bind, rind(Nrec);
+    std::vector<uint8_t> seen(N, 0);
+    int32_t maxb = 0;
+    for (int64_t r = 0; r < Nrec; ++r) {
+        int32_t i = indiv[r];
+        if (i < 0 || i >= N)
+            return set_err(ctx, GLOBE_ERR_FORMAT,
+                           "record %lld: individual index %d outside [0,%d) (IDs must be 1..N, N = number of "
+                           "distinct IDs)", (long long)r, i, N);
+        if (r == 0 || indiv[r - 1] != i) {
+            if (seen[i])
+                return set_err(ctx, GLOBE_ERR_FORMAT,
+                               "records of individual %d are not contiguous (records must be grouped by "
+                               "individual)", i + 1);
+            seen[i] = 1;
+            if (!bstart.empty()) maxb = std::max<int32_t>(maxb, (int32_t)(r - bstart.back()));
+            bstart.push_back((int32_t)r);
+            bind.push_back(i);
+        }
+        rind[r] = i;
+    }
+    maxb = std::max<int32_t>(maxb, (int32_t)(Nrec - bstart.back()));
+    if ((int32_t)bind.size() != N)
+        return set_err(ctx, GLOBE_ERR_FORMAT, "%d individuals have records but N = %d", (int)bind.size(), N);
+    bstart.push_back((int32_t)Nrec);
+    for (int64_t e = 0; e < Nrec * (int64_t)(p + 1); ++e)
+        if (!std::isfinite(X[e])) return set_err(ctx, GLOBE_ERR_FORMAT, "non-finite covariate/time value");
+    for (int64_t e = 0; e < Nrec; ++e)
+        if (!std::isfinite(y[e])) return set_err(ctx, GLOBE_ERR_FORMAT, "non-finite phenotype value");
+    free_cohort(ctx);
+    free_genetic(ctx);
+    auto& c = ctx->coh;
+    c.Nrec = Nrec;
+    c.N = N;
+    c.p = p;
+    c.max_block = maxb;
+    GLOBE_RET(dalloc(ctx, &c.X, (size_t)Nrec * (p + 1)));
+    GLOBE_RET(dalloc(ctx, &c.y, (size_t)Nrec));
+    GLOBE_RET(dalloc(ctx, &c.bstart, (size_t)N + 1));
+    GLOBE_RET(dalloc(ctx, &c.bind, (size_t)N));
+    GLOBE_RET(dalloc(ctx, &c.rind, (size_t)Nrec));
+    GLOBE_RET(dalloc(ctx, &c.bn, (size_t)N));
+    GLOBE_RET(dalloc(ctx, &c.bt, (size_t)N));
+    GLOBE_RET(dalloc(ctx, &c.btt, (size_t)N));
+    GLOBE_CK(ctx, cudaMemcpyAsync(c.X, X, sizeof(double) * Nrec * (p + 1), cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(c.y, y, sizeof(double) * Nrec, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(c.bstart, bstart.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(c.bind, bind.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(c.rind, rind.data(), sizeof(int32_t) * Nrec, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_RET(block_moments(ctx));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GLOBE_OK;
+}
+
+int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf,
+                       float max_miss, int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep,
+                       globe_bed_info* info) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int32_t N = ctx->coh.N;
+    if (N < 1) return set_err(ctx, GLOBE_ERR_STATE, "load the record table first (N comes from it)");
+    const int64_t bps = ((int64_t)N + 3) / 4;
+    if (M < 0 || stride < bps || (M > 0 && !d_bed))
+        return set_err(ctx, GLOBE_ERR_ARG, "globe_load_bed_dev: bad M/stride (stride %lld < %lld bytes per SNP)",
+                       (long long)stride, (long long)bps);
+    if (!(min_maf >= 0.0f && min_maf <= 0.5f && max_miss >= 0.0f && max_miss <= 1.0f))
+        return set_err(ctx, GLOBE_ERR_ARG, "Invalid MAF or missing rate thresholds.");
+    free_genetic(ctx);
+    // per-SNP statistics (temporaries where the caller passed NULL)
+    std::vector<void*> tmp;
+    auto need = [&](auto** p, size_t n) -> int {
+        if (*p) return GLOBE_OK;
+        void* q;
+        cudaError_t e = cudaMalloc(&q, n ? n : 16);
+        if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc(stats)");
+        tmp.push_back(q);
+        *p = (std::remove_reference_t<decltype(*p)>)q;
+        return GLOBE_OK;
+    };
+    int rc = GLOBE_OK;
+    if ((rc = need(&d_alt, sizeof(int64_t) * M)) || (rc = need(&d_miss, sizeof(int64_t) * M)) ||
+        (rc = need(&d_keep, (size_t)M))) {
+        for (void* q : tmp) cudaFree(q);
+        return rc;
+    }
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        for (void* q : tmp) cudaFree(q);
+    };
+    rc = bed_stats(ctx, d_bed, M, stride, N, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep);
+    std::vector<uint8_t> keep(M);
+    if (rc == GLOBE_OK && M > 0) {
+        cudaError_t e = cudaMemcpyAsync(keep.data(), d_keep, M, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = cuda_err(ctx, e, "copy keep mask");
+    }
+    if (rc != GLOBE_OK) { cleanup(); return rc; }
+    std::vector<int64_t> idx;
+    idx.reserve(M);
+    for (int64_t s = 0; s < M; ++s)
+        if (keep[s]) idx.push_back(s);
+    auto& g = ctx->gen;
+    g.Mk = (int64_t)idx.size();
+    g.stride = (bps + 15) / 16 * 16;
+    int64_t* d_idx = nullptr;
+    if ((rc = dalloc(ctx, &d_idx, idx.size() + 1)) != GLOBE_OK) { cleanup(); return rc; }
+    if (g.Mk > 0) {
+        cudaError_t e = cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * g.Mk, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) { cleanup(); return cuda_err(ctx, e, "copy kept index"); }
+    }
+    if ((rc = dalloc(ctx, &g.geno, (size_t)g.Mk * g.stride)) || (rc = dalloc(ctx, &g.zs, (size_t)g.Mk * 4)) ||
+        (rc = dalloc(ctx, &g.f, (size_t)g.Mk)) || (rc = dalloc(ctx, &g.inv, (size_t)g.Mk)) ||
+        (rc = dalloc(ctx, &g.gdiag, (size_t)N))) {
+        cleanup();
+        return rc;
+    }
+    if ((rc = bed_compact(ctx, d_bed, stride, d_idx, g.Mk, bps, g.geno, g.stride)) ||
+        (rc = snp_coefs(ctx, d_alt, d_miss, d_idx, g.Mk, N, g.f, g.inv, g.zs))) {
+        cleanup();
+        return rc;
+    }
+    cleanup();
+    dfree(ctx, d_idx);
+    g.src = GSRC_GENO;
+    g.gdiag_ok = false;
+    ctx->precond_ok = false;
+    if (info) {
+        info->M = M;
+        info->kept = g.Mk;
+    }
+    GLOBE_CK(ctx, cudaGetLastError());
+    return GLOBE_OK;
+}
+
+int globe_load_bed(globe_ctx* ctx, const uint8_t* bed, int64_t M, float min_maf, float max_miss,
+                   int64_t* alt_count, int64_t* miss_count, float* maf, float* miss_rate, uint8_t* keep,
+                   globe_bed_info* info) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int32_t N = ctx->coh.N;
+    if (N < 1) return set_err(ctx, GLOBE_ERR_STATE, "load the record table first (N comes from it)");
+    if (M < 0 || (M > 0 && !bed)) return set_err(ctx, GLOBE_ERR_ARG, "globe_load_bed: bad arguments");
+    const int64_t bps = ((int64_t)N + 3) / 4;
+    uint8_t* d_bed = nullptr;
+    int64_t* d_alt = nullptr;
+    int64_t* d_miss = nullptr;
+    float* d_maf = nullptr;
+    float* d_mr = nullptr;
+    uint8_t* d_keep = nullptr;
+    int rc;
+    if ((rc = dalloc(ctx, &d_bed, (size_t)M * bps)) || (rc = dalloc(ctx, &d_alt, (size_t)M)) ||
+        (rc = dalloc(ctx, &d_miss, (size_t)M)) || (rc = dalloc(ctx, &d_maf, (size_t)M)) ||
+        (rc = dalloc(ctx, &d_mr, (size_t)M)) || (rc = dalloc(ctx, &d_keep, (size_t)M)))
+        goto done;
+    if (M > 0) {
+        cudaError_t e = cudaMemcpyAsync(d_bed, bed, (size_t)M * bps, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_err(ctx, e, "copy .bed payload"); goto done; }
+    }
+    rc = globe_load_bed_dev(ctx, d_bed, M, bps, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
+    if (rc == GLOBE_OK && M > 0) {
+        cudaError_t e = cudaSuccess;
+        if (alt_count && e == cudaSuccess) e = cudaMemcpyAsync(alt_count, d_alt, 8 * M, cudaMemcpyDeviceToHost, ctx->stream);
+        if (miss_count && e == cudaSuccess) e = cudaMemcpyAsync(miss_count, d_miss, 8 * M, cudaMemcpyDeviceToHost, ctx->stream);
+        if (maf && e == cudaSuccess) e = cudaMemcpyAsync(maf, d_maf, 4 * M, cudaMemcpyDeviceToHost, ctx->stream);
+        if (miss_rate && e == cudaSuccess) e = cudaMemcpyAsync(miss_rate, d_mr, 4 * M, cudaMemcpyDeviceToHost, ctx->stream);
+        if (keep && e == cudaSuccess) e = cudaMemcpyAsync(keep, d_keep, M, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = cuda_err(ctx, e, "copy SNP statistics");
+    }
+done:
+    cudaStreamSynchronize(ctx->stream);
+    for (void* p : {(void*)d_bed, (void*)d_alt, (void*)d_miss, (void*)d_maf, (void*)d_mr, (void*)d_keep}) dfree(ctx, p);
+    return rc;
+}
+
+int globe_load_grm(globe_ctx* ctx, const float* grm_lt, int32_t N) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->coh.N < 1) return set_err(ctx, GLOBE_ERR_STATE, "load the record table first (N comes from it)");
+    if (N != ctx->coh.N)
+        return set_err(ctx, GLOBE_ERR_ARG, "GRM has N = %d but the record table has %d individuals", N, ctx->coh.N);
+    if (!grm_lt) return set_err(ctx, GLOBE_ERR_ARG, "globe_load_grm: null GRM");
+    free_genetic(ctx);
+    auto& g = ctx->gen;
+    size_t nelt = (size_t)N * (N + 1) / 2;
+    GLOBE_RET(dalloc(ctx, &g.grm, nelt));
+    GLOBE_RET(dalloc(ctx, &g.gdiag, (size_t)N));
+    GLOBE_CK(ctx, cudaMemcpyAsync(g.grm, grm_lt, nelt * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    g.src = GSRC_DENSE;
+    g.gdiag_ok = false;
+    ctx->precond_ok = false;
+    return GLOBE_OK;
+}
+
+int globe_set_vc(globe_ctx* ctx, const double vc[5]) {
+    if (!ctx || !vc) return GLOBE_ERR_ARG;
+    for (int k = 0; k < 5; ++k)
+        if (!std::isfinite(vc[k])) return set_err(ctx, GLOBE_ERR_ARG, "variance component %d is not finite", k);
+    if (!(vc[0] > 0.0)) return set_err(ctx, GLOBE_ERR_ARG, "sig2e must be > 0 (got %g)", vc[0]);
+    bool same = ctx->vc_set;
+    for (int k = 0; k < 5; ++k) same = same && ctx->vc[k] == vc[k];
+    if (same) return GLOBE_OK;
+    std::memcpy(ctx->vc, vc, sizeof(double) * 5);
+    ctx->vc_set = true;
+    ctx->precond_ok = false;
+    ctx->mme_ok = ctx->fth_ok = false;
+    return GLOBE_OK;
+}
+
+int globe_synth_bed_dev(globe_ctx* ctx, uint8_t* d_bed, int64_t M, int32_t N, int64_t stride, uint64_t seed,
+                        float maf_lo, float maf_hi, float miss_rate) {
+    if (!ctx || !d_bed || M < 0 || N < 1 || stride < ((int64_t)N + 3) / 4)
+        return set_err(ctx, GLOBE_ERR_ARG, "globe_synth_bed_dev: bad arguments");
+    cudaSetDevice(ctx->device);
+    return synth_bed(ctx, d_bed, M, N, stride, seed, maf_lo, maf_hi, miss_rate);
+}
+
+}  // extern "C"

@@ -1,0 +1,223 @@
+// internal.cuh -- context state and shared helpers of libglobe_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "globe.h"
+
+namespace globe {
+
+// Device layout of one cohort (all column-major, ld = rows):
+//   X      Nrec x (p+1), time = last column            (double)
+//   y      Nrec                                        (double)
+//   blocks: one per individual, records contiguous;   bstart[N+1], bind[N]
+//           (individual of block b), rind[Nrec] (individual of record r)
+//   moments per block: n, sum t, sum t^2              (double, N each)
+// Genetic source:
+//   genotype: kept SNP rows, `stride` bytes each (multiple of 16), PLINK
+//             2-bit codes; per-SNP zs table zs[s*4 + code] (double) with
+//             zs = (g - 2f) * inv_std, missing -> g = 0
+//   dense:    packed lower triangle float32, N(N+1)/2
+struct Cohort {
+    int64_t Nrec = 0;
+    int32_t N = 0, p = 0;
+    double* X = nullptr;
+    double* y = nullptr;
+    int32_t* bstart = nullptr;
+    int32_t* bind = nullptr;
+    int32_t* rind = nullptr;
+    double* bn = nullptr;
+    double* bt = nullptr;
+    double* btt = nullptr;
+    int32_t max_block = 0;
+    const double* times() const { return X + (size_t)p * Nrec; }
+};
+
+enum GeneticSource { GSRC_NONE = 0, GSRC_GENO = 1, GSRC_DENSE = 2 };
+
+struct Genetic {
+    int src = GSRC_NONE;
+    // genotype source
+    int64_t Mk = 0;          // kept SNPs
+    int64_t stride = 0;      // bytes per SNP row (multiple of 16)
+    uint8_t* geno = nullptr; // Mk x stride
+    double* zs = nullptr;    // Mk x 4
+    double* f = nullptr;     // Mk
+    double* inv = nullptr;   // Mk
+    // dense source
+    float* grm = nullptr;    // N(N+1)/2
+    // both
+    double* gdiag = nullptr; // A_ii
+    bool gdiag_ok = false;
+};
+
+// Growable device workspace slots.
+struct Slot {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+enum SlotId {
+    WS_R, WS_Z, WS_P, WS_VP, WS_ZI, WS_GZ, WS_S1, WS_PART, WS_SCAL, WS_COLS, WS_W,
+    WS_GPART, WS_B, WS_TMP1, WS_TMP2, WS_TMP3, WS_TMP4, WS_H, WS_HSTAR, WS_PROBE,
+    WS_UH, WS_SMALL, WS_IO1, WS_IO2, WS_COUNT
+};
+
+// Scalars kept on the device during a solve (per column, k entries each).
+struct PcgScalars {
+    double* rz;     // r'z
+    double* rz_new;
+    double* pvp;    // p'Vp
+    double* alpha;
+    double* beta;
+    double* rr;     // |r|^2
+    double* bb;     // |b|^2
+};
+
+}  // namespace globe
+
+struct globe_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t dev_bytes = 0;
+    int64_t launches = 0;
+    globe::Cohort coh;
+    globe::Genetic gen;
+    double vc[5] = {0, 0, 0, 0, 0};
+    bool vc_set = false;
+    bool precond_ok = false;      // H built for the current vc
+    globe::Slot ws[globe::WS_COUNT];
+    // MME state (V^-1 X, (X'V^-1X)^-1, V^-1 r, uhat) kept for AIREML terms
+    double* vinv_X = nullptr;
+    double* vinv_r = nullptr;
+    double* uhat = nullptr;
+    double* f_theta = nullptr;    // Nrec x 5, last globe_aireml_grad
+    std::vector<double> xtvx_inv;
+    bool mme_ok = false;
+    bool fth_ok = false;
+    std::vector<std::pair<void*, size_t>> allocs;  // persistent allocations (freed on destroy)
+    double* hpin = nullptr;       // pinned host scratch for per-iteration scalars
+    size_t hpin_n = 0;
+    // event profiling (globe_prof_*)
+    bool prof_on = false;
+    struct ProfEv {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<ProfEv> prof_pool;
+    size_t prof_used = 0;
+    int64_t prof_count[GLOBE_PROF_KINDS] = {0};
+    double prof_ms[GLOBE_PROF_KINDS] = {0};
+};
+
+namespace globe {
+
+int set_err(globe_ctx* ctx, int code, const char* fmt, ...);
+int cuda_err(globe_ctx* ctx, cudaError_t e, const char* what);
+
+// persistent device allocation tracked by the context
+int dalloc_bytes(globe_ctx* ctx, void** p, size_t bytes);
+template <class T>
+int dalloc(globe_ctx* ctx, T** p, size_t n) {
+    return dalloc_bytes(ctx, (void**)p, n * sizeof(T));
+}
+void dfree(globe_ctx* ctx, void* p);
+// workspace slot of at least `bytes`
+int wslot(globe_ctx* ctx, int id, size_t bytes, void** out);
+template <class T>
+int ws(globe_ctx* ctx, int id, size_t n, T** out) {
+    return wslot(ctx, id, n * sizeof(T), (void**)out);
+}
+
+#define GLOBE_CK(ctx, call)                                          \
+    do {                                                             \
+        cudaError_t e__ = (call);                                    \
+        if (e__ != cudaSuccess) return ::globe::cuda_err(ctx, e__, #call); \
+    } while (0)
+
+#define GLOBE_RET(call)                 \
+    do {                                \
+        int rc__ = (call);              \
+        if (rc__ != GLOBE_OK) return rc__; \
+    } while (0)
+
+// launch bookkeeping: count + error check
+int after_launch(globe_ctx* ctx, const char* name);
+#define GLOBE_LAUNCHED(ctx, name) GLOBE_RET(::globe::after_launch(ctx, name))
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// profiling scopes: prof_begin returns a handle (or -1 when off)
+int prof_begin(globe_ctx* ctx, int kind);
+void prof_end(globe_ctx* ctx, int h);
+struct ProfScope {
+    globe_ctx* c;
+    int h;
+    ProfScope(globe_ctx* ctx, int kind) : c(ctx), h(prof_begin(ctx, kind)) {}
+    ~ProfScope() { prof_end(c, h); }
+};
+
+// ---- kernels entry points (defined in the k_*.cu files) ----
+
+// k_bed.cu
+int bed_stats(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, int32_t N,
+              float min_maf, float max_miss, int64_t* d_alt, int64_t* d_miss, float* d_maf,
+              float* d_mr, uint8_t* d_keep);
+int bed_compact(globe_ctx* ctx, const uint8_t* d_bed, int64_t stride_in, const int64_t* d_idx,
+                int64_t Mk, int64_t bps, uint8_t* d_out, int64_t stride_out);
+int snp_coefs(globe_ctx* ctx, const int64_t* d_alt, const int64_t* d_miss, const int64_t* d_idx,
+              int64_t Mk, int32_t N, double* d_f, double* d_inv, double* d_zs);
+int synth_bed(globe_ctx* ctx, uint8_t* d_bed, int64_t M, int32_t N, int64_t stride, uint64_t seed,
+              float maf_lo, float maf_hi, float miss_rate);
+
+// k_records.cu
+int block_moments(globe_ctx* ctx);
+int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H);
+int seg_sums(globe_ctx* ctx, const double* x, const double* z, const double* beta, double* xout,
+             const int32_t* cols, int kact, double* Zi, double* S1);
+int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double* Zi,
+                const double* S1, const int32_t* cols, int kact, double* out, double* dot_out);
+int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, double* r,
+               const double* p, const double* Vp, double* z, const int32_t* cols, int kact,
+               double* rr, double* rz);
+int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z,
+                  const int32_t* cols, int kact, double* rz);
+int col_dots(globe_ctx* ctx, const double* a, const double* b, int64_t n, int64_t lda, int64_t ldb,
+             const int32_t* cols, int kact, double* out);
+int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int kact);
+int xt_mat(globe_ctx* ctx, const double* X, int m1, const double* S, int m2, double* out);
+int sub_mat(globe_ctx* ctx, const double* A, const double* Bm, int m, const double* c, double* out,
+            int kout);
+int bhat_kernel(globe_ctx* ctx, const double* vr, double* bhat);
+int ftheta_kernel(globe_ctx* ctx, const double* vr, const double* uh, double* fth);
+int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen,
+                 double* Y);
+int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double* TY, int numMC,
+                double* out);
+
+// k_grm_geno.cu
+int geno_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
+int geno_diag(globe_ctx* ctx, double* d);
+
+// k_grm_dense.cu
+int dense_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
+int dense_diag(globe_ctx* ctx, double* d);
+
+// solver.cu
+int grm_apply_dev(globe_ctx* ctx, const double* Z, int k, double* out);
+int ensure_gdiag(globe_ctx* ctx);
+int ensure_precond(globe_ctx* ctx);
+int vx_dev(globe_ctx* ctx, const double* x, int k, double* out);
+int pcg_dev(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o,
+            globe_pcg_info* info);
+int reduce_cols(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out);
+
+}  // namespace globe

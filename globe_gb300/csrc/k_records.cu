@@ -1,0 +1,660 @@
+// k_records.cu -- record-level kernels of the LGMM operator and block PCG.
+//
+// Records of one individual form one contiguous block.  All record-level
+// work is per block: one warp owns a block, so segment sums, the 2x2 random
+// intercept/slope term and the block preconditioner fuse without atomics.
+//
+//   V x   = J (sig2g A J' x) + U D U' x + sig2e x          (PCGsolver.cpp:1095-1266)
+//   U D U' x on block b = (D00 s0 + D01 s1) + t (D01 s0 + D11 s1),
+//         s0 = sum x, s1 = sum t x  -- the O(n) form of the O(n^2) loop at
+//         PCGsolver.cpp:1237-1254 (same matrix, different rounding).
+//   Q_b = sig2e I + W C W', W = [1 t], C = D + diag(sig2g A_ii, 0): the block
+//         of computePreconditioner_Block (PCGsolver.cpp:1014-1049).  Its
+//         inverse by Woodbury: Q_b^-1 r = (r - W H W' r) / sig2e with
+//         H = (sig2e I + C W'W)^-1 C, a 2x2 per individual.
+//
+// Reductions are deterministic: per-CTA partials, then a fixed-order reduce.
+#include "internal.cuh"
+
+namespace globe {
+
+constexpr int RB_THREADS = 256;  // 8 warps, one block of records per warp
+constexpr int RB_WARPS = RB_THREADS / 32;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct VC {
+    double e, g, b0, b01, b1;
+};
+__device__ __forceinline__ VC load_vc(const double* vc) { return VC{vc[0], vc[1], vc[2], vc[3], vc[4]}; }
+
+// CTA-level reduction of per-warp values: vals[warp][q] -> part[blockIdx.x + q*gridDim.x]
+// smem layout: sm[q * RB_WARPS + warp]
+__device__ __forceinline__ void cta_partials(double* sm, int nq, double* part) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double a = 0.0;
+#pragma unroll
+        for (int w = 0; w < RB_WARPS; ++w) a += sm[q * RB_WARPS + w];
+        part[blockIdx.x + (size_t)q * gridDim.x] = a;
+    }
+}
+
+// ---------------------------------------------------------------------------
+
+__global__ void k_block_moments(const int32_t* __restrict__ bstart, const double* __restrict__ t,
+                                int32_t nblk, double* bn, double* bt, double* btt) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (b >= nblk) return;
+    const int st = bstart[b], en = bstart[b + 1];
+    double s1 = 0, s2 = 0;
+    for (int r = st + lane; r < en; r += 32) {
+        double tr = t[r];
+        s1 += tr;
+        s2 += tr * tr;
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if (lane == 0) {
+        bn[b] = (double)(en - st);
+        bt[b] = s1;
+        btt[b] = s2;
+    }
+}
+
+int block_moments(globe_ctx* ctx) {
+    auto& c = ctx->coh;
+    k_block_moments<<<div_up(c.N, RB_WARPS), RB_THREADS, 0, ctx->stream>>>(c.bstart, c.times(), c.N,
+                                                                           c.bn, c.bt, c.btt);
+    GLOBE_LAUNCHED(ctx, "k_block_moments");
+    return GLOBE_OK;
+}
+
+// H_b = (sig2e I + C G)^-1 C,  C = [[b0 + g, b01], [b01, b1]],  G = [[n, St], [St, Stt]]
+__global__ void k_build_H(int32_t nblk, const double* __restrict__ bn, const double* __restrict__ bt,
+                          const double* __restrict__ btt, const int32_t* __restrict__ bind,
+                          const double* __restrict__ gdiag, double gconst, VC v, double* __restrict__ H) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    double g = gdiag ? v.g * gdiag[bind[b]] : gconst;
+    double c00 = v.b0 + g, c01 = v.b01, c11 = v.b1;
+    double g00 = bn[b], g01 = bt[b], g11 = btt[b];
+    double m00 = v.e + c00 * g00 + c01 * g01;
+    double m01 = c00 * g01 + c01 * g11;
+    double m10 = c01 * g00 + c11 * g01;
+    double m11 = v.e + c01 * g01 + c11 * g11;
+    double det = m00 * m11 - m01 * m10;
+    double i00 = m11 / det, i01 = -m01 / det, i10 = -m10 / det, i11 = m00 / det;
+    H[4 * b + 0] = i00 * c00 + i01 * c01;
+    H[4 * b + 1] = i00 * c01 + i01 * c11;
+    H[4 * b + 2] = i10 * c00 + i11 * c01;
+    H[4 * b + 3] = i10 * c01 + i11 * c11;
+}
+
+int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H) {
+    VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
+    auto& c = ctx->coh;
+    k_build_H<<<div_up(c.N, 128), 128, 0, ctx->stream>>>(c.N, c.bn, c.bt, c.btt, c.bind, gdiag, gconst, v, H);
+    GLOBE_LAUNCHED(ctx, "k_build_H");
+    return GLOBE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Segment sums (J' x and t-weighted), optionally fused with p = z + beta p.
+
+__global__ void k_seg_sums(int32_t nblk, int64_t ld, int32_t N, const int32_t* __restrict__ bstart,
+                           const int32_t* __restrict__ bind, const double* __restrict__ t,
+                           double* x, const double* __restrict__ z, const double* __restrict__ beta,
+                           const int32_t* __restrict__ cols, int kact, double* __restrict__ Zi,
+                           double* __restrict__ S1) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (b >= nblk) return;
+    const int st = bstart[b], en = bstart[b + 1];
+    const int i = bind[b];
+    for (int c = 0; c < kact; ++c) {
+        const int col = cols ? cols[c] : c;
+        double* xc = x + (size_t)col * ld;
+        double s0 = 0, s1 = 0;
+        if (beta) {
+            const double bb = beta[col];
+            const double* zc = z + (size_t)col * ld;
+            for (int r = st + lane; r < en; r += 32) {
+                double v = zc[r] + bb * xc[r];
+                xc[r] = v;
+                s0 += v;
+                s1 += t[r] * v;
+            }
+        } else {
+            for (int r = st + lane; r < en; r += 32) {
+                double v = xc[r];
+                s0 += v;
+                s1 += t[r] * v;
+            }
+        }
+        s0 = warp_sum(s0);
+        s1 = warp_sum(s1);
+        if (lane == 0) {
+            Zi[i + (size_t)c * N] = s0;
+            if (S1) S1[i + (size_t)c * N] = s1;
+        }
+    }
+}
+
+int seg_sums(globe_ctx* ctx, const double* x, const double* z, const double* beta, double* xout,
+             const int32_t* cols, int kact, double* Zi, double* S1) {
+    auto& c = ctx->coh;
+    // in-place p update: xout must alias x when beta is given
+    double* xx = beta ? xout : const_cast<double*>(x);
+    k_seg_sums<<<div_up(c.N, RB_WARPS), RB_THREADS, 0, ctx->stream>>>(
+        c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), xx, z, beta, cols, kact, Zi, S1);
+    GLOBE_LAUNCHED(ctx, "k_seg_sums");
+    return GLOBE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// out = J GZ + U D U' x + sig2e x  (+ per-column partial dot x'out)
+
+__global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t* __restrict__ bstart,
+                              const int32_t* __restrict__ bind, const double* __restrict__ t, VC v,
+                              const double* __restrict__ x, const double* __restrict__ GZ,
+                              const double* __restrict__ Zi, const double* __restrict__ S1,
+                              const int32_t* __restrict__ cols, int kact, double* __restrict__ out,
+                              double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x * RB_WARPS + warp;
+    const bool live = b < nblk;
+    int st = 0, en = 0, i = 0;
+    if (live) { st = bstart[b]; en = bstart[b + 1]; i = bind[b]; }
+    for (int c = 0; c < kact; ++c) {
+        const int col = cols ? cols[c] : c;
+        double dot = 0;
+        if (live) {
+            const double s0 = Zi[i + (size_t)c * N], s1 = S1[i + (size_t)c * N];
+            const double g = GZ ? GZ[i + (size_t)c * N] : 0.0;
+            const double a0 = g + v.b0 * s0 + v.b01 * s1;
+            const double a1 = v.b01 * s0 + v.b1 * s1;
+            const double* xc = x + (size_t)col * ld;
+            double* oc = out + (size_t)col * ld;
+            for (int r = st + lane; r < en; r += 32) {
+                double xv = xc[r];
+                double o = a0 + t[r] * a1 + v.e * xv;
+                oc[r] = o;
+                dot += xv * o;
+            }
+        }
+        if (part) {
+            dot = warp_sum(dot);
+            if (lane == 0) sm[c * RB_WARPS + warp] = dot;
+        }
+    }
+    if (part) cta_partials(sm, kact, part);
+}
+
+int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double* Zi, const double* S1,
+                const int32_t* cols, int kact, double* out, double* dot_out) {
+    auto& c = ctx->coh;
+    VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
+    int nb = div_up(c.N, RB_WARPS);
+    double* part = nullptr;
+    if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+    size_t sm = dot_out ? sizeof(double) * RB_WARPS * kact : 0;
+    k_vx_assemble<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), v, x,
+                                                       GZ, Zi, S1, cols, kact, out, part);
+    GLOBE_LAUNCHED(ctx, "k_vx_assemble");
+    if (dot_out) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, dot_out));
+    return GLOBE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// x += a p; r -= a Vp; z = Q^-1 r; partial |r|^2 and r'z.
+
+__global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
+                             const double* __restrict__ t, double inv_e, const double* __restrict__ H,
+                             const double* __restrict__ alpha, double* __restrict__ x, double* __restrict__ r,
+                             const double* __restrict__ p, const double* __restrict__ Vp,
+                             double* __restrict__ z, const int32_t* __restrict__ cols, int kact,
+                             double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x * RB_WARPS + warp;
+    const bool live = b < nblk;
+    int st = 0, en = 0;
+    double h00 = 0, h01 = 0, h10 = 0, h11 = 0;
+    if (live) {
+        st = bstart[b];
+        en = bstart[b + 1];
+        h00 = H[4 * b];
+        h01 = H[4 * b + 1];
+        h10 = H[4 * b + 2];
+        h11 = H[4 * b + 3];
+    }
+    for (int c = 0; c < kact; ++c) {
+        const int col = cols ? cols[c] : c;
+        double rr = 0, rz = 0;
+        if (live) {
+            const double a = alpha[col];
+            double* xc = x + (size_t)col * ld;
+            double* rc = r + (size_t)col * ld;
+            const double* pc = p + (size_t)col * ld;
+            const double* vc = Vp + (size_t)col * ld;
+            double s0 = 0, s1 = 0;
+            for (int q = st + lane; q < en; q += 32) {
+                xc[q] += a * pc[q];
+                double rn = rc[q] - a * vc[q];
+                rc[q] = rn;
+                rr += rn * rn;
+                s0 += rn;
+                s1 += t[q] * rn;
+            }
+            s0 = warp_sum(s0);
+            s1 = warp_sum(s1);
+            const double g0 = h00 * s0 + h01 * s1, g1 = h10 * s0 + h11 * s1;
+            double* zc = z + (size_t)col * ld;
+            for (int q = st + lane; q < en; q += 32) {
+                double rn = rc[q];
+                double zv = (rn - g0 - g1 * t[q]) * inv_e;
+                zc[q] = zv;
+                rz += rn * zv;
+            }
+        }
+        rr = warp_sum(rr);
+        rz = warp_sum(rz);
+        if (lane == 0) {
+            sm[c * RB_WARPS + warp] = rr;
+            sm[(kact + c) * RB_WARPS + warp] = rz;
+        }
+    }
+    cta_partials(sm, 2 * kact, part);
+}
+
+int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, double* r, const double* p,
+               const double* Vp, double* z, const int32_t* cols, int kact, double* rr, double* rz) {
+    auto& c = ctx->coh;
+    int nb = div_up(c.N, RB_WARPS);
+    double* part;
+    GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+    size_t sm = sizeof(double) * RB_WARPS * kact * 2;
+    k_pcg_update<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0], H,
+                                                      alpha, x, r, p, Vp, z, cols, kact, part);
+    GLOBE_LAUNCHED(ctx, "k_pcg_update");
+    GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rr));
+    GLOBE_RET(reduce_cols(ctx, part + (size_t)nb * kact, nb, kact, cols, rz));
+    return GLOBE_OK;
+}
+
+// z = Q^-1 r (+ partial r'z)
+__global__ void k_precond_apply(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
+                                const double* __restrict__ t, double inv_e, const double* __restrict__ H,
+                                const double* __restrict__ r, double* __restrict__ z,
+                                const int32_t* __restrict__ cols, int kact, double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x * RB_WARPS + warp;
+    const bool live = b < nblk;
+    int st = 0, en = 0;
+    double h00 = 0, h01 = 0, h10 = 0, h11 = 0;
+    if (live) {
+        st = bstart[b];
+        en = bstart[b + 1];
+        h00 = H[4 * b];
+        h01 = H[4 * b + 1];
+        h10 = H[4 * b + 2];
+        h11 = H[4 * b + 3];
+    }
+    for (int c = 0; c < kact; ++c) {
+        const int col = cols ? cols[c] : c;
+        double rz = 0;
+        if (live) {
+            const double* rc = r + (size_t)col * ld;
+            double s0 = 0, s1 = 0;
+            for (int q = st + lane; q < en; q += 32) {
+                s0 += rc[q];
+                s1 += t[q] * rc[q];
+            }
+            s0 = warp_sum(s0);
+            s1 = warp_sum(s1);
+            const double g0 = h00 * s0 + h01 * s1, g1 = h10 * s0 + h11 * s1;
+            double* zc = z + (size_t)col * ld;
+            for (int q = st + lane; q < en; q += 32) {
+                double zv = (rc[q] - g0 - g1 * t[q]) * inv_e;
+                zc[q] = zv;
+                rz += rc[q] * zv;
+            }
+        }
+        if (part) {
+            rz = warp_sum(rz);
+            if (lane == 0) sm[c * RB_WARPS + warp] = rz;
+        }
+    }
+    if (part) cta_partials(sm, kact, part);
+}
+
+int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z, const int32_t* cols, int kact,
+                  double* rz) {
+    auto& c = ctx->coh;
+    int nb = div_up(c.N, RB_WARPS);
+    double* part = nullptr;
+    if (rz) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+    size_t sm = rz ? sizeof(double) * RB_WARPS * kact : 0;
+    k_precond_apply<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0], H,
+                                                         r, z, cols, kact, part);
+    GLOBE_LAUNCHED(ctx, "k_precond_apply");
+    if (rz) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rz));
+    return GLOBE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Column reductions
+
+// part[j + c*nparts], j < nparts  ->  out[cols ? cols[c] : c]
+__global__ void k_reduce_cols(const double* __restrict__ part, int nparts, const int32_t* __restrict__ cols,
+                              double* __restrict__ out) {
+    __shared__ double sm[256];
+    const int c = blockIdx.x;
+    double a = 0;
+    for (int j = threadIdx.x; j < nparts; j += blockDim.x) a += part[j + (size_t)c * nparts];
+    sm[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[cols ? cols[c] : c] = sm[0];
+}
+
+// out[cols ? cols[c] : c] = sum_j part[j + c*nparts]
+int reduce_cols(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out) {
+    k_reduce_cols<<<kact, 256, 0, ctx->stream>>>(part, nparts, cols, out);
+    GLOBE_LAUNCHED(ctx, "k_reduce_cols");
+    return GLOBE_OK;
+}
+
+// per-column partial dots a_c . b_c over n rows
+__global__ void k_col_dots(const double* __restrict__ a, const double* __restrict__ b, int64_t n, int64_t lda,
+                           int64_t ldb, const int32_t* __restrict__ cols, double* __restrict__ part) {
+    __shared__ double sm[32];
+    const int c = blockIdx.y;
+    const int col = cols ? cols[c] : c;
+    const double* ac = a + (size_t)col * lda;
+    const double* bc = b + (size_t)col * ldb;
+    double acc = 0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        acc += ac[r] * bc[r];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sm[w];
+        part[blockIdx.x + (size_t)c * gridDim.x] = s;
+    }
+}
+
+int col_dots(globe_ctx* ctx, const double* a, const double* b, int64_t n, int64_t lda, int64_t ldb,
+             const int32_t* cols, int kact, double* out) {
+    int nb = div_up(n, 256 * 4);
+    if (nb > 304) nb = 304;
+    if (nb < 1) nb = 1;
+    double* part;
+    GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+    k_col_dots<<<dim3(nb, kact), 256, 0, ctx->stream>>>(a, b, n, lda, ldb, cols, part);
+    GLOBE_LAUNCHED(ctx, "k_col_dots");
+    return reduce_cols(ctx, part, nb, kact, cols, out);
+}
+
+__global__ void k_scal_div(const double* __restrict__ num, const double* __restrict__ den, double* out, int k) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < k) out[c] = (den[c] != 0.0) ? num[c] / den[c] : 0.0;
+}
+
+int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int k) {
+    k_scal_div<<<div_up(k, 128), 128, 0, ctx->stream>>>(num, den, out, k);
+    GLOBE_LAUNCHED(ctx, "k_scal_div");
+    return GLOBE_OK;
+}
+
+// out (m1 x m2) = X' S over Nrec rows; X Nrec x m1, S Nrec x m2.
+__global__ void k_xt_mat(const double* __restrict__ X, int m1, const double* __restrict__ S, int64_t n,
+                         double* __restrict__ part) {
+    __shared__ double sm[32];
+    const int pair = blockIdx.y;
+    const int a = pair % m1, b = pair / m1;
+    const double* xa = X + (size_t)a * n;
+    const double* sb = S + (size_t)b * n;
+    double acc = 0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x)
+        acc += xa[r] * sb[r];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sm[w];
+        part[blockIdx.x + (size_t)pair * gridDim.x] = s;
+    }
+}
+
+int xt_mat(globe_ctx* ctx, const double* X, int m1, const double* S, int m2, double* out) {
+    int64_t n = ctx->coh.Nrec;
+    int nb = div_up(n, 256 * 8);
+    if (nb > 152) nb = 152;
+    if (nb < 1) nb = 1;
+    double* part;
+    GLOBE_RET(ws(ctx, WS_GPART, (size_t)nb * m1 * m2, &part));
+    k_xt_mat<<<dim3(nb, m1 * m2), 256, 0, ctx->stream>>>(X, m1, S, n, part);
+    GLOBE_LAUNCHED(ctx, "k_xt_mat");
+    return reduce_cols(ctx, part, nb, m1 * m2, nullptr, out);
+}
+
+// out[:, j] = A[:, j] - Bm c[:, j],  Bm Nrec x m, c m x kout (column-major)
+__global__ void k_sub_mat(const double* __restrict__ A, const double* __restrict__ Bm, int m,
+                          const double* __restrict__ c, double* __restrict__ out, int kout, int64_t n) {
+    const int j = blockIdx.y;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        double acc = A[r + (size_t)j * n];
+        for (int a = 0; a < m; ++a) acc -= Bm[r + (size_t)a * n] * c[a + (size_t)j * m];
+        out[r + (size_t)j * n] = acc;
+    }
+}
+
+int sub_mat(globe_ctx* ctx, const double* A, const double* Bm, int m, const double* c, double* out, int kout) {
+    int64_t n = ctx->coh.Nrec;
+    int nb = div_up(n, 256);
+    if (nb > 1216) nb = 1216;
+    k_sub_mat<<<dim3(nb, kout), 256, 0, ctx->stream>>>(A, Bm, m, c, out, kout, n);
+    GLOBE_LAUNCHED(ctx, "k_sub_mat");
+    return GLOBE_OK;
+}
+
+// bhat_i = (b0 s0 + b01 s1, b01 s0 + b1 s1)   (compute_bhat, PCGsolver.cpp:1475-1513)
+__global__ void k_bhat(int32_t nblk, const int32_t* __restrict__ bstart, const int32_t* __restrict__ bind,
+                       const double* __restrict__ t, VC v, const double* __restrict__ vr, double* __restrict__ bhat) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (b >= nblk) return;
+    double s0 = 0, s1 = 0;
+    for (int r = bstart[b] + lane; r < bstart[b + 1]; r += 32) {
+        s0 += vr[r];
+        s1 += t[r] * vr[r];
+    }
+    s0 = warp_sum(s0);
+    s1 = warp_sum(s1);
+    if (lane == 0) {
+        int i = bind[b];
+        bhat[2 * i] = v.b0 * s0 + v.b01 * s1;
+        bhat[2 * i + 1] = v.b01 * s0 + v.b1 * s1;
+    }
+}
+
+int bhat_kernel(globe_ctx* ctx, const double* vr, double* bhat) {
+    auto& c = ctx->coh;
+    VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
+    k_bhat<<<div_up(c.N, RB_WARPS), RB_THREADS, 0, ctx->stream>>>(c.N, c.bstart, c.bind, c.times(), v, vr, bhat);
+    GLOBE_LAUNCHED(ctx, "k_bhat");
+    return GLOBE_OK;
+}
+
+// f_theta (compute_f_theta_i, varCompEst.cpp:693-760):
+//  f0 = vr, f1 = uhat_i / sig2g, f2 = w_i, f3 = t w_i + tw_i, f4 = tw_i t
+__global__ void k_ftheta(int32_t nblk, int64_t n, const int32_t* __restrict__ bstart,
+                         const int32_t* __restrict__ bind, const double* __restrict__ t, double inv_g,
+                         const double* __restrict__ vr, const double* __restrict__ uh, double* __restrict__ f) {
+    const int lane = threadIdx.x & 31;
+    const int b = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (b >= nblk) return;
+    const int st = bstart[b], en = bstart[b + 1];
+    double w = 0, tw = 0;
+    for (int r = st + lane; r < en; r += 32) {
+        w += vr[r];
+        tw += t[r] * vr[r];
+    }
+    w = warp_sum(w);
+    tw = warp_sum(tw);
+    const double u = uh[bind[b]] * inv_g;
+    for (int r = st + lane; r < en; r += 32) {
+        f[r] = vr[r];
+        f[n + r] = u;
+        f[2 * n + r] = w;
+        f[3 * n + r] = t[r] * w + tw;
+        f[4 * n + r] = tw * t[r];
+    }
+}
+
+int ftheta_kernel(globe_ctx* ctx, const double* vr, const double* uh, double* fth) {
+    auto& c = ctx->coh;
+    k_ftheta<<<div_up(c.N, RB_WARPS), RB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.bind, c.times(),
+                                                                    1.0 / ctx->vc[1], vr, uh, fth);
+    GLOBE_LAUNCHED(ctx, "k_ftheta");
+    return GLOBE_OK;
+}
+
+// ---- Monte-Carlo probes (sample_Yvs, varCompEst.cpp:775-797) ----------
+
+__device__ __forceinline__ uint64_t pmix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// standard normal number `idx` of stream `seed` (Box-Muller on two 53-bit uniforms)
+__device__ double stream_normal(uint64_t seed, uint64_t idx) {
+    uint64_t pair = idx >> 1;
+    uint64_t h1 = pmix(seed ^ pmix(2 * pair + 1));
+    uint64_t h2 = pmix(seed ^ pmix(2 * pair + 2));
+    double u1 = ((double)(h1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    double u2 = ((double)(h2 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    double rad = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    return (idx & 1) ? rad * s : rad * c;
+}
+
+__global__ void k_probes(int64_t n, int32_t N, const int32_t* __restrict__ rind, const double* __restrict__ t,
+                         double sg, double se, double L00, double L10, double L11,
+                         const double* __restrict__ draws, uint64_t seed, int numMC, double* __restrict__ Y) {
+    const int j = blockIdx.y;
+    const size_t per = 3 * (size_t)N + n;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int i = rind[r];
+        double z1, z2a, z2b, z3;
+        if (draws) {
+            const double* d = draws + (size_t)j * per;
+            z1 = d[i];
+            z2a = d[N + 2 * i];
+            z2b = d[N + 2 * i + 1];
+            z3 = d[3 * (size_t)N + r];
+        } else {
+            const uint64_t base = (uint64_t)j * per;
+            z1 = stream_normal(seed, base + i);
+            z2a = stream_normal(seed, base + N + 2 * i);
+            z2b = stream_normal(seed, base + N + 2 * i + 1);
+            z3 = stream_normal(seed, base + 3 * (uint64_t)N + r);
+        }
+        const double tr = t[r];
+        Y[r + (size_t)j * n] = sg * z1 + se * z3 + z2a * (L00 + L10 * tr) + z2b * L11 * tr;
+    }
+}
+
+int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen, double* Y) {
+    auto& c = ctx->coh;
+    const double* v = ctx->vc;
+    // compute_chol_2x2 (varCompEst.cpp:800-813)
+    double L00 = sqrt(v[2]), L10 = v[3] / L00;
+    double d11 = v[4] - v[3] * v[3] / v[2];
+    if (d11 < 0) d11 = 0;
+    double L11 = sqrt(d11);
+    int nb = div_up(c.Nrec, 256);
+    if (nb > 1216) nb = 1216;
+    k_probes<<<dim3(nb, numMC), 256, 0, ctx->stream>>>(c.Nrec, c.N, c.rind, c.times(), sqrt(v[1]), sqrt(v[0]),
+                                                       L00, L10, L11, gen ? nullptr : draws, seed, numMC, Y);
+    GLOBE_LAUNCHED(ctx, "k_probes");
+    return GLOBE_OK;
+}
+
+// trace terms: for probe j, f~_k from (VR_j, UH_j) and dot with TY_j
+// (estimateTrace_PdV, varCompEst.cpp:955-968).  out[j*5 + k].
+__global__ void k_trace_terms(int32_t nblk, int64_t n, int32_t N, const int32_t* __restrict__ bstart,
+                              const int32_t* __restrict__ bind, const double* __restrict__ t, double inv_g,
+                              const double* __restrict__ VR, const double* __restrict__ UH,
+                              const double* __restrict__ TY, int numMC, double* __restrict__ part) {
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int b = blockIdx.x * RB_WARPS + warp;
+    const bool live = b < nblk;
+    int st = 0, en = 0, i = 0;
+    if (live) { st = bstart[b]; en = bstart[b + 1]; i = bind[b]; }
+    for (int j = 0; j < numMC; ++j) {
+        double acc[5] = {0, 0, 0, 0, 0};
+        if (live) {
+            const double* vr = VR + (size_t)j * n;
+            const double* ty = TY + (size_t)j * n;
+            double w = 0, tw = 0;
+            for (int r = st + lane; r < en; r += 32) {
+                w += vr[r];
+                tw += t[r] * vr[r];
+            }
+            w = warp_sum(w);
+            tw = warp_sum(tw);
+            const double u = UH[i + (size_t)j * N] * inv_g;
+            for (int r = st + lane; r < en; r += 32) {
+                const double y = ty[r], tr = t[r];
+                acc[0] += vr[r] * y;
+                acc[1] += u * y;
+                acc[2] += w * y;
+                acc[3] += (tr * w + tw) * y;
+                acc[4] += tw * tr * y;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            double s = warp_sum(acc[k]);
+            if (lane == 0) sm[(j * 5 + k) * RB_WARPS + warp] = s;
+        }
+    }
+    cta_partials(sm, numMC * 5, part);
+}
+
+int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double* TY, int numMC, double* out) {
+    auto& c = ctx->coh;
+    int nb = div_up(c.N, RB_WARPS);
+    double* part;
+    GLOBE_RET(ws(ctx, WS_GPART, (size_t)nb * numMC * 5, &part));
+    size_t sm = sizeof(double) * RB_WARPS * numMC * 5;
+    if (sm > 48 * 1024) {
+        cudaFuncSetAttribute(k_trace_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    }
+    k_trace_terms<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(),
+                                                       1.0 / ctx->vc[1], VR, UH, TY, numMC, part);
+    GLOBE_LAUNCHED(ctx, "k_trace_terms");
+    return reduce_cols(ctx, part, nb, numMC * 5, nullptr, out);
+}
+
+}  // namespace globe

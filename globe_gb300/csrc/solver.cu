@@ -1,0 +1,523 @@
+// solver.cu -- operator application, block PCG, MME and AIREML terms.
+//
+// Host-side orchestration of the kernels in k_*.cu.  The PCG recurrences,
+// dot products and the small (p+1)-sized systems are FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace globe {
+
+int check_ready(globe_ctx* ctx) {
+    if (ctx->coh.N < 1) return set_err(ctx, GLOBE_ERR_STATE, "no record table loaded");
+    if (ctx->gen.src == GSRC_NONE) return set_err(ctx, GLOBE_ERR_STATE, "no genotypes or GRM loaded");
+    if (!ctx->vc_set) return set_err(ctx, GLOBE_ERR_STATE, "variance components not set");
+    return GLOBE_OK;
+}
+
+int grm_apply_dev(globe_ctx* ctx, const double* Z, int k, double* out) {
+    ProfScope ps(ctx, GLOBE_PROF_GRM);
+    if (ctx->gen.src == GSRC_GENO) {
+        const double scale = ctx->vc[1] * (ctx->gen.Mk > 0 ? 1.0 / (double)ctx->gen.Mk : 0.0);
+        return geno_apply_f64(ctx, Z, k, scale, out);
+    }
+    if (ctx->gen.src == GSRC_DENSE) return dense_apply_f64(ctx, Z, k, ctx->vc[1], out);
+    return set_err(ctx, GLOBE_ERR_STATE, "no genetic relationship source loaded");
+}
+
+int ensure_gdiag(globe_ctx* ctx) {
+    auto& g = ctx->gen;
+    if (g.gdiag_ok) return GLOBE_OK;
+    if (g.src == GSRC_GENO) GLOBE_RET(geno_diag(ctx, g.gdiag));
+    else if (g.src == GSRC_DENSE) GLOBE_RET(dense_diag(ctx, g.gdiag));
+    else return set_err(ctx, GLOBE_ERR_STATE, "no genetic relationship source loaded");
+    g.gdiag_ok = true;
+    return GLOBE_OK;
+}
+
+int ensure_precond(globe_ctx* ctx) {
+    if (ctx->precond_ok) return GLOBE_OK;
+    GLOBE_RET(ensure_gdiag(ctx));
+    double* H;
+    GLOBE_RET(ws(ctx, WS_H, (size_t)ctx->coh.N * 4, &H));
+    GLOBE_RET(build_H(ctx, ctx->gen.gdiag, 0.0, H));
+    ctx->precond_ok = true;
+    return GLOBE_OK;
+}
+
+static double* Hptr(globe_ctx* ctx) { return (double*)ctx->ws[WS_H].p; }
+
+int vx_dev(globe_ctx* ctx, const double* x, int k, double* out) {
+    const int32_t N = ctx->coh.N;
+    double *Zi, *S1, *GZ;
+    GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * k, &Zi));
+    GLOBE_RET(ws(ctx, WS_S1, (size_t)N * k, &S1));
+    GLOBE_RET(ws(ctx, WS_GZ, (size_t)N * k, &GZ));
+    GLOBE_RET(seg_sums(ctx, x, nullptr, nullptr, nullptr, nullptr, k, Zi, S1));
+    GLOBE_RET(grm_apply_dev(ctx, Zi, k, GZ));
+    GLOBE_RET(vx_assemble(ctx, x, GZ, Zi, S1, nullptr, k, out, nullptr));
+    return GLOBE_OK;
+}
+
+__global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ out, int64_t n) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        out[e] = a[e] - b[e];
+}
+
+static int sub_vec(globe_ctx* ctx, const double* a, const double* b, double* out, int64_t n) {
+    int nb = div_up(n, 256);
+    if (nb > 4096) nb = 4096;
+    k_sub<<<nb, 256, 0, ctx->stream>>>(a, b, out, n);
+    GLOBE_LAUNCHED(ctx, "k_sub");
+    return GLOBE_OK;
+}
+
+static int d2h(globe_ctx* ctx, double* h, const double* d, size_t n) {
+    GLOBE_CK(ctx, cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GLOBE_OK;
+}
+
+int pcg_dev(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info) {
+    GLOBE_RET(check_ready(ctx));
+    if (k < 1) return set_err(ctx, GLOBE_ERR_ARG, "number of right-hand sides must be >= 1");
+    if (!o) return set_err(ctx, GLOBE_ERR_ARG, "null PCG options");
+    if (o->precision != GLOBE_PREC_FP64 && o->precision != GLOBE_PREC_MIXED)
+        return set_err(ctx, GLOBE_ERR_ARG, "unknown precision mode %d", o->precision);
+    if (o->precision == GLOBE_PREC_MIXED)
+        return set_err(ctx, GLOBE_ERR_UNSUPPORTED, "mixed precision is not available in this build");
+    if (!(o->tol >= 0) || o->maxit < 0) return set_err(ctx, GLOBE_ERR_ARG, "bad tolerance / iteration cap");
+    auto& c = ctx->coh;
+    const int64_t n = c.Nrec;
+    const int32_t N = c.N;
+    GLOBE_RET(ensure_precond(ctx));
+    double *r, *z, *p, *Vp, *Zi, *GZ, *S1, *scal, *part;
+    int32_t* dcols;
+    GLOBE_RET(ws(ctx, WS_R, (size_t)n * k, &r));
+    GLOBE_RET(ws(ctx, WS_Z, (size_t)n * k, &z));
+    GLOBE_RET(ws(ctx, WS_P, (size_t)n * k, &p));
+    GLOBE_RET(ws(ctx, WS_VP, (size_t)n * k, &Vp));
+    GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * k, &Zi));
+    GLOBE_RET(ws(ctx, WS_GZ, (size_t)N * k, &GZ));
+    GLOBE_RET(ws(ctx, WS_S1, (size_t)N * k, &S1));
+    GLOBE_RET(ws(ctx, WS_SCAL, (size_t)8 * k, &scal));
+    GLOBE_RET(ws(ctx, WS_COLS, (size_t)k, &dcols));
+    GLOBE_RET(ws(ctx, WS_PART, (size_t)std::max<int64_t>(div_up(N, 8), 304) * k * 2, &part));
+    const double* H = Hptr(ctx);
+    double* rz = scal;
+    double* rz2 = scal + k;
+    double* pvp = scal + 2 * k;
+    double* alpha = scal + 3 * k;
+    double* beta = scal + 4 * k;
+    double* rr = scal + 5 * k;
+    double* bb = scal + 6 * k;
+    if ((size_t)4 * k > ctx->hpin_n) return set_err(ctx, GLOBE_ERR_ARG, "too many right-hand sides (%d)", k);
+    double* h_rr = ctx->hpin;
+    double* h_bb = ctx->hpin + k;
+    double* h_pvp = ctx->hpin + 2 * k;
+
+    GLOBE_RET(col_dots(ctx, B, B, n, n, n, nullptr, k, bb));
+    switch (o->x0mode) {
+        case GLOBE_X0_ZERO:
+            GLOBE_CK(ctx, cudaMemsetAsync(X, 0, sizeof(double) * n * k, ctx->stream));
+            GLOBE_CK(ctx, cudaMemcpyAsync(r, B, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
+            break;
+        case GLOBE_X0_PRECOND:
+            GLOBE_RET(precond_apply(ctx, H, B, X, nullptr, k, nullptr));
+            GLOBE_RET(vx_dev(ctx, X, k, Vp));
+            GLOBE_RET(sub_vec(ctx, B, Vp, r, n * k));
+            break;
+        case GLOBE_X0_GIVEN:
+            GLOBE_RET(vx_dev(ctx, X, k, Vp));
+            GLOBE_RET(sub_vec(ctx, B, Vp, r, n * k));
+            break;
+        default:
+            return set_err(ctx, GLOBE_ERR_ARG, "unknown x0 mode %d", o->x0mode);
+    }
+    GLOBE_RET(precond_apply(ctx, H, r, z, nullptr, k, rz));
+    GLOBE_CK(ctx, cudaMemcpyAsync(p, z, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
+    GLOBE_RET(col_dots(ctx, r, r, n, n, n, nullptr, k, rr));
+    GLOBE_CK(ctx, cudaMemcpyAsync(h_bb, bb, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+
+    std::vector<double> nb(k), nr(k);
+    for (int j = 0; j < k; ++j) {
+        nb[j] = std::sqrt(h_bb[j]);
+        nr[j] = std::sqrt(h_rr[j]);
+    }
+    const double small_b = (double)1e-12f;  // PCGsolver.cpp:1365, :1393
+    auto max_ratio = [&]() {
+        double m = 0.0;
+        for (int j = 0; j < k; ++j) {
+            double q = nb[j] > small_b ? nr[j] / nb[j] : 0.0;
+            if (q > m) m = q;
+        }
+        return m;
+    };
+    // Columns with b = 0 have the solution x = 0 and never enter the loop
+    // (the reference divides 0 by 0 there).
+    std::vector<int32_t> cols;
+    for (int j = 0; j < k; ++j)
+        if (h_bb[j] > 0.0) cols.push_back(j);
+        else GLOBE_CK(ctx, cudaMemsetAsync(X + (size_t)j * n, 0, sizeof(double) * n, ctx->stream));
+    std::vector<int32_t> uploaded;
+    double last = max_ratio();
+    const double stag_frac = (double)5e-3f;
+    int stag = 0, it = 0;
+    bool converged = false, stagnated = false;
+    int64_t rhs_iters = 0;
+    if (cols.empty()) converged = true;
+    for (it = 0; it < o->maxit && !cols.empty(); ++it) {
+        const int kact = (int)cols.size();
+        ProfScope iter_scope(ctx, GLOBE_PROF_PCG_ITER);
+        if (cols != uploaded) {
+            GLOBE_CK(ctx, cudaMemcpyAsync(dcols, cols.data(), sizeof(int32_t) * kact, cudaMemcpyHostToDevice, ctx->stream));
+            uploaded = cols;
+        }
+        if (it > 0) GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kact, Zi, S1));
+        else GLOBE_RET(seg_sums(ctx, p, nullptr, nullptr, nullptr, dcols, kact, Zi, S1));
+        GLOBE_RET(grm_apply_dev(ctx, Zi, kact, GZ));
+        GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kact, Vp, pvp));
+        GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
+        GLOBE_RET(pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kact, rr, rz2));
+        GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+        GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+        GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        rhs_iters += kact;
+        for (int j : cols) {
+            if (!(h_pvp[j] > 0.0) || !std::isfinite(h_rr[j]))
+                return set_err(ctx, GLOBE_ERR_NUMERIC, "PCG breakdown in column %d at iteration %d (p'Vp = %g)", j,
+                               it + 1, h_pvp[j]);
+            nr[j] = std::sqrt(h_rr[j]);
+        }
+        if (o->rule == GLOBE_RULE_PCGSOLVER) {
+            double mx = max_ratio();
+            if (mx < o->tol) { converged = true; ++it; break; }
+            double impr = last - mx;
+            if (impr < stag_frac * last) ++stag;
+            else stag = 0;
+            last = mx;
+            if (stag >= 10) { stagnated = true; ++it; break; }
+        } else {
+            bool all = true;
+            for (int j = 0; j < k; ++j)
+                if (h_bb[j] > 0.0 && !(nr[j] < o->tol * nb[j])) { all = false; break; }
+            if (all) { converged = true; ++it; break; }
+        }
+        if (o->mask) {
+            std::vector<int32_t> keep;
+            for (int j : cols)
+                if (!(nr[j] < o->tol * nb[j])) keep.push_back(j);
+            if (keep.empty()) { converged = true; ++it; break; }
+            cols.swap(keep);
+        }
+        GLOBE_RET(scal_alpha(ctx, rz2, rz, beta, k));
+        std::swap(rz, rz2);
+    }
+    if (info) {
+        info->iters = it;
+        info->inner_iters = it;
+        info->rhs_iters = rhs_iters;
+        info->max_rel_res = max_ratio();
+        info->converged = converged ? 1 : 0;
+        info->stagnated = stagnated ? 1 : 0;
+    }
+    return GLOBE_OK;
+}
+
+// (m x m) inverse, Gauss-Jordan with partial pivoting, column-major
+bool small_inverse(std::vector<double>& A, int m) {
+    std::vector<double> I(m * m, 0.0);
+    for (int i = 0; i < m; ++i) I[i * m + i] = 1.0;
+    for (int col = 0; col < m; ++col) {
+        int pr = col;
+        for (int r = col + 1; r < m; ++r)
+            if (std::fabs(A[col * m + r]) > std::fabs(A[col * m + pr])) pr = r;
+        if (A[col * m + pr] == 0.0) return false;
+        if (pr != col)
+            for (int j = 0; j < m; ++j) {
+                std::swap(A[j * m + col], A[j * m + pr]);
+                std::swap(I[j * m + col], I[j * m + pr]);
+            }
+        double d = A[col * m + col];
+        for (int j = 0; j < m; ++j) {
+            A[j * m + col] /= d;
+            I[j * m + col] /= d;
+        }
+        for (int r = 0; r < m; ++r) {
+            if (r == col) continue;
+            double f = A[col * m + r];
+            if (f == 0.0) continue;
+            for (int j = 0; j < m; ++j) {
+                A[j * m + r] -= f * A[j * m + col];
+                I[j * m + r] -= f * I[j * m + col];
+            }
+        }
+    }
+    A.swap(I);
+    return true;
+}
+
+// out = P V = V - V^-1X (X'V^-1X)^-1 X' V  for V (Nrec x m)
+static int project_dev(globe_ctx* ctx, const double* V, int m, double* out) {
+    const int p1 = ctx->coh.p + 1;
+    double* small;
+    GLOBE_RET(ws(ctx, WS_SMALL, (size_t)2 * p1 * m + 64, &small));
+    GLOBE_RET(xt_mat(ctx, ctx->coh.X, p1, V, m, small));
+    std::vector<double> xv(p1 * m), cc(p1 * m);
+    GLOBE_RET(d2h(ctx, xv.data(), small, (size_t)p1 * m));
+    const auto& inv = ctx->xtvx_inv;
+    for (int j = 0; j < m; ++j)
+        for (int a = 0; a < p1; ++a) {
+            double acc = 0.0;
+            for (int b = 0; b < p1; ++b) acc += inv[b * p1 + a] * xv[j * p1 + b];
+            cc[j * p1 + a] = acc;
+        }
+    double* dc = small + (size_t)p1 * m;
+    GLOBE_CK(ctx, cudaMemcpyAsync(dc, cc.data(), sizeof(double) * p1 * m, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_RET(sub_mat(ctx, V, ctx->vinv_X, p1, dc, out, m));
+    return GLOBE_OK;
+}
+
+}  // namespace globe
+
+using namespace globe;
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+template <class F>
+static int host_io(globe_ctx* ctx, const double* in, size_t nin, double* out, size_t nout, F&& body) {
+    double *din, *dout;
+    GLOBE_RET(ws(ctx, WS_IO1, nin, &din));
+    GLOBE_RET(ws(ctx, WS_IO2, nout, &dout));
+    if (in) GLOBE_CK(ctx, cudaMemcpyAsync(din, in, sizeof(double) * nin, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_RET(body(din, dout));
+    GLOBE_CK(ctx, cudaMemcpyAsync(out, dout, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GLOBE_OK;
+}
+
+extern "C" {
+
+int globe_grm_apply_dev(globe_ctx* ctx, const double* d_Z, double* d_out, int k) {
+    if (!ctx || !d_Z || !d_out || k < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    return grm_apply_dev(ctx, d_Z, k, d_out);
+}
+
+int globe_grm_apply(globe_ctx* ctx, const double* Z, double* out, int k) {
+    if (!ctx || !Z || !out || k < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    size_t n = (size_t)ctx->coh.N * k;
+    return host_io(ctx, Z, n, out, n, [&](double* a, double* b) { return grm_apply_dev(ctx, a, k, b); });
+}
+
+int globe_vx_dev(globe_ctx* ctx, const double* d_x, double* d_out, int k) {
+    if (!ctx || !d_x || !d_out || k < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    return vx_dev(ctx, d_x, k, d_out);
+}
+
+int globe_vx(globe_ctx* ctx, const double* x, double* out, int k) {
+    if (!ctx || !x || !out || k < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    size_t n = (size_t)ctx->coh.Nrec * k;
+    return host_io(ctx, x, n, out, n, [&](double* a, double* b) { return vx_dev(ctx, a, k, b); });
+}
+
+int globe_precond_apply(globe_ctx* ctx, const double* r, double* z, int k) {
+    if (!ctx || !r || !z || k < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    GLOBE_RET(ensure_precond(ctx));
+    size_t n = (size_t)ctx->coh.Nrec * k;
+    return host_io(ctx, r, n, z, n, [&](double* a, double* b) {
+        return precond_apply(ctx, (const double*)ctx->ws[WS_H].p, a, b, nullptr, k, nullptr);
+    });
+}
+
+int globe_genetic_diag(globe_ctx* ctx, double* diag) {
+    if (!ctx || !diag) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->coh.N < 1 || ctx->gen.src == GSRC_NONE)
+        return set_err(ctx, GLOBE_ERR_STATE, "records and a genetic source must be loaded");
+    GLOBE_RET(ensure_gdiag(ctx));
+    return d2h(ctx, diag, ctx->gen.gdiag, ctx->coh.N);
+}
+
+int globe_pcg_dev(globe_ctx* ctx, const double* d_B, double* d_X, int k, const globe_pcg_opts* opts,
+                  globe_pcg_info* info) {
+    if (!ctx || !d_B || !d_X) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return pcg_dev(ctx, d_B, d_X, k, opts, info);
+}
+
+int globe_pcg(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* opts, globe_pcg_info* info) {
+    if (!ctx || !B || !X || k < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    size_t n = (size_t)ctx->coh.Nrec * k;
+    double *dB, *dX;
+    GLOBE_RET(ws(ctx, WS_IO1, n, &dB));
+    GLOBE_RET(ws(ctx, WS_IO2, n, &dX));
+    GLOBE_CK(ctx, cudaMemcpyAsync(dB, B, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    if (opts && opts->x0mode == GLOBE_X0_GIVEN)
+        GLOBE_CK(ctx, cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_RET(pcg_dev(ctx, dB, dX, k, opts, info));
+    GLOBE_CK(ctx, cudaMemcpyAsync(X, dX, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GLOBE_OK;
+}
+
+int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat, double* vinv_r,
+              globe_pcg_info* info) {
+    if (!ctx || !opts) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    auto& c = ctx->coh;
+    const int64_t n = c.Nrec;
+    const int32_t N = c.N;
+    const int p1 = c.p + 1, k = c.p + 2;
+    if (!ctx->vinv_X) GLOBE_RET(dalloc(ctx, &ctx->vinv_X, (size_t)n * k));
+    if (!ctx->vinv_r) GLOBE_RET(dalloc(ctx, &ctx->vinv_r, (size_t)n));
+    if (!ctx->uhat) GLOBE_RET(dalloc(ctx, &ctx->uhat, (size_t)N));
+    ctx->mme_ok = ctx->fth_ok = false;
+    double* B;
+    GLOBE_RET(ws(ctx, WS_B, (size_t)n * k, &B));
+    GLOBE_CK(ctx, cudaMemcpyAsync(B, c.X, sizeof(double) * n * p1, cudaMemcpyDeviceToDevice, ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(B + (size_t)n * p1, c.y, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    double* S = ctx->vinv_X;  // [V^-1 X | V^-1 y]
+    GLOBE_RET(pcg_dev(ctx, B, S, k, opts, info));
+    double* small;
+    GLOBE_RET(ws(ctx, WS_SMALL, (size_t)p1 * (p1 + 2) + 64, &small));
+    GLOBE_RET(xt_mat(ctx, c.X, p1, S, k, small));  // [X'V^-1X | X'V^-1y]
+    std::vector<double> xs((size_t)p1 * k);
+    GLOBE_RET(d2h(ctx, xs.data(), small, xs.size()));
+    std::vector<double> A(xs.begin(), xs.begin() + (size_t)p1 * p1);
+    if (!small_inverse(A, p1)) return set_err(ctx, GLOBE_ERR_NUMERIC, "X'V^-1X is singular");
+    std::vector<double> b(p1);
+    for (int a = 0; a < p1; ++a) {
+        double acc = 0;
+        for (int q = 0; q < p1; ++q) acc += A[q * p1 + a] * xs[(size_t)p1 * p1 + q];
+        b[a] = acc;
+    }
+    ctx->xtvx_inv = A;
+    double* dbeta = small + (size_t)p1 * k;
+    GLOBE_CK(ctx, cudaMemcpyAsync(dbeta, b.data(), sizeof(double) * p1, cudaMemcpyHostToDevice, ctx->stream));
+    GLOBE_RET(sub_mat(ctx, S + (size_t)n * p1, S, p1, dbeta, ctx->vinv_r, 1));
+    double *Zi, *S1, *dbhat;
+    GLOBE_RET(ws(ctx, WS_ZI, (size_t)N, &Zi));
+    GLOBE_RET(ws(ctx, WS_S1, (size_t)N, &S1));
+    GLOBE_RET(seg_sums(ctx, ctx->vinv_r, nullptr, nullptr, nullptr, nullptr, 1, Zi, S1));
+    GLOBE_RET(grm_apply_dev(ctx, Zi, 1, ctx->uhat));
+    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)2 * N, &dbhat));
+    GLOBE_RET(bhat_kernel(ctx, ctx->vinv_r, dbhat));
+    if (beta) std::memcpy(beta, b.data(), sizeof(double) * p1);
+    if (uhat) GLOBE_CK(ctx, cudaMemcpyAsync(uhat, ctx->uhat, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    if (bhat) GLOBE_CK(ctx, cudaMemcpyAsync(bhat, dbhat, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vinv_r) GLOBE_CK(ctx, cudaMemcpyAsync(vinv_r, ctx->vinv_r, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->mme_ok = true;
+    return GLOBE_OK;
+}
+
+int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
+                      double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
+    if (!ctx || !opts || numMC < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    if (!ctx->mme_ok) return set_err(ctx, GLOBE_ERR_STATE, "call globe_mme at the current components first");
+    if (!(ctx->vc[1] > 0.0) || !(ctx->vc[2] > 0.0))
+        return set_err(ctx, GLOBE_ERR_ARG, "AIREML needs sig2g > 0 and sig2b0 > 0");
+    auto& c = ctx->coh;
+    const int64_t n = c.Nrec;
+    const int32_t N = c.N;
+    if (!ctx->f_theta) GLOBE_RET(dalloc(ctx, &ctx->f_theta, (size_t)n * 5));
+    double* fth = ctx->f_theta;
+    GLOBE_RET(ftheta_kernel(ctx, ctx->vinv_r, ctx->uhat, fth));
+    double* small;
+    GLOBE_RET(ws(ctx, WS_SMALL, (size_t)numMC * 5 + 64, &small));
+    GLOBE_RET(xt_mat(ctx, ctx->vinv_r, 1, fth, 5, small));
+    double h_first[5];
+    GLOBE_RET(d2h(ctx, h_first, small, 5));
+    // probes Y_v ~ N(0, V*)
+    double *Y, *TY, *VY, *VR, *UH, *Hs, *Zi, *S1;
+    GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * numMC, &Y));
+    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * numMC, &TY));
+    GLOBE_RET(ws(ctx, WS_TMP3, (size_t)n * numMC, &VY));
+    GLOBE_RET(ws(ctx, WS_TMP4, (size_t)n * numMC, &VR));
+    GLOBE_RET(ws(ctx, WS_UH, (size_t)N * numMC, &UH));
+    GLOBE_RET(ws(ctx, WS_HSTAR, (size_t)N * 4, &Hs));
+    if (probes) {
+        double* dd;
+        size_t cnt = (size_t)numMC * (3 * (size_t)N + n);
+        GLOBE_RET(ws(ctx, WS_PROBE, cnt, &dd));
+        GLOBE_CK(ctx, cudaMemcpyAsync(dd, probes, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->stream));
+        GLOBE_RET(probes_build(ctx, dd, numMC, seed, false, Y));
+    } else {
+        GLOBE_RET(probes_build(ctx, nullptr, numMC, seed, true, Y));
+    }
+    // V*^-1 Y by the Woodbury block inverse with g = sig2g (varCompEst.cpp:839-862)
+    GLOBE_RET(build_H(ctx, nullptr, ctx->vc[1], Hs));
+    GLOBE_RET(precond_apply(ctx, Hs, Y, TY, nullptr, numMC, nullptr));
+    GLOBE_CK(ctx, cudaMemcpyAsync(VY, TY, sizeof(double) * n * numMC, cudaMemcpyDeviceToDevice, ctx->stream));
+    globe_pcg_opts o = *opts;
+    o.rule = GLOBE_RULE_AIREML;
+    o.x0mode = GLOBE_X0_GIVEN;
+    GLOBE_RET(pcg_dev(ctx, Y, VY, numMC, &o, info));
+    GLOBE_RET(project_dev(ctx, VY, numMC, VR));
+    GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * numMC, &Zi));
+    GLOBE_RET(ws(ctx, WS_S1, (size_t)N * numMC, &S1));
+    GLOBE_RET(seg_sums(ctx, VR, nullptr, nullptr, nullptr, nullptr, numMC, Zi, S1));
+    GLOBE_RET(grm_apply_dev(ctx, Zi, numMC, UH));
+    GLOBE_RET(ws(ctx, WS_SMALL, (size_t)numMC * 5 + 64, &small));
+    GLOBE_RET(trace_terms(ctx, VR, UH, TY, numMC, small));
+    std::vector<double> tt((size_t)numMC * 5);
+    GLOBE_RET(d2h(ctx, tt.data(), small, tt.size()));
+    double h_trace[5], h_grad[5];
+    for (int q = 0; q < 5; ++q) {
+        double a = 0;
+        for (int j = 0; j < numMC; ++j) a += tt[(size_t)j * 5 + q];
+        h_trace[q] = a / numMC;
+        h_grad[q] = 0.5 * (h_first[q] - h_trace[q]);  // varCompEst.cpp:1006-1010
+    }
+    if (first) std::memcpy(first, h_first, sizeof(h_first));
+    if (trace) std::memcpy(trace, h_trace, sizeof(h_trace));
+    if (grad) std::memcpy(grad, h_grad, sizeof(h_grad));
+    if (f_theta) GLOBE_RET(d2h(ctx, f_theta, fth, (size_t)n * 5));
+    ctx->fth_ok = true;
+    return GLOBE_OK;
+}
+
+int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai, globe_pcg_info* info) {
+    if (!ctx || !opts || !ai) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    if (!ctx->fth_ok) return set_err(ctx, GLOBE_ERR_STATE, "call globe_aireml_grad first");
+    const int64_t n = ctx->coh.Nrec;
+    double *Vf, *Pf, *small;
+    GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * 5, &Vf));
+    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * 5, &Pf));
+    globe_pcg_opts o = *opts;
+    o.rule = GLOBE_RULE_AIREML;
+    o.x0mode = GLOBE_X0_PRECOND;
+    GLOBE_RET(pcg_dev(ctx, ctx->f_theta, Vf, 5, &o, info));
+    GLOBE_RET(project_dev(ctx, Vf, 5, Pf));
+    GLOBE_RET(ws(ctx, WS_SMALL, 64, &small));
+    GLOBE_RET(xt_mat(ctx, ctx->f_theta, 5, Pf, 5, small));
+    double h[25];
+    GLOBE_RET(d2h(ctx, h, small, 25));
+    for (int e = 0; e < 25; ++e) ai[e] = 0.5 * h[e];  // varCompEst.cpp:1038
+    return GLOBE_OK;
+}
+
+}  // extern "C"

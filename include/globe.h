@@ -1,0 +1,285 @@
+/*
+ * globe.h -- C ABI of the GB300-native GLOBE longitudinal genomic mixed-model
+ * solve (libglobe_gb300.so).
+ *
+ * The reference (ahmadazim/GLOBE) has no library interface: its stable
+ * boundary is the runPCGsolver / runAIREML command lines and their files.
+ * Every entry point below replaces one internal function of those programs
+ * and cites it (file:line in the GLOBE source tree).  The command-line
+ * programs shipped here (runPCGsolver, runAIREML) are written on top of this
+ * ABI only.
+ *
+ * Conventions
+ *  - Every call returns an int status: GLOBE_OK (0) or a negative code;
+ *    globe_last_error(ctx) then holds a message.  Nothing calls exit().
+ *  - Matrices are column-major with the leading dimension equal to the row
+ *    count (records, individuals or SNPs).
+ *  - Host buffers are caller-owned and copied; "_dev" entry points take
+ *    device pointers on the context's device and run on the context's stream.
+ *  - One context = one GPU and one CUDA stream.  Calls on one context are not
+ *    reentrant; distinct contexts are independent.
+ *  - Variance components are ordered (sig2e, sig2g, sig2b0, sigb01, sig2b1)
+ *    as in varCompEst.cpp:48-60.
+ */
+#ifndef GLOBE_H
+#define GLOBE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLOBE_OK 0
+#define GLOBE_ERR_ARG (-1)         /* invalid argument / size mismatch */
+#define GLOBE_ERR_CUDA (-2)        /* CUDA runtime error */
+#define GLOBE_ERR_STATE (-3)       /* call order: data or components missing */
+#define GLOBE_ERR_IO (-4)          /* file cannot be opened / read / written */
+#define GLOBE_ERR_FORMAT (-5)      /* malformed input file */
+#define GLOBE_ERR_NOMEM (-6)       /* device allocation failed */
+#define GLOBE_ERR_NUMERIC (-7)     /* breakdown (non-finite or zero curvature) */
+#define GLOBE_ERR_UNSUPPORTED (-8) /* option not available for this input */
+
+/* precision of the GRM product inside the solver */
+#define GLOBE_PREC_FP64 0   /* plain FP64 everywhere (the drop-in path) */
+#define GLOBE_PREC_MIXED 1  /* low-precision GRM product + FP64 refinement */
+
+/* PCG stopping rules */
+#define GLOBE_RULE_PCGSOLVER 0 /* max_j |r_j|/|b_j| < tol, or 10 iterations with
+                                  < 0.5% improvement (PCGsolver.cpp:1381-1415) */
+#define GLOBE_RULE_AIREML 1    /* all_j |r_j| < tol |b_j| (varCompEst.cpp:505-508) */
+
+/* PCG starting points (varCompEst.cpp:453-476) */
+#define GLOBE_X0_ZERO 0      /* x0 = 0 (PCGsolver.cpp:1339-1344) */
+#define GLOBE_X0_PRECOND 1   /* x0 = Q^-1 b ("use_initial_guess") */
+#define GLOBE_X0_GIVEN 2     /* x0 = X on entry ("use_input_initial") */
+
+typedef struct globe_ctx globe_ctx;
+
+typedef struct {
+    double tol;     /* relative residual tolerance (reference: 1e-5) */
+    int maxit;      /* iteration cap (reference: 1000) */
+    int rule;       /* GLOBE_RULE_* */
+    int x0mode;     /* GLOBE_X0_* */
+    int mask;       /* 1: freeze converged columns (per-column masking);
+                       0: every column iterates until the rule stops all */
+    int precision;  /* GLOBE_PREC_* */
+} globe_pcg_opts;
+
+typedef struct {
+    int iters;          /* iterations of the (outer) solve */
+    int inner_iters;    /* low-precision inner iterations (mixed), else = iters */
+    int64_t rhs_iters;  /* sum over iterations of active columns */
+    double max_rel_res; /* max_j |b_j - V x_j| / |b_j| at exit (recurrence) */
+    int converged;      /* 1 if the rule was met (not maxit / stagnation) */
+    int stagnated;      /* 1 if PCGsolver's stagnation stop fired */
+} globe_pcg_info;
+
+typedef struct {
+    int64_t M;       /* SNPs in the .bed */
+    int64_t kept;    /* SNPs passing the MAF / missingness filter */
+} globe_bed_info;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Create a context on `device` (one CUDA stream).  No reference
+ * counterpart: the reference is a single process holding its state in the
+ * structs of PCGsolver.cpp:32-75. */
+int globe_create(globe_ctx** ctx, int device);
+void globe_destroy(globe_ctx* ctx);
+/* Last error message of ctx (or of the failing globe_create when ctx is
+ * NULL).  Replaces the std::cerr + exit(EXIT_FAILURE) convention of
+ * PCGsolver.cpp:338-444. */
+const char* globe_last_error(const globe_ctx* ctx);
+/* The context's cudaStream_t (for events / interop). */
+int globe_get_stream(globe_ctx* ctx, void** stream);
+int globe_synchronize(globe_ctx* ctx);
+/* Device bytes currently held by the context. */
+int64_t globe_device_bytes(const globe_ctx* ctx);
+/* Number of kernels this context has launched (for accounting). */
+int64_t globe_kernel_launches(const globe_ctx* ctx);
+/* Sizes of the loaded inputs (any pointer may be NULL): records, individuals,
+ * covariates, kept SNPs (0 for a dense GRM). */
+int globe_get_dims(const globe_ctx* ctx, int64_t* Nrec, int32_t* N, int32_t* p, int64_t* kept_snps);
+
+/* ---- inputs ----------------------------------------------------------- */
+
+/* Record table: Nrec records of N individuals, p covariates plus time.
+ * indiv: 0-based individual index of each record (the file's INDIV - 1,
+ * PCGsolver.cpp:579); X: Nrec x (p+1) with time as the last column
+ * (PCGsolver.cpp:581); y: phenotype.  Records of one individual must be
+ * contiguous, and every index in 0..N-1 must occur (the reference assumes
+ * both, PCGsolver.cpp:499-519, :1002-1009).  Replaces readInputData
+ * (PCGsolver.cpp:529-587, varCompEst.cpp:199-262). */
+int globe_load_records(globe_ctx* ctx, int64_t Nrec, int32_t N, int32_t p,
+                       const int32_t* indiv, const double* X, const double* y);
+
+/* PLINK .bed payload (the bytes after the 3-byte magic): M SNP rows of
+ * ceil(N/4) bytes, N from globe_load_records.  Computes per-SNP A1 counts,
+ * missing counts, the float32 A1 frequency and missing rate, applies the
+ * filter maf in [min_maf, 1-min_maf], miss_rate <= max_miss -- bit-exact
+ * with prepGenotypeInput (PCGsolver.cpp:615-763) -- and keeps the passing
+ * SNPs in HBM as the genetic relationship source.  Any per-SNP output may
+ * be NULL. */
+int globe_load_bed(globe_ctx* ctx, const uint8_t* bed, int64_t M, float min_maf,
+                   float max_miss, int64_t* alt_count, int64_t* miss_count, float* maf,
+                   float* miss_rate, uint8_t* keep, globe_bed_info* info);
+/* Same from a device buffer of M rows, `stride` bytes apart (stride >=
+ * ceil(N/4)).  Per-SNP outputs are device pointers (may be NULL). */
+int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride,
+                       float min_maf, float max_miss, int64_t* d_alt, int64_t* d_miss,
+                       float* d_maf, float* d_miss_rate, uint8_t* d_keep, globe_bed_info* info);
+
+/* Dense GRM: float32 packed lower triangle, row major with the diagonal,
+ * N(N+1)/2 values (.grm.bin payload).  Replaces readFullGRM
+ * (PCGsolver.cpp:778-809) and readGRM (varCompEst.cpp:270-295). */
+int globe_load_grm(globe_ctx* ctx, const float* grm_lt, int32_t N);
+
+/* Variance components (sig2e, sig2g, sig2b0, sigb01, sig2b1).  sig2e must be
+ * > 0 (the block preconditioner is singular otherwise). */
+int globe_set_vc(globe_ctx* ctx, const double vc[5]);
+
+/* ---- operators -------------------------------------------------------- */
+
+/* out (N x k) = sig2g * A * Z for Z (N x k): the GRM product of
+ * computeVx_multi with multGRM_uhat = true (PCGsolver.cpp:1127-1217,
+ * :1446-1473), genotype branch sig2g/M Zs'(Zs Z) or dense branch. */
+int globe_grm_apply(globe_ctx* ctx, const double* Z, double* out, int k);
+int globe_grm_apply_dev(globe_ctx* ctx, const double* d_Z, double* d_out, int k);
+/* out (Nrec x k) = V x (computeVx_multi, PCGsolver.cpp:1095-1266;
+ * computeVx_multi_VC, varCompEst.cpp:322-352). */
+int globe_vx(globe_ctx* ctx, const double* x, double* out, int k);
+int globe_vx_dev(globe_ctx* ctx, const double* d_x, double* d_out, int k);
+/* z = Q^-1 r with the per-individual block preconditioner
+ * (computePreconditioner_Block + applyPreconditioner, PCGsolver.cpp:991-1093;
+ * varCompEst.cpp:355-450).  Built from the current components. */
+int globe_precond_apply(globe_ctx* ctx, const double* r, double* z, int k);
+/* A_ii (computeGeneticDiagonal, PCGsolver.cpp:924-989). */
+int globe_genetic_diag(globe_ctx* ctx, double* diag);
+
+/* ---- solves ----------------------------------------------------------- */
+
+/* Solve V X = B (Nrec x k) by block PCG (runPCG_multi,
+ * PCGsolver.cpp:1324-1444; runPCG_multi_VC, varCompEst.cpp:453-528).  With
+ * GLOBE_X0_GIVEN, X holds the starting point on entry. */
+int globe_pcg(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* opts,
+              globe_pcg_info* info);
+int globe_pcg_dev(globe_ctx* ctx, const double* d_B, double* d_X, int k,
+                  const globe_pcg_opts* opts, globe_pcg_info* info);
+
+/* Mixed-model equations at the current components (main,
+ * PCGsolver.cpp:262-297; fitMME, varCompEst.cpp:587-685): solves V [X y],
+ * beta = (X'V^-1X)^-1 X'V^-1y, V^-1 r, uhat = sig2g A J' V^-1 r
+ * (compute_uhat, :1446-1473), bhat_i = sum_r V^-1r (sig2b0 + sigb01 t,
+ * sigb01 + sig2b1 t) (compute_bhat, :1475-1513).  Keeps V^-1X and
+ * (X'V^-1X)^-1 for the AIREML terms.  Any output may be NULL. */
+int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat,
+              double* bhat, double* vinv_r, globe_pcg_info* info);
+
+/* AIREML score at the current components, after globe_mme
+ * (computeDerivative_first + estimateTrace_PdV, varCompEst.cpp:693-1012).
+ * probes: numMC x (N + 2N + Nrec) standard normal draws in the order
+ * sample_Yvs consumes them (Z1, Z2, Z3 per probe, varCompEst.cpp:783-786),
+ * or NULL to draw them on the GPU from `seed` (counter-based, reproducible).
+ * f_theta (Nrec x 5, may be NULL) receives dV/dtheta_k V^-1 r; first, trace,
+ * grad (5 each) receive the score terms. */
+int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed,
+                      const globe_pcg_opts* opts, double* f_theta, double* first,
+                      double* trace, double* grad, globe_pcg_info* info);
+/* Average-information matrix AI = 1/2 f' P f (5 x 5) for the f_theta of the
+ * last globe_aireml_grad (computeDerivative_AImat, varCompEst.cpp:1015-1041). */
+int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai,
+                    globe_pcg_info* info);
+
+/* Trust-region step of oneIter_AIREML (varCompEst.cpp:1148-1199): maximise
+ * g'p - p'AI p/2 over p in [-10,10]^5 subject to sum_k AI_kk p_k <= delta,
+ * theta_k + p_k >= 1e-5 (k != 3) and (theta_3+p_3)^2 <= (theta_2+p_2)(theta_4
+ * +p_4) - 1e-3.  The reference solves this with NLopt's MMA (a closed
+ * binary); this is a primal-dual interior-point method written from the
+ * problem statement.  Host-only, FP64.  status: 0 solved, 1 infeasible,
+ * 2 not converged. */
+int globe_trust_region_step(const double theta[5], const double grad[5], const double ai[25],
+                            double delta, double p[5], int* status);
+
+typedef struct {
+    int maxiter;       /* --maxiter (varCompEst.cpp:21, default 50) */
+    double tol;        /* --tol (default 1e-3) */
+    int numMC;         /* --numMC (default 15) */
+    double theta0[5];  /* starting components (varCompEst.cpp:48-52 defaults) */
+    double pcg_tol;    /* PCG tolerance (reference: 1e-5) */
+    int pcg_maxit;     /* reference: 1000 */
+    int precision;     /* GLOBE_PREC_* */
+    int mask;          /* per-column convergence masking */
+    uint64_t seed;     /* probe seed when probes == NULL */
+    const double* probes;  /* optional injected draws, consumed in order */
+    int64_t probes_len;
+} globe_aireml_opts;
+
+typedef struct {
+    int iterations;     /* AIREML iterations run */
+    int converged;
+    double theta[5];    /* final components */
+    double se[5];       /* sqrt(diag(AI^-1)) */
+    double ai[25];
+    double grad[5];
+    int64_t grad_evals; /* gradient evaluations (each one fitMME + trace) */
+    int64_t pcg_rhs_iters;
+} globe_aireml_result;
+
+/* The AIREML loop of runAIREML (main + oneIter_AIREML,
+ * varCompEst.cpp:1148-1497) on the loaded records and dense GRM; progress
+ * is written to `log_path` (NULL: no log) in the reference's .log layout. */
+int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* opts, const char* log_path,
+                     globe_aireml_result* result);
+
+/* ---- files ------------------------------------------------------------ */
+
+/* Record table reader (checkInputs + readInputData, PCGsolver.cpp:465-587):
+ * first call with X == NULL to get Nrec, N, p; second call fills indiv
+ * (0-based), X (Nrec x (p+1), time last) and y. */
+int globe_read_records(const char* path, int64_t* Nrec, int32_t* N, int32_t* p, int32_t* indiv,
+                       double* X, double* y, char* err, int errlen);
+/* saveVector (utils.cpp:18-34): int32 length + float32 payload. */
+int globe_save_vector_f32(const char* path, const double* v, int32_t n);
+/* Same layout with a float64 payload (what the float->double build of the
+ * reference writes; used for full-precision outputs). */
+int globe_save_vector_f64(const char* path, const double* v, int32_t n);
+/* PLINK trio: M = number of lines of <prefix>.bim (PCGsolver.cpp:631-639);
+ * checks the .bed magic (6C 1B 01, SNP-major; :648-664) and that the file
+ * holds M rows of ceil(N/4) bytes. */
+int globe_bed_dims(const char* prefix, int32_t N, int64_t* M, char* err, int errlen);
+/* Reads the M x ceil(N/4) payload after the magic into `payload`. */
+int globe_read_bed(const char* prefix, int32_t N, int64_t M, uint8_t* payload, char* err, int errlen);
+/* <prefix>.grm.bin: N(N+1)/2 float32 (readFullGRM, PCGsolver.cpp:778-809). */
+int globe_read_grm(const char* prefix, int32_t N, float* grm_lt, char* err, int errlen);
+
+/* ---- profiling ---------------------------------------------------------- */
+
+/* CUDA-event timing of the context's own kernels, recorded on its stream.
+ * No reference counterpart (the reference prints wall time per iteration,
+ * varCompEst.cpp:1462-1464). */
+#define GLOBE_PROF_GRM 0        /* one GRM product (all its launches) */
+#define GLOBE_PROF_GRM_PASS1 1  /* genotype pass 1 (w = Zs v) / dense kernel */
+#define GLOBE_PROF_GRM_PASS2 2  /* genotype pass 2 (Zs' w) */
+#define GLOBE_PROF_PCG_ITER 3   /* one block-PCG iteration */
+#define GLOBE_PROF_KINDS 8
+/* on != 0 starts recording (and clears the counters); 0 stops. */
+int globe_prof_enable(globe_ctx* ctx, int on);
+/* Launch count and summed duration (ms) of `kind` since enabling;
+ * synchronises the stream. */
+int globe_prof_query(globe_ctx* ctx, int kind, int64_t* count, double* ms);
+
+/* ---- benchmarking support --------------------------------------------- */
+
+/* Fill d_bed (M rows, `stride` bytes apart) with PLINK-coded genotypes
+ * drawn on the GPU: per SNP an A1 frequency U(maf_lo, maf_hi) (A1 flipped
+ * for half the SNPs), g ~ Binomial(2, f), missing with probability
+ * miss_rate, padding pairs 00.  Counter-based: the same (seed, SNP,
+ * individual) always gives the same genotype.  No reference counterpart. */
+int globe_synth_bed_dev(globe_ctx* ctx, uint8_t* d_bed, int64_t M, int32_t N, int64_t stride,
+                        uint64_t seed, float maf_lo, float maf_hi, float miss_rate);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GLOBE_H */

@@ -1,0 +1,145 @@
+#!/usr/bin/env python3
+"""Make the golden fixtures in tests/golden/ by running the reference itself.
+
+Run in a container that has the GLOBE sources (oracle/build_ref.py builds
+them into oracle/_ref/).  Inputs are written with globe_gb300.synth from fixed
+seeds; the reference programs' outputs are stored next to them:
+
+* ``<case>.{txt,bed,bim,fam,grm.bin}``  -- inputs (record table, PLINK, GRM)
+* ``<case>_ref.npz``                    -- reference outputs:
+    stats_*   per-SNP counts / float32 maf / missing rate / keep from the FP32
+              build with the per-SNP print (runPCGsolver_stats);
+    f32_*     beta / uhat / bhat of the shipped FP32 build (--geno);
+    geno64_*  beta / uhat / bhat of the float->double build (--geno, tol 1e-13);
+    grm64_*   the same with --grm.
+* ``aireml_small_ref.json`` -- runAIREML (float->double build, PCG tol 1e-12,
+  probe draws injected from globe_gb300.synth.normal_stream(PROBE_SEED)):
+  per-iteration gradients, AI matrices, steps, rho, accepted components.
+"""
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from globe_gb300 import synth  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+VC = (0.6, 0.4, 0.4, 0.2, 0.2)
+PROBE_SEED = 5
+AIREML_NUMMC = 4
+AIREML_MAXITER = 6
+
+CASES = {
+    # name: (seed, N, M, record dist, T, miss_rate, edge SNPs)
+    "geno_small": (7, 203, 1000, ("uniform", 3, 10), 5.0, 0.01, True),
+    "tiny": (3, 37, 64, ("uniform", 1, 4), 4.0, 0.05, True),
+}
+
+
+def _vec(fn):
+    b = open(fn, "rb").read()
+    n = int(np.frombuffer(b[:4], np.int32)[0])
+    dt = np.float64 if len(b) - 4 == 8 * n else np.float32
+    return np.frombuffer(b[4:], dt)[:n].copy()
+
+
+def _vcargs(vc):
+    return ["--sig2e", repr(vc[0]), "--sig2g", repr(vc[1]), "--sig2b0", repr(vc[2]), "--sigb01", repr(vc[3]),
+            "--sig2b1", repr(vc[4])]
+
+
+def make_pcg_case(name, seed, N, M, recs, T, miss, edge, tmp):
+    coh = synth.simulate_cohort(seed, N, M, recs, T, miss_rate=miss, edge_snps=edge)
+    pre = synth.write_cohort(HERE, name, coh, grm=True)
+    out = {}
+    r = subprocess.run([os.path.join(REF, "runPCGsolver_stats"), "--input", pre + ".txt", "--output",
+                        os.path.join(tmp, name + "_s"), "--geno", pre] + _vcargs(VC),
+                       capture_output=True, text=True, check=True)
+    rows = [ln.split() for ln in r.stdout.splitlines() if ln.startswith("[snpstat]")]
+    out["stats_alt"] = np.array([int(x[2]) for x in rows], np.int64)
+    out["stats_miss"] = np.array([int(x[3]) for x in rows], np.int64)
+    out["stats_maf"] = np.array([float.fromhex(x[4]) for x in rows], np.float32)
+    out["stats_miss_rate"] = np.array([float.fromhex(x[5]) for x in rows], np.float32)
+    out["stats_keep"] = np.array([int(x[6]) for x in rows], np.uint8)
+    for tag, exe, src in (("f32", "runPCGsolver", ["--geno", pre]), ("geno64", "runPCGsolver64", ["--geno", pre]),
+                          ("grm64", "runPCGsolver64", ["--grm", pre])):
+        o = os.path.join(tmp, name + "_" + tag)
+        subprocess.run([os.path.join(REF, exe), "--input", pre + ".txt", "--output", o] + src + _vcargs(VC),
+                       capture_output=True, text=True, check=True)
+        for v in ("beta", "uhat", "bhat"):
+            out["%s_%s" % (tag, v)] = _vec("%s_%s.bin" % (o, v))
+    np.savez_compressed(os.path.join(HERE, name + "_ref.npz"), **out)
+    print(name, "N=%d Nrec=%d M=%d kept=%d" % (N, coh["Nrec"], M, int(out["stats_keep"].sum())))
+
+
+def _floats(s):
+    return [float(x) for x in s.split()]
+
+
+def parse_aireml_log(text):
+    """Per-iteration blocks of the reference log (17-digit prints)."""
+    its = []
+    for blk in re.split(r"\n-+ Iteration \d+ -+\n", text)[1:]:
+        d = {"gradients": [_floats(m) for m in re.findall(r"Gradient:\s*([^\n]+)", blk)],
+             "ai": [[_floats(l) for l in m.strip().split("\n")] for m in
+                    re.findall(r"AI matrix: \n((?:[^\n]+\n){5})", blk)],
+             "steps": [_floats(m) for m in re.findall(r"Predicted step:\s*([^\n]+)", blk)],
+             "nlopt": [int(m) for m in re.findall(r"NLopt result: (-?\d+)", blk)],
+             "rho": [float(m) for m in re.findall(r"Rho: ([^\n]+)", blk)],
+             "theta_new": [_floats(m) for m in re.findall(r"theta_new: ([^\n]+)", blk)]}
+        m = re.search(r"Estimated variance components:\s*sig2e = ([^,]+), sig2g = ([^,]+), sig2b0 = ([^,]+), "
+                      r"sigb01 = ([^,]+), sig2b1 = ([^\n]+)", blk)
+        d["theta"] = [float(m.group(k)) for k in range(1, 6)] if m else None
+        its.append(d)
+    fin = re.search(r"Final variance components[^\n]*\n((?:[^\n]+\n){5})", text)
+    final = []
+    if fin:
+        for ln in fin.group(1).strip().split("\n"):
+            a, b = ln.split("=")[1].split("\xc2\xb1") if "\xc2\xb1" in ln else ln.split("=")[1].split("±")
+            final.append([float(a), float(b)])
+    return its, final
+
+
+def make_aireml_case(tmp):
+    name = "aireml_small"
+    vc = (0.6, 0.4, 0.4, 0.05, 0.2)
+    coh = synth.simulate_cohort(22, 300, 1500, ("poisson", 5), 10.0, maf_lo=0.01, miss_rate=0.0, vc=vc)
+    pre = os.path.join(HERE, name)
+    synth.write_record_table(pre + ".txt", coh)
+    synth.write_grm_bin(pre, synth.grm_from_packed(coh["packed"], coh["N"]))
+    per = AIREML_NUMMC * (3 * coh["N"] + coh["Nrec"])
+    probe_file = os.path.join(tmp, "probes.bin")
+    synth.normal_stream(PROBE_SEED, per * 200).tofile(probe_file)
+    env = dict(os.environ, GLOBE_PROBE_FILE=probe_file)
+    out = os.path.join(tmp, name)
+    subprocess.run([os.path.join(REF, "runAIREML64"), pre + ".txt", pre, out, "--numMC", str(AIREML_NUMMC),
+                    "--maxiter", str(AIREML_MAXITER)], env=env, capture_output=True, text=True, check=True)
+    text = open(out + ".log", encoding="utf-8", errors="replace").read()
+    its, final = parse_aireml_log(text)
+    with open(os.path.join(HERE, name + "_ref.json"), "w") as f:
+        json.dump({"numMC": AIREML_NUMMC, "maxiter": AIREML_MAXITER, "probe_seed": PROBE_SEED,
+                   "pcg_tol": 1e-12, "theta0": [0.5, 0.30000001192092896, 0.20000000298023224,
+                                                 0.10000000149011612, 0.10000000149011612],
+                   "N": coh["N"], "Nrec": coh["Nrec"], "iterations": its, "final": final}, f, indent=1)
+    print(name, "N=%d Nrec=%d iterations=%d" % (coh["N"], coh["Nrec"], len(its)))
+
+
+def main():
+    if not os.path.exists(os.path.join(REF, "runPCGsolver64")):
+        sys.exit("build the reference first: python oracle/build_ref.py")
+    tmp = "/tmp/globe_golden"
+    os.makedirs(tmp, exist_ok=True)
+    for name, args in CASES.items():
+        make_pcg_case(name, *args, tmp)
+    if os.path.exists(os.path.join(REF, "runAIREML64")):
+        make_aireml_case(tmp)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,71 @@
+"""Shared test helpers: golden cases, cohorts and comparison metrics."""
+import json
+import os
+
+import numpy as np
+
+from globe_gb300 import synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+VC = (0.6, 0.4, 0.4, 0.2, 0.2)
+VC_F = tuple(float(np.float32(v)) for v in VC)   # as std::stof parses them
+
+
+def rel(a, b):
+    """max |a-b| / max |b|."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    d = np.abs(b).max()
+    return float(np.abs(a - b).max() / (d if d > 0 else 1.0))
+
+
+def read_bed_payload(prefix, N):
+    raw = np.fromfile(prefix + ".bed", np.uint8)
+    assert list(raw[:3]) == [0x6C, 0x1B, 0x01]
+    bps = (N + 3) // 4
+    M = (raw.size - 3) // bps
+    return raw[3:3 + M * bps].reshape(M, bps)
+
+
+def parse_records_py(path):
+    """Independent numpy parse of the record table (named columns first)."""
+    with open(path) as f:
+        hdr = f.readline().split()
+        rows = [l.split() for l in f if l.strip()]
+    a = np.array(rows, dtype=np.float64)
+    ci, cp, ct = hdr.index("INDIV"), hdr.index("PHENO"), hdr.index("TIMES")
+    cov = [j for j in range(len(hdr)) if j not in (ci, cp, ct)]
+    ids = a[:, ci].astype(int)
+    N = len(set(ids.tolist()))
+    X = np.column_stack([a[:, j] for j in cov] + [a[:, ct]])
+    return (ids - 1).astype(np.int32), np.asfortranarray(X), a[:, cp].copy(), N
+
+
+def golden_case(name):
+    pre = os.path.join(GOLDEN, name)
+    indiv, X, y, N = parse_records_py(pre + ".txt")
+    d = dict(prefix=pre, indiv=indiv, X=X, y=y, N=N, Nrec=len(indiv))
+    if os.path.exists(pre + ".bed"):
+        d["packed"] = read_bed_payload(pre, N)
+    if os.path.exists(pre + ".grm.bin"):
+        d["grm"] = np.fromfile(pre + ".grm.bin", np.float32)
+    ref = pre + "_ref.npz"
+    if os.path.exists(ref):
+        d["ref"] = dict(np.load(ref))
+    js = pre + "_ref.json"
+    if os.path.exists(js):
+        d["ref"] = json.load(open(js))
+    return d
+
+
+def aireml_probes(case, n_evals):
+    ref = case["ref"]
+    per = ref["numMC"] * (3 * case["N"] + case["Nrec"])
+    return synth.normal_stream(ref["probe_seed"], per * n_evals), per
+
+
+def cohort(seed, N, M, recs=("uniform", 3, 10), T=5.0, miss=0.01, edge=False, maf_lo=0.05):
+    coh = synth.simulate_cohort(seed, N, M, recs, T, maf_lo=maf_lo, miss_rate=miss, edge_snps=edge)
+    coh["X"] = np.asfortranarray(np.column_stack([coh["cov"], coh["times"]]))
+    return coh

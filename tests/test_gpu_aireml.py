@@ -1,0 +1,60 @@
+"""AIREML terms and loop on the GPU vs the reference run (golden, probes
+injected) and the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import globe_gb300 as G
+from helpers import aireml_probes, golden_case, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case(gctx):
+    c = golden_case("aireml_small")
+    gctx.load_records(c["indiv"], c["X"], c["y"], c["N"])
+    gctx.load_grm(c["grm"], c["N"])
+    return c
+
+
+def test_first_evaluation_matches_reference(gctx, orc, case):
+    ref = case["ref"]
+    probes, per = aireml_probes(case, 1)
+    gctx.set_vc(ref["theta0"])
+    tol = ref["pcg_tol"]
+    gctx.mme(tol=tol, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND)
+    g = gctx.aireml_grad(ref["numMC"], probes=probes, tol=tol)
+    ai = gctx.aireml_ai(tol=tol)
+    it1 = ref["iterations"][0]
+    assert rel(g["grad"], it1["gradients"][0]) < 1e-8
+    assert rel(ai, np.array(it1["ai"][0])) < 1e-8
+    s = orc.Solver(case["indiv"], case["X"], case["y"], case["N"], ref["theta0"], grm_lt=case["grm"])
+    s.mme(tol, rule=1, x0mode=1)
+    og = s.aireml_grad(probes, ref["numMC"], tol)
+    assert rel(g["first"], og["first"]) < 1e-9 and rel(g["trace"], og["trace"]) < 1e-9
+    assert rel(g["f_theta"], og["f_theta"]) < 1e-9
+
+
+def test_device_probes_are_reproducible(gctx, case):
+    th = case["ref"]["theta0"]
+    gctx.set_vc(th)
+    gctx.mme(tol=1e-10, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND)
+    a = gctx.aireml_grad(8, seed=77, tol=1e-10)["grad"]
+    b = gctx.aireml_grad(8, seed=77, tol=1e-10)["grad"]
+    c = gctx.aireml_grad(8, seed=78, tol=1e-10)["grad"]
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+
+
+def test_loop_follows_reference_trajectory(gctx, case, tmp_path):
+    ref = case["ref"]
+    probes, per = aireml_probes(case, 60)
+    log = os.path.join(str(tmp_path), "a.log")
+    r = gctx.aireml_run(theta0=ref["theta0"], maxiter=ref["maxiter"], numMC=ref["numMC"], pcg_tol=ref["pcg_tol"],
+                        probes=probes, log_path=log)
+    assert r["iterations"] == ref["maxiter"]
+    assert rel(r["theta"], ref["iterations"][-1]["theta"]) < 1e-5
+    assert rel(r["se"], [f[1] for f in ref["final"]]) < 1e-4
+    text = open(log).read()
+    assert "Final variance components" in text and text.count("Rho:") == sum(len(i["rho"]) for i in ref["iterations"])

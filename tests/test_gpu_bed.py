@@ -1,0 +1,42 @@
+"""PLINK statistics and filter on the GPU: bit-exact with the reference."""
+import numpy as np
+import pytest
+
+from globe_gb300 import Context
+from helpers import cohort, golden_case
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["geno_small", "tiny"])
+def test_stats_bit_exact_vs_reference(gctx, name):
+    c = golden_case(name)
+    gctx.load_records(c["indiv"], c["X"], c["y"], c["N"])
+    st = gctx.load_bed(c["packed"])
+    r = c["ref"]
+    assert np.array_equal(st["alt"], r["stats_alt"])
+    assert np.array_equal(st["miss"], r["stats_miss"])
+    assert np.array_equal(st["maf"].view(np.uint32), r["stats_maf"].view(np.uint32))
+    assert np.array_equal(st["miss_rate"].view(np.uint32), r["stats_miss_rate"].view(np.uint32))
+    assert np.array_equal(st["keep"], r["stats_keep"].astype(bool))
+    assert st["kept"] == int(r["stats_keep"].sum())
+
+
+@pytest.mark.parametrize("N", [61, 62, 63, 64, 65, 131])
+@pytest.mark.parametrize("thr", [(0.01, 0.2), (0.0, 1.0), (0.2, 0.05), (0.5, 0.0)])
+def test_stats_vs_oracle_all_phantom_counts(gctx, orc, N, thr):
+    coh = cohort(100 + N, N, 203, recs=("uniform", 1, 3), miss=0.08, edge=True)
+    gctx.load_records(coh["indiv"], coh["X"], coh["y"], N)
+    st = gctx.load_bed(coh["packed"], *thr)
+    alt, miss, maf, mr, keep = orc.bed_stats(coh["packed"], N, *thr)
+    assert np.array_equal(st["alt"], alt) and np.array_equal(st["miss"], miss)
+    assert np.array_equal(st["maf"].view(np.uint32), maf.view(np.uint32))
+    assert np.array_equal(st["miss_rate"].view(np.uint32), mr.view(np.uint32))
+    assert np.array_equal(st["keep"], keep)
+
+
+def test_no_snp_passes(gctx):
+    coh = cohort(5, 40, 16, miss=0.0)
+    gctx.load_records(coh["indiv"], coh["X"], coh["y"], 40)
+    st = gctx.load_bed(coh["packed"], 0.5, 0.0)   # maf must be exactly 0.5
+    assert st["kept"] == int(st["keep"].sum())

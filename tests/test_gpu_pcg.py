@@ -1,0 +1,85 @@
+"""Block PCG on the GPU (runPCG_multi / runPCG_multi_VC) vs the oracle."""
+import numpy as np
+import pytest
+
+import globe_gb300 as G
+from helpers import VC_F, cohort, golden_case, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup(gctx, orc):
+    c = golden_case("geno_small")
+    gctx.load_records(c["indiv"], c["X"], c["y"], c["N"])
+    gctx.load_bed(c["packed"])
+    gctx.set_vc(VC_F)
+    s = orc.Solver(c["indiv"], c["X"], c["y"], c["N"], VC_F, packed=c["packed"])
+    s.precond_build()
+    B = np.column_stack([c["X"], c["y"]])
+    return gctx, s, B
+
+
+def test_rule_pcgsolver_matches_oracle(setup):
+    ctx, s, B = setup
+    X, info = ctx.pcg(B, tol=1e-12, rule=G.RULE_PCGSOLVER)
+    Xo, it = s.pcg(B, 1e-12, rule=0)
+    assert abs(info["iters"] - it) <= 1
+    assert rel(X, Xo) < 1e-9
+    assert info["converged"] and info["rhs_iters"] == B.shape[1] * info["iters"]
+
+
+@pytest.mark.parametrize("x0mode", [G.X0_ZERO, G.X0_PRECOND])
+def test_rule_aireml_x0_modes(setup, x0mode):
+    ctx, s, B = setup
+    X, info = ctx.pcg(B, tol=1e-11, rule=G.RULE_AIREML, x0mode=x0mode)
+    Xo, it = s.pcg(B, 1e-11, rule=1, x0mode=x0mode)
+    assert abs(info["iters"] - it) <= 1
+    assert rel(X, Xo) < 1e-8
+    r = B - ctx.vx(X)
+    assert np.all(np.linalg.norm(r, axis=0) < 1.01e-11 * np.linalg.norm(B, axis=0))
+
+
+def test_given_start_point(setup):
+    ctx, s, B = setup
+    X1, _ = ctx.pcg(B, tol=1e-4, rule=G.RULE_AIREML)
+    X2, info = ctx.pcg(B, X0=X1, tol=1e-11, rule=G.RULE_AIREML)
+    Xo, _ = s.pcg(B, 1e-11, rule=1, x0mode=2, X0=X1)
+    assert rel(X2, Xo) < 1e-8
+
+
+def test_masking_freezes_converged_columns(setup):
+    ctx, s, B = setup
+    B2 = B.copy()
+    B2[:, 0] *= 1e-3      # columns converge at different iterations
+    X, info = ctx.pcg(B2, tol=1e-10, rule=G.RULE_AIREML, mask=True)
+    Xf, info_f = ctx.pcg(B2, tol=1e-10, rule=G.RULE_AIREML, mask=False)
+    assert info["rhs_iters"] <= info_f["rhs_iters"]
+    r = B2 - ctx.vx(X)
+    assert np.all(np.linalg.norm(r, axis=0) < 1.01e-10 * np.linalg.norm(B2, axis=0))
+    assert rel(X, Xf) < 1e-7
+
+
+def test_zero_rhs_column_and_cap(setup):
+    ctx, s, B = setup
+    B2 = B.copy()
+    B2[:, 2] = 0.0
+    X, info = ctx.pcg(B2, tol=1e-10, rule=G.RULE_AIREML)
+    assert np.all(X[:, 2] == 0.0) and np.all(np.isfinite(X))
+    X3, info3 = ctx.pcg(B, tol=1e-14, maxit=3, rule=G.RULE_AIREML)
+    assert info3["iters"] == 3 and not info3["converged"]
+
+
+def test_dense_and_odd_sizes(gctx, orc):
+    from globe_gb300 import synth
+    coh = cohort(21, 131, 257, recs=("uniform", 1, 6), miss=0.03)
+    grm = synth.grm_from_packed(coh["packed"], 131)
+    gctx.load_records(coh["indiv"], coh["X"], coh["y"], 131)
+    gctx.load_grm(grm, 131)
+    gctx.set_vc(VC_F)
+    s = orc.Solver(coh["indiv"], coh["X"], coh["y"], 131, VC_F, grm_lt=grm)
+    s.precond_build()
+    B = np.column_stack([coh["X"], coh["y"]])
+    X, info = gctx.pcg(B, tol=1e-12, rule=G.RULE_PCGSOLVER)
+    Xo, it = s.pcg(B, 1e-12, rule=0)
+    assert rel(X, Xo) < 1e-9
