@@ -89,6 +89,7 @@ SIGNATURES = {
     "globe_bed_dims": (C.c_int, [C.c_char_p, C.c_int32, _i64p, C.c_char_p, C.c_int]),
     "globe_read_bed": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, _u8p, C.c_char_p, C.c_int]),
     "globe_read_grm": (C.c_int, [C.c_char_p, C.c_int32, _fp, C.c_char_p, C.c_int]),
+    "globe_set_precision": (C.c_int, [_vp, C.c_int]),
     "globe_prof_enable": (C.c_int, [_vp, C.c_int]),
     "globe_prof_query": (C.c_int, [_vp, C.c_int, _i64p, _dp]),
     "globe_synth_bed_dev": (C.c_int, [_vp, _vp, C.c_int64, C.c_int32, C.c_int64, C.c_uint64, C.c_float, C.c_float,

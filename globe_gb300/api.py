@@ -128,6 +128,9 @@ class Context:
         assert g.size == N * (N + 1) // 2
         self._ck(self._L.globe_load_grm(self.h, _p(g, C.c_float), N))
 
+    def set_precision(self, precision):
+        self._ck(self._L.globe_set_precision(self.h, precision))
+
     def set_vc(self, vc):
         v = np.ascontiguousarray(vc, dtype=np.float64)
         self._ck(self._L.globe_set_vc(self.h, _p(v)))

@@ -133,7 +133,7 @@ static void free_cohort(globe_ctx* ctx) {
 
 static void free_genetic(globe_ctx* ctx) {
     auto& g = ctx->gen;
-    for (void* p : {(void*)g.geno, (void*)g.zs, (void*)g.f, (void*)g.inv, (void*)g.grm, (void*)g.gdiag})
+    for (void* p : {(void*)g.geno, (void*)g.zs, (void*)g.f, (void*)g.inv, (void*)g.grm, (void*)g.gdiag, (void*)g.gt})
         dfree(ctx, p);
     g = Genetic();
     ctx->precond_ok = false;
@@ -454,6 +454,14 @@ int globe_set_vc(globe_ctx* ctx, const double vc[5]) {
     ctx->vc_set = true;
     ctx->precond_ok = false;
     ctx->mme_ok = ctx->fth_ok = false;
+    return GLOBE_OK;
+}
+
+int globe_set_precision(globe_ctx* ctx, int precision) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (precision != GLOBE_PREC_FP64 && precision != GLOBE_PREC_MIXED)
+        return set_err(ctx, GLOBE_ERR_ARG, "unknown precision mode %d", precision);
+    ctx->prec = precision;
     return GLOBE_OK;
 }
 

@@ -51,6 +51,10 @@ struct Genetic {
     double* zs = nullptr;    // Mk x 4
     double* f = nullptr;     // Mk
     double* inv = nullptr;   // Mk
+    // individual-major copy for the tensor-core pass 2 (built on first use):
+    // N rows of strideT bytes, byte b = SNPs 4b..4b+3, padding codes 11
+    uint8_t* gt = nullptr;
+    int64_t strideT = 0;
     // dense source
     float* grm = nullptr;    // N(N+1)/2
     // both
@@ -67,7 +71,8 @@ struct Slot {
 enum SlotId {
     WS_R, WS_Z, WS_P, WS_VP, WS_ZI, WS_GZ, WS_S1, WS_PART, WS_SCAL, WS_COLS, WS_W,
     WS_GPART, WS_B, WS_TMP1, WS_TMP2, WS_TMP3, WS_TMP4, WS_H, WS_HSTAR, WS_PROBE,
-    WS_UH, WS_SMALL, WS_IO1, WS_IO2, WS_COUNT
+    WS_UH, WS_SMALL, WS_IO1, WS_IO2,
+    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_COUNT
 };
 
 // Scalars kept on the device during a solve (per column, k entries each).
@@ -93,6 +98,7 @@ struct globe_ctx {
     globe::Genetic gen;
     double vc[5] = {0, 0, 0, 0, 0};
     bool vc_set = false;
+    int prec = GLOBE_PREC_FP64;   // precision of operator calls (globe_set_precision / PCG options)
     bool precond_ok = false;      // H built for the current vc
     globe::Slot ws[globe::WS_COUNT];
     // MME state (V^-1 X, (X'V^-1X)^-1, V^-1 r, uhat) kept for AIREML terms
@@ -210,6 +216,11 @@ int geno_diag(globe_ctx* ctx, double* d);
 // k_grm_dense.cu
 int dense_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 int dense_diag(globe_ctx* ctx, double* d);
+
+// k_tc_geno.cu
+int ensure_gt(globe_ctx* ctx);
+int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
+int tc_check_error(globe_ctx* ctx);
 
 // solver.cu
 int grm_apply_dev(globe_ctx* ctx, const double* Z, int k, double* out);

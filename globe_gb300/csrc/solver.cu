@@ -22,6 +22,7 @@ int grm_apply_dev(globe_ctx* ctx, const double* Z, int k, double* out) {
     ProfScope ps(ctx, GLOBE_PROF_GRM);
     if (ctx->gen.src == GSRC_GENO) {
         const double scale = ctx->vc[1] * (ctx->gen.Mk > 0 ? 1.0 / (double)ctx->gen.Mk : 0.0);
+        if (ctx->prec == GLOBE_PREC_MIXED) return geno_apply_tc(ctx, Z, k, scale, out);
         return geno_apply_f64(ctx, Z, k, scale, out);
     }
     if (ctx->gen.src == GSRC_DENSE) return dense_apply_f64(ctx, Z, k, ctx->vc[1], out);
@@ -81,14 +82,23 @@ static int d2h(globe_ctx* ctx, double* h, const double* d, size_t n) {
     return GLOBE_OK;
 }
 
+static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info);
+
 int pcg_dev(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info) {
-    GLOBE_RET(check_ready(ctx));
-    if (k < 1) return set_err(ctx, GLOBE_ERR_ARG, "number of right-hand sides must be >= 1");
     if (!o) return set_err(ctx, GLOBE_ERR_ARG, "null PCG options");
     if (o->precision != GLOBE_PREC_FP64 && o->precision != GLOBE_PREC_MIXED)
         return set_err(ctx, GLOBE_ERR_ARG, "unknown precision mode %d", o->precision);
-    if (o->precision == GLOBE_PREC_MIXED)
-        return set_err(ctx, GLOBE_ERR_UNSUPPORTED, "mixed precision is not available in this build");
+    const int saved = ctx->prec;
+    ctx->prec = o->precision;
+    int rc = pcg_run(ctx, B, X, k, o, info);
+    ctx->prec = saved;
+    if (rc == GLOBE_OK && o->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
+    return rc;
+}
+
+static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info) {
+    GLOBE_RET(check_ready(ctx));
+    if (k < 1) return set_err(ctx, GLOBE_ERR_ARG, "number of right-hand sides must be >= 1");
     if (!(o->tol >= 0) || o->maxit < 0) return set_err(ctx, GLOBE_ERR_ARG, "bad tolerance / iteration cap");
     auto& c = ctx->coh;
     const int64_t n = c.Nrec;
@@ -316,7 +326,8 @@ int globe_grm_apply(globe_ctx* ctx, const double* Z, double* out, int k) {
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
     size_t n = (size_t)ctx->coh.N * k;
-    return host_io(ctx, Z, n, out, n, [&](double* a, double* b) { return grm_apply_dev(ctx, a, k, b); });
+    GLOBE_RET(host_io(ctx, Z, n, out, n, [&](double* a, double* b) { return grm_apply_dev(ctx, a, k, b); }));
+    return ctx->prec == GLOBE_PREC_MIXED ? tc_check_error(ctx) : GLOBE_OK;
 }
 
 int globe_vx_dev(globe_ctx* ctx, const double* d_x, double* d_out, int k) {
@@ -331,7 +342,8 @@ int globe_vx(globe_ctx* ctx, const double* x, double* out, int k) {
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
     size_t n = (size_t)ctx->coh.Nrec * k;
-    return host_io(ctx, x, n, out, n, [&](double* a, double* b) { return vx_dev(ctx, a, k, b); });
+    GLOBE_RET(host_io(ctx, x, n, out, n, [&](double* a, double* b) { return vx_dev(ctx, a, k, b); }));
+    return ctx->prec == GLOBE_PREC_MIXED ? tc_check_error(ctx) : GLOBE_OK;
 }
 
 int globe_precond_apply(globe_ctx* ctx, const double* r, double* z, int k) {

@@ -139,6 +139,12 @@ int globe_load_grm(globe_ctx* ctx, const float* grm_lt, int32_t N);
  * > 0 (the block preconditioner is singular otherwise). */
 int globe_set_vc(globe_ctx* ctx, const double vc[5]);
 
+/* Precision of the operator calls below (globe_grm_apply, globe_vx):
+ * GLOBE_PREC_FP64 (default) or GLOBE_PREC_MIXED (genotype GRM on the FP8
+ * tensor cores with exact digit slicing; see globe_pcg_opts.precision).
+ * PCG / MME / AIREML calls take the precision from their options. */
+int globe_set_precision(globe_ctx* ctx, int precision);
+
 /* ---- operators -------------------------------------------------------- */
 
 /* out (N x k) = sig2g * A * Z for Z (N x k): the GRM product of
