@@ -275,33 +275,55 @@ def run_ours(args, cfg):
     e2e = {"value": e2e_units / t_e2e, "unit": "RHS*iters/s", "h2d_bytes_per_step": int(8 * Nrec * k),
            "d2h_bytes_per_step": int(8 * Nrec * k)}
 
+    # FP64-plain comparison on the same data (one iteration per step)
+    fp64 = None
+    if prec != G.PREC_FP64 and not args.no_fp64:
+        o64 = dict(opts, precision=G.PREC_FP64, maxit=1)
+        ctx.pcg_dev(B.data_ptr(), Xs.data_ptr(), k, **o64)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        u64 = 0
+        for _ in range(2):
+            u64 += ctx.pcg_dev(B.data_ptr(), Xs.data_ptr(), k, **o64)["rhs_iters"]
+        e1.record(stream)
+        barrier()
+        t64 = e0.elapsed_time(e1)
+        fp64 = {"value": u64 / (t64 / 1000.0), "unit": "RHS*iters/s", "ms_per_iteration": t64 / 2,
+                "speedup_of_mixed": value / (u64 / (t64 / 1000.0))}
+
     # roofline of the dominant GRM kernel (one genotype pass per launch)
     hbm, bf16, peak_src = load_peaks()
     n1, ms1 = prof[G._lib.PROF_GRM_PASS1]
     n2, ms2 = prof[G._lib.PROF_GRM_PASS2]
-    dom = ("k_geno_p2", n2, ms2) if ms2 >= ms1 else ("k_geno_p1", n1, ms1)
-    bytes_per_launch = Mk * bps + (N + Mk) * k * 8
+    tcname = "k_tc_gemm" if prec == G.PREC_MIXED else "k_geno"
+    dom = (tcname + "(pass 2: Zs'w)", n2, ms2) if ms2 >= ms1 else (tcname + "(pass 1: Zs v)", n1, ms1)
+    # algorithmic bytes of one pass: the packed genotypes once + the k right-hand sides in and out (FP32-equivalent)
+    bytes_per_launch = Mk * bps + (N + Mk) * k * 4
     avg_s = dom[2] / 1000.0 / max(dom[1], 1)
     achieved = bytes_per_launch / avg_s / 1e9
     traffic = None
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
-        traffic = json.load(open(tf)).get("%s:%s:%s" % (args.config, args.precision, dom[0]))
+        traffic = json.load(open(tf)).get("%s:%s:%s" % (args.config, args.precision, dom[0].split("(")[0]))
     ngrm, msgrm = prof[G._lib.PROF_GRM]
     niter, msiter = prof[G._lib.PROF_PCG_ITER]
     roof = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": peak_src, "traffic": traffic,
             "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_s * 1000.0, "launches": dom[1],
-            "grm_product_share_of_iteration": (msgrm / msiter) if msiter else None}
+            "grm_product_share_of_iteration": (msgrm / msiter) if msiter else None,
+            "pass_ms": {"pass1": ms1 / max(n1, 1), "pass2": ms2 / max(n2, 1)}}
     line = {"metric": METRIC, "value": value, "unit": "RHS*iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == G.PREC_FP64 else "mixed",
+            "vs_baseline": None, "dtype": "f64" if prec == G.PREC_FP64 else "e4m3 x e4m3 -> f32 (exact digits), f64 PCG",
             "data": "synthetic (GPU counter-based genotypes, seeded numpy records)",
             "config": {"workload": args.config, "shape": cfg["label"], "precision": args.precision,
                        "iters_per_step": args.iters, "kept_snps": Mk, "records": Nrec,
                        "l2": "inputs larger than L2 (packed genotypes %.1f GB)" % (Mk * stride / 1e9),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches)}
+    if fp64 is not None:
+        line["fp64_plain"] = fp64
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle
         alt, miss, maf, _, keep = oracle.bed_stats(sample_rows, N)
@@ -322,11 +344,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="precision")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--iters", type=int, default=2, help="PCG iterations per step")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--iters", type=int, default=0, help="PCG iterations per step (0: 10 mixed, 1 fp64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the in-run FP64-plain comparison")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
+    if args.iters <= 0:
+        args.iters = 10 if args.precision == "mixed" else 1
     if args.impl == "reference":
         return run_reference(args, cfg)
     return run_ours(args, cfg)

@@ -8,7 +8,7 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libglobe_gb300.so")
+LIB_PATH = os.environ.get("GLOBE_LIB", os.path.join(HERE, "libglobe_gb300.so"))
 
 GLOBE_OK = 0
 ERRORS = {-1: "GLOBE_ERR_ARG", -2: "GLOBE_ERR_CUDA", -3: "GLOBE_ERR_STATE", -4: "GLOBE_ERR_IO",

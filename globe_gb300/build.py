@@ -13,9 +13,13 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+# GLOBE_BUILD_TAG / GLOBE_NVCC_FLAGS build a variant library (e.g. other pipeline
+# depths) next to the default one: lib<tag>.so, objects in _build_<tag>.
+TAG = os.environ.get("GLOBE_BUILD_TAG", "")
+EXTRA = os.environ.get("GLOBE_NVCC_FLAGS", "").split()
+BUILD = os.path.join(HERE, "_build" + ("_" + TAG if TAG else ""))
 BIN = os.path.join(HERE, "bin")
-LIB = os.path.join(HERE, "libglobe_gb300.so")
+LIB = os.path.join(HERE, "libglobe_gb300%s.so" % ("_" + TAG if TAG else ""))
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", os.path.join(ROOT, "include"), "-I", SRC,
@@ -41,8 +45,7 @@ def _compile(src):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     if not _newer(obj, [src] + _headers()):
         return obj
-    extra = ARCH if src.endswith(".cu") else ["-x", "cu"] + ARCH if False else []
-    cmd = [NVCC] + COMMON + (ARCH if src.endswith(".cu") else []) + ["-c", src, "-o", obj]
+    cmd = [NVCC] + COMMON + EXTRA + (ARCH if src.endswith(".cu") else []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-6000:]))
@@ -60,7 +63,7 @@ def build(verbose=True):
     if _newer(LIB, objs):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
         subprocess.check_call(cmd)
-    for name, src in CLI.items():
+    for name, src in (CLI.items() if not TAG else []):
         s = os.path.join(SRC, src)
         exe = os.path.join(BIN, name)
         if os.path.exists(s) and _newer(exe, [s, LIB] + _headers()):

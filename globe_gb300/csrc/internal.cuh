@@ -55,6 +55,10 @@ struct Genetic {
     // N rows of strideT bytes, byte b = SNPs 4b..4b+3, padding codes 11
     uint8_t* gt = nullptr;
     int64_t strideT = 0;
+    // tile-blocked copies for the tensor-core passes: block (tile, chunk) = 128 rows x 32 B
+    uint8_t* blk1 = nullptr;   // SNP-major (pass 1)
+    uint8_t* blk2 = nullptr;   // individual-major (pass 2)
+    int nch1 = 0, ntiles1 = 0, nch2 = 0, ntiles2 = 0;
     // dense source
     float* grm = nullptr;    // N(N+1)/2
     // both

@@ -14,13 +14,18 @@
 // rounding, and the digits are recombined in FP64.  With 12 digits the
 // product matches an FP64 evaluation to ~1e-14 relative.
 //
-// Kernel (one CTA = 128 rows x one K range, M=128 x N=NMMA MMAs):
-//   warp 0    TMA producer: packed 2-bit tile [128 rows x 32 B] and the digit
-//             tile [NMMA rows x 128 B, 128B-swizzled] per stage (4 stages)
-//   warp 1    TMEM allocation and the single-thread tcgen05.mma issue
-//             (kind::f8f6f4, E4M3 x E4M3 -> F32, 4 MMAs of K=32 per stage)
-//   warps 2-9 decode 2-bit codes to e4m3 bytes in shared memory (128B-swizzled
-//             K-major layout), then the epilogue (tcgen05.ld -> FP32 partials)
+// Kernel (one CTA = MT x 128 rows x one K range, M=128 x N=NMMA MMAs per tile):
+//   warp 0     bulk copies of the packed 2-bit tiles (tile-blocked layout: each
+//              128-row x 32-byte stage is one contiguous 4 KB block)
+//   warp 1     TMA of the digit tiles [NMMA rows x 128 B, 128B-swizzled]
+//   warp 2     TMEM allocation and the single-thread tcgen05.mma issue
+//              (kind::f8f6f4, E4M3 x E4M3 -> F32, A from TMEM, B from smem)
+//   warps 3-10 decode 2-bit codes to e4m3 bytes in registers and store them
+//              straight into TMEM (tcgen05.st) as the A operand, then the
+//              epilogue (tcgen05.ld -> FP32 partials)
+// Keeping the decoded operand out of shared memory matters: staged through
+// smem it costs ~4 bytes of smem traffic per genotype and caps the kernel
+// near 40% of HBM bandwidth.
 // The decode of 16 genotypes (one 32-bit word) is 3 logic ops, 2 shifts and
 // 4 byte permutes; it permutes K within each group of 16, which the digit
 // tiles repeat (kpos()).
@@ -34,26 +39,58 @@
 namespace globe {
 namespace tc {
 
-constexpr int BM = 128;           // tile rows (TMEM lanes)
+constexpr int BM = 128;           // rows per MMA tile (TMEM lanes)
 constexpr int BK = 128;           // K elements per stage (one 128-byte swizzle panel of e4m3)
 constexpr int PKB = BK / 4;       // packed bytes per row per stage
-constexpr int STAGES = 4;
-constexpr int DSTAGES = 2;
-constexpr int DEC_WARPS = 8;
-constexpr int NTHREADS = (2 + DEC_WARPS) * 32;
+#ifndef TC_ASTAGES
+#define TC_ASTAGES 6
+#endif
+#ifndef TC_BSTAGES
+#define TC_BSTAGES 3
+#endif
+#ifndef TC_DSTAGES
+#define TC_DSTAGES 2
+#endif
+#ifndef TC_SLEEP
+#define TC_SLEEP 1       // producers / MMA issuer suspend in their waits
+#endif
+#ifndef TC_SLEEP_DEC
+#define TC_SLEEP_DEC 0   // decoders poll
+#endif
+constexpr int ASTAGES = TC_ASTAGES;  // packed-genotype ring (keeps DRAM reads in flight)
+constexpr int BSTAGES = TC_BSTAGES;  // digit-tile ring (L2-resident operand)
+constexpr int DSTAGES = TC_DSTAGES;  // decoded-A ring
+// Row tiles per CTA (one MMA-issuing warp each): an M=128, K=32 MMA occupies
+// its issuing context ~157 cycles whatever N is, so small-N products need
+// several concurrent issue streams to use the tensor pipe; TMEM (512
+// columns) bounds MT * NMMA + DSTAGES * MT * 32.
+template <int NMMA>
+struct Geo {
+    static constexpr int MT = NMMA <= 64 ? 4 : (NMMA <= 192 ? 2 : 1);
+    static constexpr int DECW = MT >= 2 ? 16 : 8;          // decoder warps
+    static constexpr int DBASE = MT > 2 ? 8 : 4;           // first decoder warp (multiple of 4)
+    static constexpr int NTHREADS = (DBASE + DECW) * 32;
+    static constexpr int NH = MT == 4 ? 2 : 1;             // 16-byte halves per decoder thread
+    static constexpr int DPT = DECW / MT;                  // decoder warps per tile
+    static constexpr int CPARTS = DPT / 4;                 // warps per TMEM quadrant in the epilogue
+};
 constexpr int NDIG = 12;          // digits per right-hand-side column
 constexpr int MAX_RHS_GROUP = 21; // 21 * 12 = 252 <= 256 MMA columns
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
 constexpr uint32_t LUT_G = 0x00380040u;  // code 00 -> 2.0 (0x40), 01 -> 0, 10 -> 1.0 (0x38), 11 -> 0
 
-__host__ __device__ constexpr int ncols_alloc(int n) { return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 256; }
+__host__ __device__ constexpr int ncols_alloc(int n) {
+    return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
+}
 
-template <int NMMA>
+// MT row tiles of 128 share every digit tile.  TMEM columns: accumulators
+// [0, MT*NMMA), then DSTAGES x MT decoded A tiles of 32 columns (K = 128 e4m3).
+template <int NMMA, int MT>
 struct __align__(1024) Smem {
-    uint8_t adec[DSTAGES][BM * BK];      // decoded A, SW128 K-major (16 KB each)
-    uint8_t bt[STAGES][NMMA * BK];       // digit tiles (TMA, SW128)
-    uint8_t pk[STAGES][BM * PKB];        // packed tiles (TMA, no swizzle)
-    uint64_t full[STAGES], empty[STAGES], adfull[DSTAGES], adempty[DSTAGES], accfull;
+    uint8_t bt[BSTAGES][NMMA * BK];         // digit tiles (TMA, SW128), 1024-aligned
+    uint8_t pk[ASTAGES][MT * BM * PKB];     // packed tiles (bulk copies)
+    uint64_t afull[ASTAGES], aempty[ASTAGES], bfull[BSTAGES], bempty[BSTAGES];
+    uint64_t adfull[MT][DSTAGES], adempty[MT][DSTAGES], accfull[MT];
     uint32_t tmem_base;
     int abort;
 };
@@ -84,17 +121,33 @@ __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait; false on timeout or when another role aborted
+// try_wait that may suspend the thread until the phase completes (hint in ns)
+__device__ __forceinline__ bool mbar_try_sleep(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(b)), "r"(parity), "r"(200000u)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; false on timeout or when another role aborted.  The clock
+// and the abort flag are read only every 256 polls, off the fast path.
+template <bool SLEEP = (TC_SLEEP != 0)>
 __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* abort, unsigned* err, unsigned bit) {
     if (mbar_try(b, parity)) return true;
-    const uint64_t t0 = gtime();
-    while (true) {
-        if (mbar_try(b, parity)) return true;
-        if (*(volatile int*)abort) return false;
-        if (gtime() - t0 > WAIT_LIMIT_NS) {
-            *(volatile int*)abort = 1;
-            atomicOr(err, bit);
-            return false;
+    uint64_t t0 = 0;
+    for (uint32_t spins = 1;; ++spins) {
+        if (SLEEP ? mbar_try_sleep(b, parity) : mbar_try(b, parity)) return true;
+        if ((spins & 255u) == 0) {
+            if (*(volatile int*)abort) return false;
+            const uint64_t t = gtime();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > WAIT_LIMIT_NS) {
+                *(volatile int*)abort = 1;
+                atomicOr(err, bit);
+                return false;
+            }
         }
     }
 }
@@ -110,6 +163,12 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
             saddr(dst)),
         "l"((uint64_t)tm), "r"(x), "r"(y), "r"(saddr(bar))
         : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -129,6 +188,22 @@ __device__ __forceinline__ void mma_f8(uint32_t d, uint64_t a, uint64_t b, uint3
         "l"(a), "l"(b), "r"(idesc), "r"(acc)
         : "memory");
 }
+__device__ __forceinline__ void mma_f8_ta(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
                  : "memory");
@@ -160,33 +235,47 @@ __device__ __forceinline__ void decode_word(uint32_t w, uint32_t& r0, uint32_t& 
     r3 = __byte_perm(LUT_G, 0u, o >> 16);
 }
 
+// A operand: tile-blocked packed genotypes, block (tile t, chunk c) = 128 rows x 32 B contiguous at
+// blk + (t * nchunks + c) * 4096 (the two 16-byte halves of row r swapped when bit 2 of r is set,
+// which makes the decoders' shared-memory reads conflict-free); one stage = MT bulk copies.
 template <int NMMA>
-__global__ void __launch_bounds__(NTHREADS, 1)
-    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int rows, int nchunks,
+__global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
+    k_tc_gemm(const uint8_t* __restrict__ blk, const __grid_constant__ CUtensorMap tmB, int rows, int nchunks,
               int cps, float* __restrict__ part, int64_t ldp, unsigned* __restrict__ err) {
+    using G = Geo<NMMA>;
+    constexpr int MT = G::MT;
     static_assert(NMMA % 32 == 0 && NMMA >= 32 && NMMA <= 256, "NMMA");
-    constexpr uint32_t NCOLS = ncols_alloc(NMMA);
+    constexpr int ACOL0 = MT * NMMA;                     // first TMEM column of the decoded A stages
+    static_assert(MT * NMMA + DSTAGES * MT * 32 <= 512, "TMEM columns");
+    constexpr uint32_t NCOLS = ncols_alloc(MT * NMMA + DSTAGES * MT * 32);
+    constexpr int ROWS = MT * BM;
     extern __shared__ uint8_t smraw[];
-    Smem<NMMA>& S = *reinterpret_cast<Smem<NMMA>*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    Smem<NMMA, MT>& S = *reinterpret_cast<Smem<NMMA, MT>*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tile = blockIdx.x, split = blockIdx.y;
+    const int row0 = blockIdx.x * ROWS, split = blockIdx.y;
     const int c0 = split * cps;
     const int nloc = min(nchunks, c0 + cps) - c0;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&S.full[s], 1);
-            mbar_init(&S.empty[s], DEC_WARPS * 32 + 1);
+        for (int s = 0; s < ASTAGES; ++s) {
+            mbar_init(&S.afull[s], 1);
+            mbar_init(&S.aempty[s], G::DECW);
         }
-        for (int d = 0; d < DSTAGES; ++d) {
-            mbar_init(&S.adfull[d], DEC_WARPS * 32);
-            mbar_init(&S.adempty[d], 1);
+        for (int s = 0; s < BSTAGES; ++s) {
+            mbar_init(&S.bfull[s], 1);
+            mbar_init(&S.bempty[s], MT);
         }
-        mbar_init(&S.accfull, 1);
+        for (int m = 0; m < MT; ++m) {
+            for (int d = 0; d < DSTAGES; ++d) {
+                mbar_init(&S.adfull[m][d], G::DPT);
+                mbar_init(&S.adempty[m][d], 1);
+            }
+            mbar_init(&S.accfull[m], 1);
+        }
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) tmem_alloc(&S.tmem_base, NCOLS);
+    if (warp == 2) tmem_alloc(&S.tmem_base, NCOLS);
     tc_before();
     __syncthreads();
     tc_after();
@@ -194,90 +283,129 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     int* abort = &S.abort;
 
     if (warp == 0) {
+        // packed genotype tiles: up to ASTAGES chunks ahead of the decoders
         if (lane == 0 && nloc > 0) {
             int issued = 0;
             for (int it = 0; it < nloc; ++it) {
-                const int s = it % STAGES, n = it / STAGES;
-                if (n > 0 && !mbar_wait(&S.empty[s], (n - 1) & 1, abort, err, 1u)) break;
-                mbar_expect_tx(&S.full[s], BM * PKB + NMMA * BK);
-                const int kc = c0 + it;
-                tma_load_2d(S.pk[s], &tmA, kc * PKB, tile * BM, &S.full[s]);
-                tma_load_2d(S.bt[s], &tmB, kc * BK, 0, &S.full[s]);
+                const int s = it % ASTAGES, n = it / ASTAGES;
+                if (n > 0 && !mbar_wait(&S.aempty[s], (n - 1) & 1, abort, err, 1u)) break;
+                mbar_expect_tx(&S.afull[s], ROWS * PKB);
+#pragma unroll
+                for (int m = 0; m < MT; ++m) {
+                    const int64_t t = (int64_t)blockIdx.x * MT + m;
+                    bulk_load(S.pk[s] + m * (BM * PKB), blk + (t * nchunks + (c0 + it)) * (int64_t)(BM * PKB),
+                              BM * PKB, &S.afull[s]);
+                }
                 issued = it + 1;
             }
-            // copies still in flight complete into full[]; wait for the last ones before leaving
-            for (int it = issued - 1; it >= 0 && it >= issued - STAGES; --it)
-                mbar_drain(&S.full[it % STAGES], (it / STAGES) & 1);
+            for (int it = issued - 1; it >= 0 && it >= issued - ASTAGES; --it)
+                mbar_drain(&S.afull[it % ASTAGES], (it / ASTAGES) & 1);
         }
     } else if (warp == 1) {
+        // digit tiles: up to BSTAGES chunks ahead of the MMAs
+        if (lane == 0 && nloc > 0) {
+            int issued = 0;
+            for (int it = 0; it < nloc; ++it) {
+                const int s = it % BSTAGES, n = it / BSTAGES;
+                if (n > 0 && !mbar_wait(&S.bempty[s], (n - 1) & 1, abort, err, 2u)) break;
+                mbar_expect_tx(&S.bfull[s], NMMA * BK);
+                tma_load_2d(S.bt[s], &tmB, (c0 + it) * BK, 0, &S.bfull[s]);
+                issued = it + 1;
+            }
+            for (int it = issued - 1; it >= 0 && it >= issued - BSTAGES; --it)
+                mbar_drain(&S.bfull[it % BSTAGES], (it / BSTAGES) & 1);
+        }
+    } else if (warp >= 2 && warp < 2 + MT) {
+        // one MMA issue stream per row tile
+        const int m = warp - 2;
         if (lane == 0 && nloc > 0) {
             const uint32_t idesc = (1u << 4) | ((uint32_t)(NMMA >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+            const uint32_t dcol = tmem + (uint32_t)(m * NMMA);
             for (int it = 0; it < nloc; ++it) {
-                const int s = it % STAGES, ds = it % DSTAGES;
-                if (!mbar_wait(&S.full[s], (it / STAGES) & 1, abort, err, 2u)) break;
-                if (!mbar_wait(&S.adfull[ds], (it / DSTAGES) & 1, abort, err, 4u)) break;
+                const int sb = it % BSTAGES, ds = it % DSTAGES;
+                if (!mbar_wait(&S.bfull[sb], (it / BSTAGES) & 1, abort, err, 4u)) break;
+                if (!mbar_wait(&S.adfull[m][ds], (it / DSTAGES) & 1, abort, err, 8u)) break;
                 tc_after();
-                const uint32_t a0 = saddr(S.adec[ds]), b0 = saddr(S.bt[s]);
+                const uint32_t b0 = saddr(S.bt[sb]);
+                const uint32_t acol = tmem + (uint32_t)(ACOL0 + (ds * MT + m) * 32);
 #pragma unroll
                 for (int kk = 0; kk < BK / 32; ++kk)
-                    mma_f8(tmem, desc_sw128(a0 + kk * 32), desc_sw128(b0 + kk * 32), idesc, (it | kk) != 0);
-                mma_commit(&S.empty[s]);
-                mma_commit(&S.adempty[ds]);
+                    mma_f8_ta(dcol, acol + (uint32_t)(kk * 8), desc_sw128(b0 + kk * 32), idesc, (it | kk) != 0);
+                mma_commit(&S.bempty[sb]);
+                mma_commit(&S.adempty[m][ds]);
             }
-            mma_commit(&S.accfull);  // tracks every MMA issued above
+            mma_commit(&S.accfull[m]);  // tracks every MMA this thread issued
         }
-    } else {
-        const int dt = threadIdx.x - 64;      // 0..255
-        const int row = dt >> 1, half = dt & 1;
-        const uint32_t r7 = (uint32_t)(row & 7);
+    } else if (warp >= G::DBASE) {
+        // decoders: warp -> TMEM lane quadrant (warp % 4); group g picks the tile and the 16-byte half(s)
+        const int quad = warp & 3, g = (warp - G::DBASE) >> 2;
+        const int m = g % MT;                          // tile
+        const int hsel = g / MT;                       // half (NH == 1) / column part (epilogue)
+        const int r = quad * 32 + lane;                // row within the tile
+        const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
+        const int swz = (r >> 2) & 1;
         bool ok = true;
         for (int it = 0; it < nloc && ok; ++it) {
-            const int s = it % STAGES, ds = it % DSTAGES;
-            if (!mbar_wait(&S.full[s], (it / STAGES) & 1, abort, err, 8u)) { ok = false; break; }
-            if (it >= DSTAGES && !mbar_wait(&S.adempty[ds], ((it / DSTAGES) - 1) & 1, abort, err, 16u)) {
+            const int sa = it % ASTAGES, ds = it % DSTAGES;
+            if (!mbar_wait<TC_SLEEP_DEC != 0>(&S.afull[sa], (it / ASTAGES) & 1, abort, err, 16u)) { ok = false; break; }
+            if (it >= DSTAGES &&
+                !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[m][ds], ((it / DSTAGES) - 1) & 1, abort, err, 32u)) {
                 ok = false;
                 break;
             }
-            const uint4 v = *reinterpret_cast<const uint4*>(S.pk[s] + row * PKB + half * 16);
-            mbar_arrive(&S.empty[s]);
-            uint8_t* dst = S.adec[ds] + (row >> 3) * 1024 + r7 * 128;
-            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+            constexpr int NH = G::NH;
+            uint4 v[NH];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                uint4 o;
-                decode_word(w4[q], o.x, o.y, o.z, o.w);
-                const uint32_t chunk = (uint32_t)(half * 4 + q);
-                *reinterpret_cast<uint4*>(dst + ((chunk ^ r7) << 4)) = o;
+            for (int j = 0; j < NH; ++j) {
+                const int h = (NH == 2) ? j : hsel;    // logical half
+                v[j] = *reinterpret_cast<const uint4*>(S.pk[sa] + m * (BM * PKB) + (r * 2 + (h ^ swz)) * 16);
             }
-            fence_proxy_async();
-            mbar_arrive(&S.adfull[ds]);
+            uint32_t o[NH][16];
+#pragma unroll
+            for (int j = 0; j < NH; ++j) {
+                decode_word(v[j].x, o[j][0], o[j][1], o[j][2], o[j][3]);
+                decode_word(v[j].y, o[j][4], o[j][5], o[j][6], o[j][7]);
+                decode_word(v[j].z, o[j][8], o[j][9], o[j][10], o[j][11]);
+                decode_word(v[j].w, o[j][12], o[j][13], o[j][14], o[j][15]);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.aempty[sa]);   // packed stage consumed
+#pragma unroll
+            for (int j = 0; j < NH; ++j) {
+                const int h = (NH == 2) ? j : hsel;
+                tmem_st16(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[j]);
+            }
+            tmem_wait_st();
+            tc_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.adfull[m][ds]);
         }
-        // epilogue: warp -> TMEM lane quadrant, two warps per quadrant split the columns
+        // epilogue: the tile's warps of one quadrant split the accumulator columns
         bool go = ok && nloc > 0;
-        if (go) go = mbar_wait(&S.accfull, 0, abort, err, 32u);
+        if (go) go = mbar_wait(&S.accfull[m], 0, abort, err, 64u);
         go = __all_sync(0xffffffffu, go);   // tcgen05.ld is warp-collective
         if (go) {
             tc_after();
-            const int quad = warp & 3;
-            const int hc = (warp - 2) >> 2;
-            const int r = tile * BM + quad * 32 + lane;
+            constexpr int CW = NMMA / G::CPARTS;
+            const int part_id = (G::CPARTS == 1) ? 0 : hsel;
+            const int rr = row0 + m * BM + r;
 #pragma unroll 1
-            for (int cb = hc * (NMMA / 2); cb < (hc + 1) * (NMMA / 2); cb += 16) {
-                uint32_t v[16];
-                tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)cb, v);
-                if (r < rows) {
+            for (int cb = part_id * CW; cb < (part_id + 1) * CW; cb += 16) {
+                uint32_t acc[16];
+                tmem_ld16(tmem + lane_addr + (uint32_t)(m * NMMA + cb), acc);
+                if (rr < rows) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j)
-                        part[((int64_t)split * NMMA + cb + j) * ldp + r] = __uint_as_float(v[j]);
+                        part[((int64_t)split * NMMA + cb + j) * ldp + rr] = __uint_as_float(acc[j]);
                 }
             }
         }
     }
     // leave: MMAs that were issued must finish before TMEM is released
-    if (warp == 1 && nloc > 0) mbar_drain(&S.accfull, 0);
+    if (warp >= 2 && warp < 2 + MT && nloc > 0) mbar_drain(&S.accfull[warp - 2], 0);
     tc_before();
     __syncthreads();
-    if (warp == 1) {
+    if (warp == 2) {
         tc_after();
         tmem_dealloc(tmem, NCOLS);
     }
@@ -461,6 +589,32 @@ __global__ void k_fill_pad(uint8_t* __restrict__ Gt, int32_t N, int64_t strideT,
     }
 }
 
+// row-major packed rows (stride bytes) -> tile-blocked layout, 16 bytes per thread;
+// rows >= nrows and bytes >= stride become 0xFF (genotype 0)
+__global__ void k_blockify(const uint8_t* __restrict__ src, int64_t nrows, int64_t stride, int64_t ntiles,
+                           int64_t nch, uint8_t* __restrict__ dst) {
+    const int64_t total = ntiles * nch * (BM * PKB / 16);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t blkid = e / (BM * PKB / 16);
+        const int within = (int)(e % (BM * PKB / 16));
+        const int r = within >> 1, h = within & 1;
+        const int64_t t = blkid / nch, c = blkid % nch;
+        const int64_t row = t * BM + r, byte = c * PKB + h * 16;
+        uint4 v = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        if (row < nrows && byte < stride) {
+            if (byte + 16 <= stride) {
+                v = *reinterpret_cast<const uint4*>(src + row * stride + byte);
+            } else {
+                uint8_t tmp[16];
+                for (int q = 0; q < 16; ++q) tmp[q] = byte + q < stride ? src[row * stride + byte + q] : (uint8_t)0xFF;
+                v = *reinterpret_cast<const uint4*>(tmp);
+            }
+        }
+        const int64_t phys = (blkid * BM + r) * 2 + (h ^ ((r >> 2) & 1));   // halves swapped when bit 2 of r is set
+        *reinterpret_cast<uint4*>(dst + phys * 16) = v;
+    }
+}
+
 }  // namespace tc
 
 // ---- host side ---------------------------------------------------------------
@@ -495,9 +649,23 @@ static int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t i
     return GLOBE_OK;
 }
 
+static int blockify(globe_ctx* ctx, const uint8_t* src, int64_t nrows, int64_t stride, uint8_t** dst, int* nch,
+                    int* ntiles) {
+    *nch = (int)((stride + PKB - 1) / PKB);
+    *ntiles = (int)((nrows + BM - 1) / BM);
+    // whole CTAs: round the tile count up to a multiple of 4 (a CTA may own four tiles)
+    *ntiles = (*ntiles + 3) / 4 * 4;
+    GLOBE_RET(dalloc(ctx, dst, (size_t)(*ntiles) * (*nch) * BM * PKB));
+    const int64_t total = (int64_t)(*ntiles) * (*nch) * (BM * PKB / 16);
+    k_blockify<<<(unsigned)std::min<int64_t>((total + 255) / 256, 65535), 256, 0, ctx->stream>>>(
+        src, nrows, stride, *ntiles, *nch, *dst);
+    GLOBE_LAUNCHED(ctx, "k_blockify");
+    return GLOBE_OK;
+}
+
 int ensure_gt(globe_ctx* ctx) {
     auto& g = ctx->gen;
-    if (g.gt) return GLOBE_OK;
+    if (g.blk2) return GLOBE_OK;
     const int32_t N = ctx->coh.N;
     g.strideT = ((g.Mk + 3) / 4 + PKB - 1) / PKB * PKB;
     if (g.strideT < PKB) g.strideT = PKB;
@@ -515,27 +683,35 @@ int ensure_gt(globe_ctx* ctx) {
         k_fill_pad<<<1024, 256, 0, ctx->stream>>>(g.gt, N, g.strideT, from);
         GLOBE_LAUNCHED(ctx, "k_fill_pad");
     }
+    GLOBE_RET(blockify(ctx, g.geno, g.Mk, g.stride, &g.blk1, &g.nch1, &g.ntiles1));
+    GLOBE_RET(blockify(ctx, g.gt, N, g.strideT, &g.blk2, &g.nch2, &g.ntiles2));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx, g.gt);   // the row-major individual-major copy is only a staging step
+    g.gt = nullptr;
     return GLOBE_OK;
 }
 
 template <int NMMA>
-static int launch_gemm(globe_ctx* ctx, const CUtensorMap& mA, const CUtensorMap& mB, int rows, int nchunks, int splits,
+static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB, int rows, int nchunks, int splits,
                        float* part, int64_t ldp, unsigned* err) {
+    using G = Geo<NMMA>;
     const int cps = (nchunks + splits - 1) / splits;
     splits = (nchunks + cps - 1) / cps;
-    const size_t smem = sizeof(Smem<NMMA>) + 1024;
+    const size_t smem = sizeof(Smem<NMMA, G::MT>) + 1024;
     static bool attr = false;
     if (!attr) {
         GLOBE_CK(ctx, cudaFuncSetAttribute(k_tc_gemm<NMMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    dim3 grid((unsigned)((rows + BM - 1) / BM), (unsigned)splits);
-    k_tc_gemm<NMMA><<<grid, NTHREADS, smem, ctx->stream>>>(mA, mB, rows, nchunks, cps, part, ldp, err);
+    dim3 grid((unsigned)((rows + G::MT * BM - 1) / (G::MT * BM)), (unsigned)splits);
+    k_tc_gemm<NMMA><<<grid, G::NTHREADS, smem, ctx->stream>>>(blk, mB, rows, nchunks, cps, part, ldp, err);
     GLOBE_LAUNCHED(ctx, "k_tc_gemm");
     return GLOBE_OK;
 }
 
-static int gemm_dispatch(globe_ctx* ctx, int nmma, const CUtensorMap& mA, const CUtensorMap& mB, int rows,
+static int rows_per_cta(int nmma) { return BM * (nmma <= 64 ? 4 : (nmma <= 192 ? 2 : 1)); }
+
+static int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* mA, const CUtensorMap& mB, int rows,
                          int nchunks, int splits, float* part, int64_t ldp, unsigned* err) {
     switch (nmma) {
         case 32: return launch_gemm<32>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
@@ -569,13 +745,14 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     const int32_t N = ctx->coh.N;
     const int nmma = ((kg * NDIG + 31) / 32) * 32;
     // ---- pass 1 operands
-    const int nch1 = (int)((g.stride + PKB - 1) / PKB);
+    const int nch1 = g.nch1;
     const int64_t kpad1 = (int64_t)nch1 * BK;
-    const int nch2 = (int)(g.strideT / PKB);
+    const int nch2 = g.nch2;
     const int64_t kpad2 = (int64_t)nch2 * BK;
-    const int tiles1 = (int)((g.Mk + BM - 1) / BM), tiles2 = (N + BM - 1) / BM;
+    const int rpc = rows_per_cta(nmma);
+    const int tiles1 = (int)((g.Mk + rpc - 1) / rpc), tiles2 = (N + rpc - 1) / rpc;
     const int sp1 = pick_splits(tiles1, nch1), sp2 = pick_splits(tiles2, nch2);
-    const int64_t ldp1 = (int64_t)tiles1 * BM, ldp2 = (int64_t)tiles2 * BM;
+    const int64_t ldp1 = (int64_t)tiles1 * rpc, ldp2 = (int64_t)tiles2 * rpc;
     uint8_t *D1, *D2;
     float *P1, *P2;
     double *U, *cst, *pm, *ps;
@@ -593,10 +770,8 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     ps = pm + (size_t)nbr * kg;
     GLOBE_RET(ws(ctx, WS_TC_ERR, 4, &err));
     GLOBE_CK(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream));
-    CUtensorMap mA1, mB1, mA2, mB2;
-    GLOBE_RET(make_map(ctx, &mA1, g.geno, (uint64_t)g.stride, (uint64_t)g.Mk, PKB, BM, false));
+    CUtensorMap mB1, mB2;
     GLOBE_RET(make_map(ctx, &mB1, D1, (uint64_t)kpad1, (uint64_t)nmma, BK, (uint32_t)nmma, true));
-    GLOBE_RET(make_map(ctx, &mA2, g.gt, (uint64_t)g.strideT, (uint64_t)N, PKB, BM, false));
     GLOBE_RET(make_map(ctx, &mB2, D2, (uint64_t)kpad2, (uint64_t)nmma, BK, (uint32_t)nmma, true));
     // ---- digits of Z
     k_col_maxsum<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
@@ -610,7 +785,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     // ---- pass 1
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS1);
-        GLOBE_RET(gemm_dispatch(ctx, nmma, mA1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err));
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err));
     }
     const int sp1e = eff_splits(nch1, sp1);
     k_combine1<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
@@ -624,7 +799,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     GLOBE_LAUNCHED(ctx, "k_digits");
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS2);
-        GLOBE_RET(gemm_dispatch(ctx, nmma, mA2, mB2, N, nch2, sp2, P2, ldp2, err));
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, mB2, N, nch2, sp2, P2, ldp2, err));
     }
     const int sp2e = eff_splits(nch2, sp2);
     k_combine2<<<dim3(div_up(N, 256) < 1024 ? div_up(N, 256) : 1024, kg), 256, 0, ctx->stream>>>(
