@@ -1,8 +1,11 @@
 // k_records.cu -- record-level kernels of the LGMM operator and block PCG.
 //
 // Records of one individual form one contiguous block.  All record-level
-// work is per block: one warp owns a block, so segment sums, the 2x2 random
-// intercept/slope term and the block preconditioner fuse without atomics.
+// work is per block, so segment sums, the 2x2 random intercept/slope term and
+// the block preconditioner fuse without atomics.  Two layouts of the same
+// kernels: when every block holds at most SHORT_BLOCK records one thread owns
+// a (block, column) pair (grid.y = column); longer blocks use one warp per
+// block and loop over the columns.
 //
 //   V x   = J (sig2g A J' x) + U D U' x + sig2e x          (PCGsolver.cpp:1095-1266)
 //   U D U' x on block b = (D00 s0 + D01 s1) + t (D01 s0 + D11 s1),
@@ -20,6 +23,10 @@ namespace globe {
 
 constexpr int RB_THREADS = 256;  // 8 warps, one block of records per warp
 constexpr int RB_WARPS = RB_THREADS / 32;
+constexpr int TB_THREADS = 256;  // thread-per-block layout
+constexpr int SHORT_BLOCK = 48;  // longest block handled by one thread
+
+static bool short_blocks(const globe_ctx* ctx) { return ctx->coh.max_block <= SHORT_BLOCK; }
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -41,6 +48,28 @@ __device__ __forceinline__ void cta_partials(double* sm, int nq, double* part) {
 #pragma unroll
         for (int w = 0; w < RB_WARPS; ++w) a += sm[q * RB_WARPS + w];
         part[blockIdx.x + (size_t)q * gridDim.x] = a;
+    }
+}
+
+// CTA sums of NQ values per thread (thread-per-block layout):
+// sum over the CTA of v[j] -> part[blockIdx.x + q[j] * gridDim.x]
+template <int NQ>
+__device__ __forceinline__ void cta_sums(const double (&v)[NQ], const int (&q)[NQ], double* part) {
+    __shared__ double sm[NQ][TB_THREADS / 32];
+#pragma unroll
+    for (int j = 0; j < NQ; ++j) {
+        const double a = warp_sum(v[j]);
+        if ((threadIdx.x & 31) == 0) sm[j][threadIdx.x >> 5] = a;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NQ; ++j) {
+        if (threadIdx.x == j) {
+            double a = 0.0;
+#pragma unroll
+            for (int w = 0; w < TB_THREADS / 32; ++w) a += sm[j][w];
+            part[blockIdx.x + (size_t)q[j] * gridDim.x] = a;
+        }
     }
 }
 
@@ -146,11 +175,52 @@ __global__ void k_seg_sums(int32_t nblk, int64_t ld, int32_t N, const int32_t* _
     }
 }
 
+// thread-per-block layout: one thread per (block, column)
+__global__ void k_seg_sums_t(int32_t nblk, int64_t ld, int32_t N, const int32_t* __restrict__ bstart,
+                             const int32_t* __restrict__ bind, const double* __restrict__ t, double* x,
+                             const double* __restrict__ z, const double* __restrict__ beta,
+                             const int32_t* __restrict__ cols, double* __restrict__ Zi, double* __restrict__ S1) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    const int c = blockIdx.y;
+    const int col = cols ? cols[c] : c;
+    const int st = bstart[b], en = bstart[b + 1];
+    double* xc = x + (size_t)col * ld;
+    double s0 = 0, s1 = 0;
+    if (beta) {
+        const double bb = beta[col];
+        const double* zc = z + (size_t)col * ld;
+#pragma unroll 4
+        for (int r = st; r < en; ++r) {
+            const double v = zc[r] + bb * xc[r];
+            xc[r] = v;
+            s0 += v;
+            s1 += t[r] * v;
+        }
+    } else {
+#pragma unroll 4
+        for (int r = st; r < en; ++r) {
+            const double v = xc[r];
+            s0 += v;
+            s1 += t[r] * v;
+        }
+    }
+    const int i = bind[b];
+    Zi[i + (size_t)c * N] = s0;
+    if (S1) S1[i + (size_t)c * N] = s1;
+}
+
 int seg_sums(globe_ctx* ctx, const double* x, const double* z, const double* beta, double* xout,
              const int32_t* cols, int kact, double* Zi, double* S1) {
     auto& c = ctx->coh;
     // in-place p update: xout must alias x when beta is given
     double* xx = beta ? xout : const_cast<double*>(x);
+    if (short_blocks(ctx)) {
+        k_seg_sums_t<<<dim3(div_up(c.N, TB_THREADS), kact), TB_THREADS, 0, ctx->stream>>>(
+            c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), xx, z, beta, cols, Zi, S1);
+        GLOBE_LAUNCHED(ctx, "k_seg_sums_t");
+        return GLOBE_OK;
+    }
     k_seg_sums<<<div_up(c.N, RB_WARPS), RB_THREADS, 0, ctx->stream>>>(
         c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), xx, z, beta, cols, kact, Zi, S1);
     GLOBE_LAUNCHED(ctx, "k_seg_sums");
@@ -197,10 +267,52 @@ __global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t
     if (part) cta_partials(sm, kact, part);
 }
 
+__global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32_t* __restrict__ bstart,
+                                const int32_t* __restrict__ bind, const double* __restrict__ t, VC v,
+                                const double* __restrict__ x, const double* __restrict__ GZ,
+                                const double* __restrict__ Zi, const double* __restrict__ S1,
+                                const int32_t* __restrict__ cols, double* __restrict__ out,
+                                double* __restrict__ part) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    const int col = cols ? cols[c] : c;
+    double dot[1] = {0.0};
+    if (b < nblk) {
+        const int st = bstart[b], en = bstart[b + 1], i = bind[b];
+        const double s0 = Zi[i + (size_t)c * N], s1 = S1[i + (size_t)c * N];
+        const double g = GZ ? GZ[i + (size_t)c * N] : 0.0;
+        const double a0 = g + v.b0 * s0 + v.b01 * s1;
+        const double a1 = v.b01 * s0 + v.b1 * s1;
+        const double* xc = x + (size_t)col * ld;
+        double* oc = out + (size_t)col * ld;
+#pragma unroll 4
+        for (int r = st; r < en; ++r) {
+            const double xv = xc[r];
+            const double o = a0 + t[r] * a1 + v.e * xv;
+            oc[r] = o;
+            dot[0] += xv * o;
+        }
+    }
+    if (part) {
+        const int q[1] = {c};
+        cta_sums<1>(dot, q, part);
+    }
+}
+
 int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double* Zi, const double* S1,
                 const int32_t* cols, int kact, double* out, double* dot_out) {
     auto& c = ctx->coh;
     VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
+    if (short_blocks(ctx)) {
+        const int nb = div_up(c.N, TB_THREADS);
+        double* part = nullptr;
+        if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+        k_vx_assemble_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind,
+                                                                        c.times(), v, x, GZ, Zi, S1, cols, out, part);
+        GLOBE_LAUNCHED(ctx, "k_vx_assemble_t");
+        if (dot_out) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, dot_out));
+        return GLOBE_OK;
+    }
     int nb = div_up(c.N, RB_WARPS);
     double* part = nullptr;
     if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
@@ -274,9 +386,61 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
     cta_partials(sm, 2 * kact, part);
 }
 
+__global__ void k_pcg_update_t(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
+                               const double* __restrict__ t, double inv_e, const double* __restrict__ H,
+                               const double* __restrict__ alpha, double* __restrict__ x, double* __restrict__ r,
+                               const double* __restrict__ p, const double* __restrict__ Vp, double* __restrict__ z,
+                               const int32_t* __restrict__ cols, int kact, double* __restrict__ part) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    const int col = cols ? cols[c] : c;
+    double acc[2] = {0.0, 0.0};   // |r|^2, r'z
+    if (b < nblk) {
+        const int st = bstart[b], en = bstart[b + 1];
+        const double a = alpha[col];
+        double* xc = x + (size_t)col * ld;
+        double* rc = r + (size_t)col * ld;
+        const double* pc = p + (size_t)col * ld;
+        const double* vc = Vp + (size_t)col * ld;
+        double s0 = 0, s1 = 0;
+#pragma unroll 4
+        for (int q = st; q < en; ++q) {
+            xc[q] += a * pc[q];
+            const double rn = rc[q] - a * vc[q];
+            rc[q] = rn;
+            acc[0] += rn * rn;
+            s0 += rn;
+            s1 += t[q] * rn;
+        }
+        const double g0 = H[4 * b] * s0 + H[4 * b + 1] * s1, g1 = H[4 * b + 2] * s0 + H[4 * b + 3] * s1;
+        double* zc = z + (size_t)col * ld;
+#pragma unroll 4
+        for (int q = st; q < en; ++q) {
+            const double rn = rc[q];
+            const double zv = (rn - g0 - g1 * t[q]) * inv_e;
+            zc[q] = zv;
+            acc[1] += rn * zv;
+        }
+    }
+    const int qi[2] = {c, kact + c};
+    cta_sums<2>(acc, qi, part);
+}
+
 int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, double* r, const double* p,
                const double* Vp, double* z, const int32_t* cols, int kact, double* rr, double* rz) {
     auto& c = ctx->coh;
+    if (short_blocks(ctx)) {
+        const int nb = div_up(c.N, TB_THREADS);
+        double* part;
+        GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+        k_pcg_update_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
+                                                                       1.0 / ctx->vc[0], H, alpha, x, r, p, Vp, z,
+                                                                       cols, kact, part);
+        GLOBE_LAUNCHED(ctx, "k_pcg_update_t");
+        GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rr));
+        GLOBE_RET(reduce_cols(ctx, part + (size_t)nb * kact, nb, kact, cols, rz));
+        return GLOBE_OK;
+    }
     int nb = div_up(c.N, RB_WARPS);
     double* part;
     GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
@@ -336,9 +500,51 @@ __global__ void k_precond_apply(int32_t nblk, int64_t ld, const int32_t* __restr
     if (part) cta_partials(sm, kact, part);
 }
 
+__global__ void k_precond_apply_t(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
+                                  const double* __restrict__ t, double inv_e, const double* __restrict__ H,
+                                  const double* __restrict__ r, double* __restrict__ z,
+                                  const int32_t* __restrict__ cols, double* __restrict__ part) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    const int col = cols ? cols[c] : c;
+    double rz[1] = {0.0};
+    if (b < nblk) {
+        const int st = bstart[b], en = bstart[b + 1];
+        const double* rc = r + (size_t)col * ld;
+        double s0 = 0, s1 = 0;
+#pragma unroll 4
+        for (int q = st; q < en; ++q) {
+            s0 += rc[q];
+            s1 += t[q] * rc[q];
+        }
+        const double g0 = H[4 * b] * s0 + H[4 * b + 1] * s1, g1 = H[4 * b + 2] * s0 + H[4 * b + 3] * s1;
+        double* zc = z + (size_t)col * ld;
+#pragma unroll 4
+        for (int q = st; q < en; ++q) {
+            const double zv = (rc[q] - g0 - g1 * t[q]) * inv_e;
+            zc[q] = zv;
+            rz[0] += rc[q] * zv;
+        }
+    }
+    if (part) {
+        const int qi[1] = {c};
+        cta_sums<1>(rz, qi, part);
+    }
+}
+
 int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z, const int32_t* cols, int kact,
                   double* rz) {
     auto& c = ctx->coh;
+    if (short_blocks(ctx)) {
+        const int nb = div_up(c.N, TB_THREADS);
+        double* part = nullptr;
+        if (rz) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
+        k_precond_apply_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
+                                                                          1.0 / ctx->vc[0], H, r, z, cols, part);
+        GLOBE_LAUNCHED(ctx, "k_precond_apply_t");
+        if (rz) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rz));
+        return GLOBE_OK;
+    }
     int nb = div_up(c.N, RB_WARPS);
     double* part = nullptr;
     if (rz) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
@@ -358,9 +564,17 @@ __global__ void k_reduce_cols(const double* __restrict__ part, int nparts, const
                               double* __restrict__ out) {
     __shared__ double sm[256];
     const int c = blockIdx.x;
-    double a = 0;
-    for (int j = threadIdx.x; j < nparts; j += blockDim.x) a += part[j + (size_t)c * nparts];
-    sm[threadIdx.x] = a;
+    const double* pc = part + (size_t)c * nparts;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int j = threadIdx.x;
+    for (; j + 3 * (int)blockDim.x < nparts; j += 4 * blockDim.x) {
+        a0 += pc[j];
+        a1 += pc[j + blockDim.x];
+        a2 += pc[j + 2 * blockDim.x];
+        a3 += pc[j + 3 * blockDim.x];
+    }
+    for (; j < nparts; j += blockDim.x) a0 += pc[j];
+    sm[threadIdx.x] = (a0 + a1) + (a2 + a3);
     __syncthreads();
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];

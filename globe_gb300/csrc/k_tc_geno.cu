@@ -33,6 +33,7 @@
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp8.h>
 
 #include "internal.cuh"
 
@@ -419,8 +420,6 @@ __device__ __forceinline__ int kpos(int64_t i) {
     return (int)(i & ~15ll) + ((q & 1) ? 8 + (q >> 1) : (q >> 1));
 }
 
-__constant__ uint8_t E4M3_INT[17] = {0xD0, 0xCE, 0xCC, 0xCA, 0xC8, 0xC4, 0xC0, 0xB8, 0x00,
-                                     0x38, 0x40, 0x44, 0x48, 0x4A, 0x4C, 0x4E, 0x50};
 
 // per-column max |x| and sum over n rows (partials per CTA)
 __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld, double* __restrict__ pmax,
@@ -453,36 +452,98 @@ __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld
     }
 }
 
-// colinfo[c] = {scale exponent e_c (as double), column sum} from partials
+// colinfo[c] = {scale exponent e_c (as double), column sum} from partials; one warp per column
 __global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
                              double* __restrict__ colinfo) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (c >= k) return;
     double mx = 0, sm = 0;
-    for (int j = 0; j < nparts; ++j) {
+    for (int j = lane; j < nparts; j += 32) {
         mx = fmax(mx, pmax[j + (size_t)c * nparts]);
         sm += psum[j + (size_t)c * nparts];
     }
-    int E = 0;
-    if (mx > 0) frexp(mx, &E);
-    colinfo[2 * c] = (double)(E - 3);  // |x 2^-e| < 8
-    colinfo[2 * c + 1] = sm;
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    }
+    if (lane == 0) {
+        int E = 0;
+        if (mx > 0) frexp(mx, &E);
+        colinfo[2 * c] = (double)(E - 3);  // |x 2^-e| < 8
+        colinfo[2 * c + 1] = sm;
+    }
 }
 
-// digits of X (n x k, FP64) into D[(c*NDIG + j) * kpad + kpos(r)]  (e4m3)
+// 2^e sum_j 16^-j P_j of one row.  Every FP32 partial is an exact integer (|P| < 2^24), so
+// the split partials are summed in int64 and the digits combined in two exact int64 halves
+// (hi = digits 0..5, lo = digits 6..11); the only rounding is the final FP64 addition.
+constexpr int NDIG_HI = NDIG / 2;
+__device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
+                                           int64_t row, double s_hi, double s_lo) {
+    long long pj[NDIG];
+#pragma unroll
+    for (int j = 0; j < NDIG; ++j) pj[j] = (long long)__float2int_rn(part[((int64_t)c * NDIG + j) * ldp + row]);
+    for (int y = 1; y < nsplit; ++y) {
+#pragma unroll
+        for (int j = 0; j < NDIG; ++j)
+            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * NDIG + j) * ldp + row]);
+    }
+    long long hi = 0, lo = 0;
+#pragma unroll
+    for (int j = 0; j < NDIG_HI; ++j) hi = hi * 16 + pj[j];
+#pragma unroll
+    for (int j = NDIG_HI; j < NDIG; ++j) lo = lo * 16 + pj[j];
+    return (double)hi * s_hi + (double)lo * s_lo;
+}
+
+// scale factors of recombine for exponent e: 2^(e - 4 (NDIG_HI - 1)) and 2^(e - 4 (NDIG - 1))
+__device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_lo) {
+    s_hi = ldexp(1.0, e - 4 * (NDIG_HI - 1));
+    s_lo = ldexp(1.0, e - 4 * (NDIG - 1));
+}
+
+// digits of X (n x k, FP64) into D[(c*NDIG + j) * kpad + kpos(r)]  (e4m3); every position
+// in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
+// fills 4 consecutive positions P..P+3 (a 32-bit word): within a group of 16, position
+// P < 8 holds row 2P and P >= 8 holds row 2(P-8)+1 (the inverse of kpos).
+// x 2^-e is rounded once to the integer I = round(x 2^-e 16^(NDIG-1)), |I| < 2^47; its
+// balanced base-16 digits are peeled off from the least significant end in integer
+// arithmetic (d = ((I + 8) mod 16) - 8, in [-8, 7]); the leading digit is what remains,
+// in [-8, 8].  sum_j d_j 16^-j equals x 2^-e rounded to 4 (NDIG-1) fraction bits.
+__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-8, 8], exact in e4m3
+    return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
+}
+
 __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
                          uint8_t* __restrict__ D, int64_t kpad) {
     const int c = blockIdx.y;
-    const int e = (int)colinfo[2 * c];
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        double x = ldexp(X[r + c * ld], -e);
-        const int64_t p = kpos(r);
+    const double sc = ldexp(1.0, 4 * (NDIG - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
+    const int64_t nw = kpad >> 2;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = w << 2, base = P & ~(int64_t)15;
+        const int pl = (int)(P & 15);
+        long long I[4];
 #pragma unroll
-        for (int j = 0; j < NDIG; ++j) {
-            const double d = rint(x);
-            x = (x - d) * 16.0;
-            D[((int64_t)c * NDIG + j) * kpad + p] = E4M3_INT[(int)d + 8];
+        for (int q = 0; q < 4; ++q) {
+            const int pq = pl + q;
+            const int64_t src = base + (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1);
+            I[q] = src < n ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
         }
+        uint32_t word[NDIG];
+#pragma unroll
+        for (int j = 0; j < NDIG; ++j) word[j] = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int j = NDIG - 1; j > 0; --j) {
+                const int d = (int)((I[q] + 8) & 15) - 8;
+                I[q] = (I[q] - d) >> 4;   // exact: I - d is a multiple of 16
+                word[j] |= e4m3_int(d) << (8 * q);
+            }
+            word[0] |= e4m3_int((int)I[q]) << (8 * q);
+        }
+#pragma unroll
+        for (int j = 0; j < NDIG; ++j) *reinterpret_cast<uint32_t*>(D + ((int64_t)c * NDIG + j) * kpad + P) = word[j];
     }
 }
 
@@ -493,17 +554,12 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
                            double* __restrict__ psum) {
     __shared__ double smx[32], ssm[32];
     const int c = blockIdx.y;
-    const int e = (int)colinfo[2 * c];
+    double s_hi, s_lo;
+    recombine_scales((int)colinfo[2 * c], s_hi, s_lo);
     const double Sc = colinfo[2 * c + 1];
     double mx = 0, sm = 0;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < rows; s += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0.0, w = 1.0;
-        for (int j = 0; j < NDIG; ++j, w *= 0.0625) {
-            double pj = 0.0;
-            for (int y = 0; y < nsplit; ++y) pj += (double)part[((int64_t)y * nmma + c * NDIG + j) * ldp + s];
-            acc += w * pj;
-        }
-        const double gv = ldexp(acc, e);
+        const double gv = recombine(part, nsplit, nmma, ldp, c, s, s_hi, s_lo);
         const double iv = inv[s], fs = f[s];
         const double u = iv * iv * (gv - 2.0 * fs * Sc);
         U[s + c * rows] = u;
@@ -534,16 +590,11 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
 __global__ void k_combine2(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int64_t rows, int k,
                            const double* __restrict__ colinfo, double scale, double* __restrict__ out, int64_t ldo) {
     const int c = blockIdx.y;
-    const int e = (int)colinfo[2 * c];
+    double s_hi, s_lo;
+    recombine_scales((int)colinfo[2 * c], s_hi, s_lo);
     const double C2 = colinfo[2 * c + 1];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-        double acc = 0.0, w = 1.0;
-        for (int j = 0; j < NDIG; ++j, w *= 0.0625) {
-            double pj = 0.0;
-            for (int y = 0; y < nsplit; ++y) pj += (double)part[((int64_t)y * nmma + c * NDIG + j) * ldp + i];
-            acc += w * pj;
-        }
-        out[i + c * ldo] = scale * (ldexp(acc, e) - C2);
+        out[i + c * ldo] = scale * (recombine(part, nsplit, nmma, ldp, c, i, s_hi, s_lo) - C2);
     }
 }
 
@@ -776,11 +827,14 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     // ---- digits of Z
     k_col_maxsum<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
     GLOBE_LAUNCHED(ctx, "k_col_maxsum");
-    k_col_finish<<<1, 64, 0, ctx->stream>>>(pm, ps, nbr, kg, col1);
+    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col1);
     GLOBE_LAUNCHED(ctx, "k_col_finish");
-    GLOBE_CK(ctx, cudaMemsetAsync(D1, 0, (size_t)nmma * kpad1, ctx->stream));
-    k_digits<<<dim3(div_up(N, 256) < 1024 ? div_up(N, 256) : 1024, kg), 256, 0, ctx->stream>>>(Z, N, N, kg, col1, D1,
-                                                                                                 kpad1);
+    // digit rows past the kg columns stay zero
+    if (nmma > kg * NDIG)
+        GLOBE_CK(ctx, cudaMemsetAsync(D1 + (size_t)kg * NDIG * kpad1, 0, (size_t)(nmma - kg * NDIG) * kpad1,
+                                      ctx->stream));
+    k_digits<<<dim3((unsigned)std::min<int64_t>(div_up(kpad1 / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
+        Z, N, N, kg, col1, D1, kpad1);
     GLOBE_LAUNCHED(ctx, "k_digits");
     // ---- pass 1
     {
@@ -790,12 +844,14 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     const int sp1e = eff_splits(nch1, sp1);
     k_combine1<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
     GLOBE_LAUNCHED(ctx, "k_combine1");
-    k_col_finish<<<1, 64, 0, ctx->stream>>>(pm, ps, nbr, kg, col2);
+    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col2);
     GLOBE_LAUNCHED(ctx, "k_col_finish");
     // ---- digits of u, pass 2
-    GLOBE_CK(ctx, cudaMemsetAsync(D2, 0, (size_t)nmma * kpad2, ctx->stream));
-    k_digits<<<dim3(div_up(g.Mk, 256) < 2048 ? div_up(g.Mk, 256) : 2048, kg), 256, 0, ctx->stream>>>(U, g.Mk, g.Mk, kg,
-                                                                                                       col2, D2, kpad2);
+    if (nmma > kg * NDIG)
+        GLOBE_CK(ctx, cudaMemsetAsync(D2 + (size_t)kg * NDIG * kpad2, 0, (size_t)(nmma - kg * NDIG) * kpad2,
+                                      ctx->stream));
+    k_digits<<<dim3((unsigned)std::min<int64_t>(div_up(kpad2 / 4, 256), 2048), kg), 256, 0, ctx->stream>>>(
+        U, g.Mk, g.Mk, kg, col2, D2, kpad2);
     GLOBE_LAUNCHED(ctx, "k_digits");
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS2);

@@ -48,15 +48,19 @@ def decode_row(packed_row):
 
 
 def digits(col):
+    """Balanced base-16 digits as k_digits forms them: I = round(x 2^-e 16^(NDIG-1)),
+    digits peeled from the least significant end, the leading one what remains."""
     mx = np.abs(col).max()
-    e = (np.frexp(mx)[1] - 3) if mx > 0 else 0
-    x = np.ldexp(col, -e)
+    e = (np.frexp(mx)[1] - 3) if mx > 0 else -3
+    I = np.rint(np.ldexp(col, 4 * (NDIG - 1) - e)).astype(np.int64)
+    assert np.all(np.abs(I) < 2 ** 47)
     D = np.zeros((NDIG, len(col)))
-    for j in range(NDIG):
-        d = np.rint(x)
-        assert np.all(np.abs(d) <= 8)
+    for j in range(NDIG - 1, 0, -1):
+        d = ((I + 8) & 15) - 8
         D[j] = d
-        x = (x - d) * 16.0
+        I = (I - d) >> 4
+    assert np.all(np.abs(I) <= 8)
+    D[0] = I
     return D, e
 
 
