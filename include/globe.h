@@ -42,7 +42,9 @@ extern "C" {
 
 /* precision of the GRM product inside the solver */
 #define GLOBE_PREC_FP64 0   /* plain FP64 everywhere (the drop-in path) */
-#define GLOBE_PREC_MIXED 1  /* low-precision GRM product + FP64 refinement */
+#define GLOBE_PREC_MIXED 1  /* genotype GRM product on the FP8 tensor cores with exact
+                               base-16 digit slicing of the right-hand sides (matches
+                               FP64 to ~1e-14); the dense GRM stays FP64 */
 
 /* PCG stopping rules */
 #define GLOBE_RULE_PCGSOLVER 0 /* max_j |r_j|/|b_j| < tol, or 10 iterations with
@@ -68,7 +70,8 @@ typedef struct {
 
 typedef struct {
     int iters;          /* iterations of the (outer) solve */
-    int inner_iters;    /* low-precision inner iterations (mixed), else = iters */
+    int inner_iters;    /* iterations run by the kernels (equals iters: the mixed
+                           product is FP64-faithful, so there is no inner solve) */
     int64_t rhs_iters;  /* sum over iterations of active columns */
     double max_rel_res; /* max_j |b_j - V x_j| / |b_j| at exit (recurrence) */
     int converged;      /* 1 if the rule was met (not maxit / stagnation) */
