@@ -92,6 +92,7 @@ SIGNATURES = {
     "globe_set_precision": (C.c_int, [_vp, C.c_int]),
     "globe_prof_enable": (C.c_int, [_vp, C.c_int]),
     "globe_prof_query": (C.c_int, [_vp, C.c_int, _i64p, _dp]),
+    "globe_precond_apply_dev_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
     "globe_synth_bed_dev": (C.c_int, [_vp, _vp, C.c_int64, C.c_int32, C.c_int64, C.c_uint64, C.c_float, C.c_float,
                                       C.c_float]),
 }

@@ -200,6 +200,8 @@ int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, 
                double* rr, double* rz);
 int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z,
                   const int32_t* cols, int kact, double* rz);
+int precond_apply_scratch(globe_ctx* ctx, const double* H, const double* r, double* z, int kact, double* part,
+                          size_t part_cap, double* rz);
 int col_dots(globe_ctx* ctx, const double* a, const double* b, int64_t n, int64_t lda, int64_t ldb,
              const int32_t* cols, int kact, double* out);
 int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int kact);

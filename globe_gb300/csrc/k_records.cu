@@ -556,6 +556,33 @@ int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z, c
     return GLOBE_OK;
 }
 
+// Same operator with the r'z partials in caller-provided scratch (part, part_cap
+// doubles): launches kernels only, allocates nothing.  Each CTA writes its own
+// partial slot, so the scratch needs no clearing.
+int precond_apply_scratch(globe_ctx* ctx, const double* H, const double* r, double* z, int kact, double* part,
+                          size_t part_cap, double* rz) {
+    auto& c = ctx->coh;
+    const bool thr = short_blocks(ctx);
+    const int nb = thr ? div_up(c.N, TB_THREADS) : div_up(c.N, RB_WARPS);
+    if (rz && (size_t)nb * kact > part_cap)
+        return set_err(ctx, GLOBE_ERR_ARG,
+                       "r'z partials need %zu doubles of scratch (%d CTAs x %d columns); the static buffer holds %zu",
+                       (size_t)nb * kact, nb, kact, part_cap);
+    double* pp = rz ? part : nullptr;
+    if (thr) {
+        k_precond_apply_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
+                                                                          1.0 / ctx->vc[0], H, r, z, nullptr, pp);
+        GLOBE_LAUNCHED(ctx, "k_precond_apply_t");
+    } else {
+        const size_t sm = rz ? sizeof(double) * RB_WARPS * kact : 0;
+        k_precond_apply<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0], H,
+                                                             r, z, nullptr, kact, pp);
+        GLOBE_LAUNCHED(ctx, "k_precond_apply");
+    }
+    if (rz) GLOBE_RET(reduce_cols(ctx, part, nb, kact, nullptr, rz));
+    return GLOBE_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Column reductions
 

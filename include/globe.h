@@ -166,6 +166,24 @@ int globe_precond_apply(globe_ctx* ctx, const double* r, double* z, int k);
 /* A_ii (computeGeneticDiagonal, PCGsolver.cpp:924-989). */
 int globe_genetic_diag(globe_ctx* ctx, double* diag);
 
+/* z = Q^-1 r on device buffers (Nrec x k, column-major), and d_rz[j] = r_j'z_j
+ * (device, k doubles; may be NULL), without allocating device memory.  No
+ * counterpart in the reference: it is the preconditioner of globe_precond_apply
+ * for callers that may not allocate (e.g. work issued during CUDA stream
+ * capture, or where the implicit device synchronisation of an allocation is
+ * not allowed).
+ *  - The r'z partials use one static 2 MiB device buffer (2^18 doubles).  A
+ *    call needing more (about k x N/256 doubles, or k x N/8 when an individual
+ *    has more than 48 records) returns GLOBE_ERR_ARG before launching
+ *    anything.  Nothing in the buffer needs to start at zero.
+ *  - The buffer is shared by every context on a device: calls that overlap
+ *    on the GPU (other streams or contexts on the same device) race on it.
+ *  - The preconditioner must already be built at the current components
+ *    (globe_precond_apply or globe_pcg once); otherwise GLOBE_ERR_STATE.
+ *  - The first call on a device looks up the buffer's address; make that
+ *    first call before any stream capture. */
+int globe_precond_apply_dev_noalloc(globe_ctx* ctx, const double* d_r, double* d_z, int k, double* d_rz);
+
 /* ---- solves ----------------------------------------------------------- */
 
 /* Solve V X = B (Nrec x k) by block PCG (runPCG_multi,
