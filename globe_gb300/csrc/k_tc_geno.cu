@@ -65,15 +65,22 @@ constexpr int DSTAGES = TC_DSTAGES;  // decoded-A ring
 // its issuing context ~157 cycles whatever N is, so small-N products need
 // several concurrent issue streams to use the tensor pipe; TMEM (512
 // columns) bounds MT * NMMA + DSTAGES * MT * 32.
+// Decoders: two sets of 8 warps take the stages in turn (set = stage parity, so
+// each set owns one slot of the decoded-A ring) -- one set's load / TMEM-store
+// latency overlaps the other set's decode.  Within a set, warp (quadrant q, j)
+// covers TMEM lanes 32q..32q+31 of the 16-byte units u = j*MT .. j*MT+MT-1 of a
+// row (unit u = tile u/2, half u%2).
 template <int NMMA>
 struct Geo {
     static constexpr int MT = NMMA <= 64 ? 4 : (NMMA <= 192 ? 2 : 1);
-    static constexpr int DECW = MT >= 2 ? 16 : 8;          // decoder warps
+    static constexpr int NSET = 2;                         // decoder sets
+    static constexpr int DECW = 16;                        // decoder warps (NSET x 4 quadrants x 2)
     static constexpr int DBASE = MT > 2 ? 8 : 4;           // first decoder warp (multiple of 4)
     static constexpr int NTHREADS = (DBASE + DECW) * 32;
-    static constexpr int NH = MT == 4 ? 2 : 1;             // 16-byte halves per decoder thread
-    static constexpr int DPT = DECW / MT;                  // decoder warps per tile
-    static constexpr int CPARTS = DPT / 4;                 // warps per TMEM quadrant in the epilogue
+    static constexpr int UPW = MT;                         // 16-byte units per warp and stage
+    static constexpr int TPW = MT >= 2 ? MT / 2 : 1;       // tiles per warp
+    static constexpr int DPT = MT >= 2 ? 4 : 8;            // warps of one set per tile (adfull count)
+    static constexpr int ES = MT >= 2 ? 2 : 4;             // warps sharing a (tile, quadrant) epilogue
 };
 constexpr int NDIG = 12;          // digits per right-hand-side column
 constexpr int MAX_RHS_GROUP = 21; // 21 * 12 = 252 <= 256 MMA columns
@@ -260,7 +267,7 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < ASTAGES; ++s) {
             mbar_init(&S.afull[s], 1);
-            mbar_init(&S.aempty[s], G::DECW);
+            mbar_init(&S.aempty[s], G::DECW / G::NSET);
         }
         for (int s = 0; s < BSTAGES; ++s) {
             mbar_init(&S.bfull[s], 1);
@@ -338,66 +345,76 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
             mma_commit(&S.accfull[m]);  // tracks every MMA this thread issued
         }
     } else if (warp >= G::DBASE) {
-        // decoders: warp -> TMEM lane quadrant (warp % 4); group g picks the tile and the 16-byte half(s)
-        const int quad = warp & 3, g = (warp - G::DBASE) >> 2;
-        const int m = g % MT;                          // tile
-        const int hsel = g / MT;                       // half (NH == 1) / column part (epilogue)
-        const int r = quad * 32 + lane;                // row within the tile
+        static_assert(DSTAGES % G::NSET == 0 && ASTAGES % G::NSET == 0, "each ring slot belongs to one decoder set");
+        const int dw = warp - G::DBASE;
+        const int set = dw >> 3, j = (dw >> 2) & 1, quad = warp & 3;
+        const int t0 = (j * MT) >> 1;                  // first tile of this warp
+        const int r = quad * 32 + lane;                // row within a tile
         const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
         const int swz = (r >> 2) & 1;
         bool ok = true;
-        for (int it = 0; it < nloc && ok; ++it) {
+        for (int it = set; it < nloc && ok; it += G::NSET) {
             const int sa = it % ASTAGES, ds = it % DSTAGES;
             if (!mbar_wait<TC_SLEEP_DEC != 0>(&S.afull[sa], (it / ASTAGES) & 1, abort, err, 16u)) { ok = false; break; }
-            if (it >= DSTAGES &&
-                !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[m][ds], ((it / DSTAGES) - 1) & 1, abort, err, 32u)) {
-                ok = false;
-                break;
-            }
-            constexpr int NH = G::NH;
-            uint4 v[NH];
+            if (it >= DSTAGES) {
 #pragma unroll
-            for (int j = 0; j < NH; ++j) {
-                const int h = (NH == 2) ? j : hsel;    // logical half
-                v[j] = *reinterpret_cast<const uint4*>(S.pk[sa] + m * (BM * PKB) + (r * 2 + (h ^ swz)) * 16);
+                for (int q = 0; q < G::TPW; ++q)
+                    if (ok && !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[t0 + q][ds], ((it / DSTAGES) - 1) & 1, abort,
+                                                            err, 32u))
+                        ok = false;
+                if (!ok) break;
             }
-            uint32_t o[NH][16];
+            uint4 v[G::UPW];
 #pragma unroll
-            for (int j = 0; j < NH; ++j) {
-                decode_word(v[j].x, o[j][0], o[j][1], o[j][2], o[j][3]);
-                decode_word(v[j].y, o[j][4], o[j][5], o[j][6], o[j][7]);
-                decode_word(v[j].z, o[j][8], o[j][9], o[j][10], o[j][11]);
-                decode_word(v[j].w, o[j][12], o[j][13], o[j][14], o[j][15]);
+            for (int i = 0; i < G::UPW; ++i) {
+                const int u = j * MT + i, m = u >> 1, h = u & 1;
+                v[i] = *reinterpret_cast<const uint4*>(S.pk[sa] + m * (BM * PKB) + (r * 2 + (h ^ swz)) * 16);
+            }
+            uint32_t o[G::UPW][16];
+#pragma unroll
+            for (int i = 0; i < G::UPW; ++i) {
+                decode_word(v[i].x, o[i][0], o[i][1], o[i][2], o[i][3]);
+                decode_word(v[i].y, o[i][4], o[i][5], o[i][6], o[i][7]);
+                decode_word(v[i].z, o[i][8], o[i][9], o[i][10], o[i][11]);
+                decode_word(v[i].w, o[i][12], o[i][13], o[i][14], o[i][15]);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.aempty[sa]);   // packed stage consumed
 #pragma unroll
-            for (int j = 0; j < NH; ++j) {
-                const int h = (NH == 2) ? j : hsel;
-                tmem_st16(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[j]);
+            for (int i = 0; i < G::UPW; ++i) {
+                const int u = j * MT + i, m = u >> 1, h = u & 1;
+                tmem_st16(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[i]);
             }
             tmem_wait_st();
             tc_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&S.adfull[m][ds]);
+            if (lane == 0) {
+#pragma unroll
+                for (int q = 0; q < G::TPW; ++q) mbar_arrive(&S.adfull[t0 + q][ds]);
+            }
         }
-        // epilogue: the tile's warps of one quadrant split the accumulator columns
-        bool go = ok && nloc > 0;
-        if (go) go = mbar_wait(&S.accfull[m], 0, abort, err, 64u);
-        go = __all_sync(0xffffffffu, go);   // tcgen05.ld is warp-collective
-        if (go) {
+        // epilogue: the ES warps covering a (tile, quadrant) split its accumulator columns
+        const int e0 = MT >= 2 ? set : set * 2 + j;
+#pragma unroll 1
+        for (int q = 0; q < G::TPW; ++q) {
+            const int m = t0 + q;
+            bool go = ok && nloc > 0;
+            if (go) go = mbar_wait(&S.accfull[m], 0, abort, err, 64u);
+            go = __all_sync(0xffffffffu, go);   // tcgen05.ld is warp-collective
+            if (!go) {
+                ok = false;
+                continue;
+            }
             tc_after();
-            constexpr int CW = NMMA / G::CPARTS;
-            const int part_id = (G::CPARTS == 1) ? 0 : hsel;
             const int rr = row0 + m * BM + r;
 #pragma unroll 1
-            for (int cb = part_id * CW; cb < (part_id + 1) * CW; cb += 16) {
+            for (int cb = e0 * 16; cb < NMMA; cb += G::ES * 16) {
                 uint32_t acc[16];
                 tmem_ld16(tmem + lane_addr + (uint32_t)(m * NMMA + cb), acc);
                 if (rr < rows) {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        part[((int64_t)split * NMMA + cb + j) * ldp + rr] = __uint_as_float(acc[j]);
+                    for (int jj = 0; jj < 16; ++jj)
+                        part[((int64_t)split * NMMA + cb + jj) * ldp + rr] = __uint_as_float(acc[jj]);
                 }
             }
         }
