@@ -43,6 +43,8 @@ CONFIGS = {
     # name: N, M, record distribution, T, maf_lo, maf_hi, miss
     "precision": dict(N=100_000, M=500_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
                       label="N=100k indiv, M=500k 2-bit SNPs, ~700k records, k=5 RHS ([X y])"),
+    "mid": dict(N=100_000, M=50_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
+                label="N=100k indiv, M=50k 2-bit SNPs (1.25 GB), ~700k records, k=5 (profiling size)"),
     "small": dict(N=20_000, M=40_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
                   label="N=20k indiv, M=40k SNPs, ~140k records, k=5"),
     "c1": dict(N=2_000, M=10_000, recs=("uniform", 3, 10), T=5.0, maf_lo=0.05, maf_hi=0.5, miss=0.01,

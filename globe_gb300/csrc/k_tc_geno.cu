@@ -8,11 +8,12 @@
 //   pass 2:  P2[i,c] = sum_s g(s,i) u[s,c]        (rows = individuals, K = SNPs)
 //            out[i,c] = scale (P2[i,c] - sum_s 2 f_s u[s,c])
 // g in {0,1,2} is exact in FP8 e4m3.  Each right-hand-side column is split
-// into base-16 digits: x = 2^e sum_j d_j 16^-j with integer d_j in [-8,8],
-// also exact in e4m3.  |g d| <= 16, so an FP32 sum of up to 2^20 such
-// products is an exact integer: the tensor-core accumulation carries no
-// rounding, and the digits are recombined in FP64.  With 12 digits the
-// product matches an FP64 evaluation to ~1e-14 relative.
+// into balanced base-32 digits: x = 2^e sum_j d_j 32^-j with integer d_j in
+// [-16,16], also exact in e4m3 (every integer up to 16 is).  |g d| <= 32, so an
+// FP32 sum of up to 2^19 such products is an exact integer: the tensor-core
+// accumulation carries no rounding, and the digits are recombined in int64 /
+// FP64.  With 9 digits (45 bits) the product matches an FP64 evaluation to
+// ~1e-13 relative.
 //
 // Kernel (one CTA = MT x 128 rows x one K range, M=128 x N=NMMA MMAs per tile):
 //   warp 0     bulk copies of the packed 2-bit tiles (tile-blocked layout: each
@@ -82,8 +83,10 @@ struct Geo {
     static constexpr int DPT = MT >= 2 ? 4 : 8;            // warps of one set per tile (adfull count)
     static constexpr int ES = MT >= 2 ? 2 : 4;             // warps sharing a (tile, quadrant) epilogue
 };
-constexpr int NDIG = 12;          // digits per right-hand-side column
-constexpr int MAX_RHS_GROUP = 21; // 21 * 12 = 252 <= 256 MMA columns
+constexpr int DBITS = 5;          // digit base 32
+constexpr int DHALF = 1 << (DBITS - 1);   // 16: digits in [-16, 16]
+constexpr int NDIG = 9;           // digits per right-hand-side column (45 bits)
+constexpr int MAX_RHS_GROUP = 28; // 28 * 9 = 252 <= 256 MMA columns
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
 constexpr uint32_t LUT_G = 0x00380040u;  // code 00 -> 2.0 (0x40), 01 -> 0, 10 -> 1.0 (0x38), 11 -> 0
 
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
               int cps, float* __restrict__ part, int64_t ldp, unsigned* __restrict__ err) {
     using G = Geo<NMMA>;
     constexpr int MT = G::MT;
-    static_assert(NMMA % 32 == 0 && NMMA >= 32 && NMMA <= 256, "NMMA");
+    static_assert(NMMA % 16 == 0 && NMMA >= 16 && NMMA <= 256, "NMMA");
     constexpr int ACOL0 = MT * NMMA;                     // first TMEM column of the decoded A stages
     static_assert(MT * NMMA + DSTAGES * MT * 32 <= 512, "TMEM columns");
     constexpr uint32_t NCOLS = ncols_alloc(MT * NMMA + DSTAGES * MT * 32);
@@ -486,15 +489,15 @@ __global__ void k_col_finish(const double* __restrict__ pmax, const double* __re
     if (lane == 0) {
         int E = 0;
         if (mx > 0) frexp(mx, &E);
-        colinfo[2 * c] = (double)(E - 3);  // |x 2^-e| < 8
+        colinfo[2 * c] = (double)(E - (DBITS - 1));  // |x 2^-e| < 16
         colinfo[2 * c + 1] = sm;
     }
 }
 
-// 2^e sum_j 16^-j P_j of one row.  Every FP32 partial is an exact integer (|P| < 2^24), so
+// 2^e sum_j 32^-j P_j of one row.  Every FP32 partial is an exact integer (|P| < 2^24), so
 // the split partials are summed in int64 and the digits combined in two exact int64 halves
-// (hi = digits 0..5, lo = digits 6..11); the only rounding is the final FP64 addition.
-constexpr int NDIG_HI = NDIG / 2;
+// (hi = digits 0..4, lo = digits 5..8); the only rounding is the final FP64 addition.
+constexpr int NDIG_HI = (NDIG + 1) / 2;
 __device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
                                            int64_t row, double s_hi, double s_lo) {
     long long pj[NDIG];
@@ -507,34 +510,34 @@ __device__ __forceinline__ double recombine(const float* __restrict__ part, int 
     }
     long long hi = 0, lo = 0;
 #pragma unroll
-    for (int j = 0; j < NDIG_HI; ++j) hi = hi * 16 + pj[j];
+    for (int j = 0; j < NDIG_HI; ++j) hi = hi * (1 << DBITS) + pj[j];
 #pragma unroll
-    for (int j = NDIG_HI; j < NDIG; ++j) lo = lo * 16 + pj[j];
+    for (int j = NDIG_HI; j < NDIG; ++j) lo = lo * (1 << DBITS) + pj[j];
     return (double)hi * s_hi + (double)lo * s_lo;
 }
 
-// scale factors of recombine for exponent e: 2^(e - 4 (NDIG_HI - 1)) and 2^(e - 4 (NDIG - 1))
+// scale factors of recombine for exponent e: 2^(e - 5 (NDIG_HI - 1)) and 2^(e - 5 (NDIG - 1))
 __device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_lo) {
-    s_hi = ldexp(1.0, e - 4 * (NDIG_HI - 1));
-    s_lo = ldexp(1.0, e - 4 * (NDIG - 1));
+    s_hi = ldexp(1.0, e - DBITS * (NDIG_HI - 1));
+    s_lo = ldexp(1.0, e - DBITS * (NDIG - 1));
 }
 
 // digits of X (n x k, FP64) into D[(c*NDIG + j) * kpad + kpos(r)]  (e4m3); every position
 // in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
 // fills 4 consecutive positions P..P+3 (a 32-bit word): within a group of 16, position
 // P < 8 holds row 2P and P >= 8 holds row 2(P-8)+1 (the inverse of kpos).
-// x 2^-e is rounded once to the integer I = round(x 2^-e 16^(NDIG-1)), |I| < 2^47; its
-// balanced base-16 digits are peeled off from the least significant end in integer
-// arithmetic (d = ((I + 8) mod 16) - 8, in [-8, 7]); the leading digit is what remains,
-// in [-8, 8].  sum_j d_j 16^-j equals x 2^-e rounded to 4 (NDIG-1) fraction bits.
-__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-8, 8], exact in e4m3
+// x 2^-e is rounded once to the integer I = round(x 2^-e 32^(NDIG-1)), |I| < 2^44; its
+// balanced base-32 digits are peeled off from the least significant end in integer
+// arithmetic (d = ((I + 16) mod 32) - 16, in [-16, 15]); the leading digit is what
+// remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (NDIG-1) fraction bits.
+__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], exact in e4m3
     return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
 }
 
 __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
                          uint8_t* __restrict__ D, int64_t kpad) {
     const int c = blockIdx.y;
-    const double sc = ldexp(1.0, 4 * (NDIG - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
+    const double sc = ldexp(1.0, DBITS * (NDIG - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
     const int64_t nw = kpad >> 2;
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t P = w << 2, base = P & ~(int64_t)15;
@@ -553,8 +556,8 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
         for (int q = 0; q < 4; ++q) {
 #pragma unroll
             for (int j = NDIG - 1; j > 0; --j) {
-                const int d = (int)((I[q] + 8) & 15) - 8;
-                I[q] = (I[q] - d) >> 4;   // exact: I - d is a multiple of 16
+                const int d = (int)((I[q] + DHALF) & (2 * DHALF - 1)) - DHALF;
+                I[q] = (I[q] - d) >> DBITS;   // exact: I - d is a multiple of 32
                 word[j] |= e4m3_int(d) << (8 * q);
             }
             word[0] |= e4m3_int((int)I[q]) << (8 * q);
@@ -564,7 +567,7 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
     }
 }
 
-// pass-1 epilogue in FP64: u[s,c] = inv_s^2 (2^e_c sum_j 16^-j P1 - 2 f_s S_c); partial max|u|, sum 2 f u
+// pass-1 epilogue in FP64: u[s,c] = inv_s^2 (2^e_c sum_j 32^-j P1 - 2 f_s S_c); partial max|u|, sum 2 f u
 __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int64_t rows, int k,
                            const double* __restrict__ colinfo, const double* __restrict__ f,
                            const double* __restrict__ inv, double* __restrict__ U, double* __restrict__ pmax,
@@ -603,7 +606,7 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
     }
 }
 
-// pass-2 epilogue: out[i,c] = scale (2^e_c sum_j 16^-j P2 - C2_c)
+// pass-2 epilogue: out[i,c] = scale (2^e_c sum_j 32^-j P2 - C2_c)
 __global__ void k_combine2(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int64_t rows, int k,
                            const double* __restrict__ colinfo, double scale, double* __restrict__ out, int64_t ldo) {
     const int c = blockIdx.y;
@@ -782,13 +785,21 @@ static int rows_per_cta(int nmma) { return BM * (nmma <= 64 ? 4 : (nmma <= 192 ?
 static int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* mA, const CUtensorMap& mB, int rows,
                          int nchunks, int splits, float* part, int64_t ldp, unsigned* err) {
     switch (nmma) {
+        case 16: return launch_gemm<16>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 32: return launch_gemm<32>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 48: return launch_gemm<48>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 64: return launch_gemm<64>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 80: return launch_gemm<80>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 96: return launch_gemm<96>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 112: return launch_gemm<112>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 128: return launch_gemm<128>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 144: return launch_gemm<144>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 160: return launch_gemm<160>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 176: return launch_gemm<176>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 192: return launch_gemm<192>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 208: return launch_gemm<208>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 224: return launch_gemm<224>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 240: return launch_gemm<240>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
         case 256: return launch_gemm<256>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
     }
     return set_err(ctx, GLOBE_ERR_ARG, "unsupported MMA width %d", nmma);
@@ -803,7 +814,7 @@ static int pick_splits(int tiles, int nchunks) {
     int want = (8 * 152 + tiles - 1) / tiles;        // >= ~8 CTA waves
     int maxs = std::max(1, nchunks / 8);              // >= 8 stages per CTA
     want = std::min(want, maxs);
-    want = std::max(want, (nchunks + 8191) / 8192);   // K per CTA <= 2^20 (exact FP32 sums)
+    want = std::max(want, (nchunks + 4095) / 4096);   // K per CTA <= 2^19 (exact FP32 sums)
     return std::max(1, want);
 }
 
@@ -811,7 +822,7 @@ static int pick_splits(int tiles, int nchunks) {
 static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, double* out) {
     auto& g = ctx->gen;
     const int32_t N = ctx->coh.N;
-    const int nmma = ((kg * NDIG + 31) / 32) * 32;
+    const int nmma = ((kg * NDIG + 15) / 16) * 16;
     // ---- pass 1 operands
     const int nch1 = g.nch1;
     const int64_t kpad1 = (int64_t)nch1 * BK;
@@ -889,9 +900,12 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
         return GLOBE_OK;
     }
     GLOBE_RET(ensure_gt(ctx));
-    for (int c0 = 0; c0 < k; c0 += MAX_RHS_GROUP) {
-        const int kg = std::min(MAX_RHS_GROUP, k - c0);
+    // near-equal groups of <= MAX_RHS_GROUP columns (e.g. 65 -> 22 + 22 + 21)
+    const int ng = (k + MAX_RHS_GROUP - 1) / MAX_RHS_GROUP;
+    for (int gi = 0, c0 = 0; gi < ng; ++gi) {
+        const int kg = k / ng + (gi < k % ng ? 1 : 0);
         GLOBE_RET(tc_group(ctx, Z + (size_t)c0 * N, kg, scale, out + (size_t)c0 * N));
+        c0 += kg;
     }
     return GLOBE_OK;
 }

@@ -9,7 +9,8 @@ from helpers import cohort, rel
 
 LUT_G = 0x00380040
 E4M3 = {0x00: 0.0, 0x38: 1.0, 0x40: 2.0}
-NDIG = 12
+NDIG = 9      # balanced base-32 digits
+DBITS = 5
 
 
 def byte_perm(x, s):
@@ -48,18 +49,18 @@ def decode_row(packed_row):
 
 
 def digits(col):
-    """Balanced base-16 digits as k_digits forms them: I = round(x 2^-e 16^(NDIG-1)),
+    """Balanced base-32 digits as k_digits forms them: I = round(x 2^-e 32^(NDIG-1)),
     digits peeled from the least significant end, the leading one what remains."""
     mx = np.abs(col).max()
-    e = (np.frexp(mx)[1] - 3) if mx > 0 else -3
-    I = np.rint(np.ldexp(col, 4 * (NDIG - 1) - e)).astype(np.int64)
-    assert np.all(np.abs(I) < 2 ** 47)
+    e = (np.frexp(mx)[1] - (DBITS - 1)) if mx > 0 else -(DBITS - 1)
+    I = np.rint(np.ldexp(col, DBITS * (NDIG - 1) - e)).astype(np.int64)
+    assert np.all(np.abs(I) < 2 ** 44)
     D = np.zeros((NDIG, len(col)))
     for j in range(NDIG - 1, 0, -1):
-        d = ((I + 8) & 15) - 8
+        d = ((I + 16) & 31) - 16
         D[j] = d
-        I = (I - d) >> 4
-    assert np.all(np.abs(I) <= 8)
+        I = (I - d) >> DBITS
+    assert np.all(np.abs(I) <= 16)
     D[0] = I
     return D, e
 
@@ -100,7 +101,7 @@ def test_product_emulation_matches_oracle(orc):
             B[:, kpos(i)] = D[:, i]
         P = A1 @ B.T                       # exact integers
         assert np.all(P == np.rint(P)) and np.abs(P).max() < 2 ** 24
-        gv = np.ldexp(P @ (16.0 ** -np.arange(NDIG)), e)
+        gv = np.ldexp(P @ (32.0 ** -np.arange(NDIG)), e)
         U[:, c] = inv ** 2 * (gv - 2 * f * Z[:, c].sum())
     # pass 2: rows = individuals, K = SNPs (individual-major codes)
     Gk = synth.unpack_genotypes(kept, N)              # Mk x N, -1 missing
@@ -109,6 +110,6 @@ def test_product_emulation_matches_oracle(orc):
     for c in range(3):
         D, e = digits(U[:, c])
         P2 = Gt @ D.T
-        out[:, c] = np.ldexp(P2 @ (16.0 ** -np.arange(NDIG)), e) - 2 * (f * U[:, c]).sum()
+        out[:, c] = np.ldexp(P2 @ (32.0 ** -np.arange(NDIG)), e) - 2 * (f * U[:, c]).sum()
     out *= 0.4 / Mk
     assert rel(out, s.grm_apply(Z)) < 1e-12
