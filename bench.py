@@ -16,6 +16,12 @@ GRM on the packed genotypes + the PCG vector updates).  ``value`` is the
 device-resident throughput; ``e2e`` is the same through globe_pcg with pinned
 host buffers (B copied in, X copied out inside the timed region).
 
+The same run also reports AIREML time to converge (numMC=15, tol 1e-3, same
+probes for both precisions): ``aireml`` on this workload with the selected
+precision, and ``aireml_mixed_vs_fp64`` on a smaller cohort (N=20k, M=20k)
+where the plain FP64 path also finishes in seconds.  The phenotype's genetic
+term is computed from the generated genotypes (``genetic_values``).
+
 ``--impl reference`` times the reference algorithm on the host cores: the
 FP32 OpenMP restatement of computeVx_multi with the reference's loop
 structure (oracle/globe_oracle.c, orc_ref_vx_f32) on a SNP subsample of the
@@ -111,11 +117,40 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_records(cfg, seed=SEED):
+def make_records(cfg, seed=SEED, iid_genetic=True):
+    """Record table of the workload.  iid_genetic=False leaves the genetic term
+    out of y (it is added from the genotypes by genetic_values)."""
     from globe_gb300 import synth
-    coh = synth.simulate_cohort(seed, cfg["N"], 0, cfg["recs"], cfg["T"], vc=VC, exact_genetic=False)
+    vc = VC if iid_genetic else (VC[0], 0.0, VC[2], VC[3], VC[4])
+    coh = synth.simulate_cohort(seed, cfg["N"], 0, cfg["recs"], cfg["T"], vc=vc, exact_genetic=False)
     X = np.asfortranarray(np.column_stack([coh["cov"], coh["times"]]))
     return coh["indiv"].astype(np.int32), X, coh["y"], cfg["N"]
+
+
+def genetic_values(torch, raw, M, N, s2g, seed, chunk=2048):
+    """u = Zs' w sqrt(s2g / M_kept) from packed genotypes on the GPU (torch, chunks of SNPs):
+    the genetic term of the simulated phenotype, zs standardised as the reference does
+    (A1 frequency over non-missing samples, missing genotype -> 0, MAF/missingness filter)."""
+    bps = (N + 3) // 4
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    w = torch.randn(M, generator=gen, device="cuda", dtype=torch.float32)
+    lut = torch.tensor([2.0, 0.0, 1.0, 0.0], device="cuda")      # code -> A1 count, missing -> 0
+    u = torch.zeros(N, dtype=torch.float64, device="cuda")
+    kept = 0
+    for s0 in range(0, M, chunk):
+        b = raw[s0:s0 + chunk, :bps]
+        codes = torch.stack([(b >> (2 * j)) & 3 for j in range(4)], dim=2).reshape(b.shape[0], bps * 4)[:, :N].long()
+        g = lut[codes]
+        nobs = (codes != 1).sum(1).clamp(min=1).float()
+        f = g.sum(1) / (2.0 * nobs)
+        miss = 1.0 - nobs / N
+        keep = (f >= 0.01) & (f <= 0.99) & (miss <= 0.2)
+        sd = torch.sqrt(2.0 * f * (1.0 - f)).clamp(min=1e-6)
+        ww = torch.where(keep, w[s0:s0 + chunk] / sd, torch.zeros_like(sd))
+        u += ((g - 2.0 * f[:, None]) * ww[:, None]).sum(0).double()
+        kept += int(keep.sum())
+    return (u * np.sqrt(s2g / max(kept, 1))).cpu().numpy()
 
 
 def cpu_reference_vx(indiv, X, packed_rows, maf_rows, N, k, rng):
@@ -144,6 +179,35 @@ def cpu_baseline(indiv, X, N, Mk, k, sample_rows, sample_maf, budget_s=12.0):
             "record ops %.3fs; per-SNP %.3g s extrapolated to all SNPs: %.2f s per PCG iteration"
             % (ms2, Mk, N, k, t_rec, per_snp, t_matvec))
     return k / t_matvec, desc, threads
+
+
+AIREML_THETA0 = (0.5, 0.3, 0.2, 0.1, 0.1)
+AIREML_CMP = dict(N=20_000, M=20_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, miss=0.02)
+
+
+def aireml_compare(G):
+    """AIREML to convergence with the mixed and the plain FP64 GRM product on one
+    smaller cohort (N=20k, M=20k, genotype-linked y), same probes: time and agreement."""
+    from globe_gb300 import synth
+    c = AIREML_CMP
+    coh = synth.simulate_cohort(SEED + 3, c["N"], c["M"], c["recs"], c["T"], maf_lo=c["maf_lo"], miss_rate=c["miss"])
+    X = np.asfortranarray(np.column_stack([coh["cov"], coh["times"]]))
+    out = {}
+    for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+        with G.Context(0) as cx:
+            cx.load_records(coh["indiv"].astype(np.int32), X, coh["y"], c["N"])
+            cx.load_bed(coh["packed"])
+            cx.set_vc(G.as_float_vc(AIREML_THETA0))
+            cx.synchronize()
+            t0 = time.perf_counter()
+            r = cx.aireml_run(theta0=AIREML_THETA0, maxiter=50, tol=1e-3, numMC=15, precision=prec, seed=SEED)
+            out[name] = (time.perf_counter() - t0, r)
+    (tm, rm), (tf, rf) = out["mixed"], out["fp64"]
+    return {"workload": "N=20k indiv, M=20k SNPs, ~140k records, numMC=15, tol 1e-3, same probes",
+            "mixed_seconds": tm, "fp64_seconds": tf, "speedup": tf / tm,
+            "iterations": [rm["iterations"], rf["iterations"]],
+            "max_rel_theta_diff": float(np.max(np.abs(rm["theta"] - rf["theta"]) / np.abs(rf["theta"]))),
+            "theta_fp64": [float(v) for v in rf["theta"]]}
 
 
 def dist_info():
@@ -198,14 +262,15 @@ def run_ours(args, cfg):
     torch.cuda.set_device(device)
     prec = G.PREC_MIXED if args.precision == "mixed" else G.PREC_FP64
     ctx = G.Context(device)
-    indiv, X, y, N = make_records(cfg)
-    ctx.load_records(indiv, X, y, N)
+    indiv, X, y, N = make_records(cfg, iid_genetic=False)
     Nrec = len(indiv)
     bps = (N + 3) // 4
     stride = (bps + 15) // 16 * 16
     M = cfg["M"]
     raw = torch.empty((M, stride), dtype=torch.uint8, device="cuda")
     ctx.synth_bed_dev(raw.data_ptr(), M, N, stride, SEED + 7919 * rank, cfg["maf_lo"], cfg["maf_hi"], cfg["miss"])
+    y = y + genetic_values(torch, raw, M, N, VC[1], SEED + 1)[indiv]     # genotype-linked genetic term
+    ctx.load_records(indiv, X, y, N)
     Mk = ctx.load_bed_dev(raw.data_ptr(), M, stride)
     # a host copy of some kept-looking rows for the CPU baseline (rank 0)
     sample_rows = raw[: min(M, 4096)].cpu().numpy()[:, :bps].copy() if rank == 0 else None
@@ -294,6 +359,18 @@ def run_ours(args, cfg):
         fp64 = {"value": u64 / (t64 / 1000.0), "unit": "RHS*iters/s", "ms_per_iteration": t64 / 2,
                 "speedup_of_mixed": value / (u64 / (t64 / 1000.0))}
 
+    # AIREML time to converge on this workload (genotype GRM, numMC=15, tol 1e-3) -- replicas skip it
+    aireml = None
+    if not args.no_aireml and world == 1:
+        barrier()
+        t0 = time.perf_counter()
+        r = ctx.aireml_run(theta0=AIREML_THETA0, maxiter=50, tol=1e-3, numMC=15, precision=prec, seed=SEED)
+        t_air = time.perf_counter() - t0
+        aireml = {"workload": args.config + " (same genotypes and records)", "precision": args.precision,
+                  "seconds_to_converge": t_air, "converged": bool(r["converged"]), "iterations": r["iterations"],
+                  "grad_evals": r["grad_evals"], "pcg_rhs_iters": r["pcg_rhs_iters"],
+                  "theta": [float(v) for v in r["theta"]], "numMC": 15, "tol": 1e-3}
+
     # roofline of the dominant GRM kernel (one genotype pass per launch)
     hbm, bf16, peak_src = load_peaks()
     n1, ms1 = prof[G._lib.PROF_GRM_PASS1]
@@ -326,6 +403,10 @@ def run_ours(args, cfg):
             "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches)}
     if fp64 is not None:
         line["fp64_plain"] = fp64
+    if aireml is not None:
+        line["aireml"] = aireml
+    if rank == 0 and world == 1 and not args.no_aireml and prec != G.PREC_FP64:
+        line["aireml_mixed_vs_fp64"] = aireml_compare(G)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle
         alt, miss, maf, _, keep = oracle.bed_stats(sample_rows, N)
@@ -350,6 +431,7 @@ def main():
     ap.add_argument("--iters", type=int, default=0, help="PCG iterations per step (0: 10 mixed, 1 fp64)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the in-run FP64-plain comparison")
+    ap.add_argument("--no-aireml", action="store_true", help="skip the AIREML time-to-converge runs")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     if args.iters <= 0:

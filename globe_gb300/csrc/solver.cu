@@ -390,8 +390,8 @@ int globe_pcg(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg
     return GLOBE_OK;
 }
 
-int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat, double* vinv_r,
-              globe_pcg_info* info) {
+static int mme_impl(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat,
+                    double* vinv_r, globe_pcg_info* info) {
     if (!ctx || !opts) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
@@ -442,8 +442,8 @@ int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* 
     return GLOBE_OK;
 }
 
-int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
-                      double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
+static int aireml_grad_impl(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
+                            double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
     if (!ctx || !opts || numMC < 1) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
@@ -508,6 +508,47 @@ int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t 
     if (f_theta) GLOBE_RET(d2h(ctx, f_theta, fth, (size_t)n * 5));
     ctx->fth_ok = true;
     return GLOBE_OK;
+}
+
+// The GRM products outside the PCG solves (u-hat, the probes' u-hat) run at the
+// precision of the solve: opts->precision holds for the whole call.
+struct PrecScope {
+    globe_ctx* ctx;
+    int saved;
+    PrecScope(globe_ctx* c, int p) : ctx(c), saved(c->prec) { c->prec = p; }
+    ~PrecScope() { ctx->prec = saved; }
+};
+
+static int check_prec(globe_ctx* ctx, const globe_pcg_opts* o) {
+    if (o->precision != GLOBE_PREC_FP64 && o->precision != GLOBE_PREC_MIXED)
+        return set_err(ctx, GLOBE_ERR_ARG, "unknown precision mode %d", o->precision);
+    return GLOBE_OK;
+}
+
+int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat, double* vinv_r,
+              globe_pcg_info* info) {
+    if (!ctx || !opts) return GLOBE_ERR_ARG;
+    GLOBE_RET(check_prec(ctx, opts));
+    int rc;
+    {
+        PrecScope ps(ctx, opts->precision);
+        rc = mme_impl(ctx, opts, beta, uhat, bhat, vinv_r, info);
+    }
+    if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
+    return rc;
+}
+
+int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
+                      double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
+    if (!ctx || !opts) return GLOBE_ERR_ARG;
+    GLOBE_RET(check_prec(ctx, opts));
+    int rc;
+    {
+        PrecScope ps(ctx, opts->precision);
+        rc = aireml_grad_impl(ctx, probes, numMC, seed, opts, f_theta, first, trace, grad, info);
+    }
+    if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
+    return rc;
 }
 
 int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai, globe_pcg_info* info) {

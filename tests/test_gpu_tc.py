@@ -62,3 +62,27 @@ def test_pcg_mixed_masked_block(gctx, orc):
     s.precond_build()
     Xo, _ = s.pcg(B, 1e-10, rule=1)
     assert rel(X, Xo) < 1e-7
+
+
+def test_mixed_precision_covers_every_grm_product(gctx, orc):
+    """With precision MIXED every GRM product of the call (PCG, u-hat, the probes' u-hat)
+    runs on the tensor cores: the context's own precision stays FP64 and is restored,
+    and the AIREML loop on genotypes matches the FP64 loop (same probes)."""
+    coh = cohort(21, 400, 700, recs=("uniform", 1, 4), miss=0.02)
+    indiv, N = coh["indiv"].astype(np.int32), coh["N"]
+    s = _load(gctx, orc, indiv, coh["X"], coh["y"], N, coh["packed"])
+    gctx.set_precision(G.PREC_FP64)
+    gctx.prof_enable(True)
+    grm0, tc0 = gctx.prof_query(G._lib.PROF_GRM)[0], gctx.prof_query(G._lib.PROF_GRM_PASS1)[0]
+    gctx.mme(tol=1e-10, rule=G.RULE_AIREML, precision=G.PREC_MIXED)
+    gctx.aireml_grad(5, seed=3, tol=1e-10, rule=G.RULE_AIREML, precision=G.PREC_MIXED)
+    grm1, tc1 = gctx.prof_query(G._lib.PROF_GRM)[0], gctx.prof_query(G._lib.PROF_GRM_PASS1)[0]
+    gctx.prof_enable(False)
+    assert grm1 > grm0 and tc1 - tc0 == grm1 - grm0        # every GRM product ran one tensor-core pass 1
+    res = {}
+    for prec in (G.PREC_FP64, G.PREC_MIXED):
+        gctx.set_vc(VC_F)
+        res[prec] = gctx.aireml_run(theta0=(0.5, 0.3, 0.2, 0.1, 0.1), maxiter=8, tol=1e-3, numMC=5,
+                                    pcg_tol=1e-10, precision=prec, seed=7)
+    assert res[G.PREC_MIXED]["iterations"] == res[G.PREC_FP64]["iterations"]
+    assert rel(res[G.PREC_MIXED]["theta"], res[G.PREC_FP64]["theta"]) < 1e-6
