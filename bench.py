@@ -53,6 +53,9 @@ CONFIGS = {
                 label="N=100k indiv, M=50k 2-bit SNPs (1.25 GB), ~700k records, k=5 (profiling size)"),
     "small": dict(N=20_000, M=40_000, recs=("poisson", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
                   label="N=20k indiv, M=40k SNPs, ~140k records, k=5"),
+    # dense .grm.bin path: the GRM is built on the GPU from 50k synthetic SNPs (float32 packed lower triangle)
+    "c2": dict(N=20_000, M=50_000, recs=("poisson", 5), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.0, dense=True, k=16,
+               label="N=20k indiv, ~120k records, dense float32 GRM (800 MB) from M=50k SNPs, k=16 RHS"),
     "c1": dict(N=2_000, M=10_000, recs=("uniform", 3, 10), T=5.0, maf_lo=0.05, maf_hi=0.5, miss=0.01,
                label="N=2000 indiv, M=10k SNPs, ~13k records, k=5"),
 }
@@ -151,6 +154,31 @@ def genetic_values(torch, raw, M, N, s2g, seed, chunk=2048):
         u += ((g - 2.0 * f[:, None]) * ww[:, None]).sum(0).double()
         kept += int(keep.sum())
     return (u * np.sqrt(s2g / max(kept, 1))).cpu().numpy()
+
+
+def dense_grm(torch, raw, M, N, chunk=2048):
+    """A = Zs'Zs / M_kept (float32 packed lower triangle, row-major with the diagonal: the
+    .grm.bin payload) from packed genotypes on the GPU, standardised as genetic_values does."""
+    bps = (N + 3) // 4
+    lut = torch.tensor([2.0, 0.0, 1.0, 0.0], device="cuda")
+    A = torch.zeros((N, N), dtype=torch.float32, device="cuda")
+    kept = 0
+    for s0 in range(0, M, chunk):
+        b = raw[s0:s0 + chunk, :bps]
+        codes = torch.stack([(b >> (2 * j)) & 3 for j in range(4)], dim=2).reshape(b.shape[0], bps * 4)[:, :N].long()
+        g = lut[codes]
+        nobs = (codes != 1).sum(1).clamp(min=1).float()
+        f = g.sum(1) / (2.0 * nobs)
+        keep = (f >= 0.01) & (f <= 0.99) & ((1.0 - nobs / N) <= 0.2)
+        z = ((g - 2.0 * f[:, None]) / torch.sqrt(2.0 * f * (1.0 - f)).clamp(min=1e-6)[:, None])[keep]
+        A.addmm_(z.t(), z)
+        kept += int(keep.sum())
+    A /= max(kept, 1)
+    r, c = torch.tril_indices(N, N, device="cuda")
+    lt = A[r, c].cpu().numpy()
+    del A, r, c
+    torch.cuda.empty_cache()
+    return lt, kept
 
 
 def cpu_reference_vx(indiv, X, packed_rows, maf_rows, N, k, rng):
@@ -271,16 +299,25 @@ def run_ours(args, cfg):
     ctx.synth_bed_dev(raw.data_ptr(), M, N, stride, SEED + 7919 * rank, cfg["maf_lo"], cfg["maf_hi"], cfg["miss"])
     y = y + genetic_values(torch, raw, M, N, VC[1], SEED + 1)[indiv]     # genotype-linked genetic term
     ctx.load_records(indiv, X, y, N)
-    Mk = ctx.load_bed_dev(raw.data_ptr(), M, stride)
-    # a host copy of some kept-looking rows for the CPU baseline (rank 0)
-    sample_rows = raw[: min(M, 4096)].cpu().numpy()[:, :bps].copy() if rank == 0 else None
+    dense = bool(cfg.get("dense"))
+    if dense:
+        grm_lt, Mk = dense_grm(torch, raw, M, N)
+        ctx.load_grm(grm_lt, N)
+        del grm_lt
+        sample_rows = None
+    else:
+        Mk = ctx.load_bed_dev(raw.data_ptr(), M, stride)
+        # a host copy of some kept-looking rows for the CPU baseline (rank 0)
+        sample_rows = raw[: min(M, 4096)].cpu().numpy()[:, :bps].copy() if rank == 0 else None
     del raw
     torch.cuda.empty_cache()
     ctx.set_vc(G.as_float_vc(VC))
-    k = 5
+    k = int(cfg.get("k", 5))
     B = torch.empty((k, Nrec), dtype=torch.float64, device="cuda")      # column-major Nrec x k
-    B[: k - 1] = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
-    B[k - 1] = torch.from_numpy(y).cuda()
+    B[:4] = torch.from_numpy(np.ascontiguousarray(X.T)).cuda()
+    B[4] = torch.from_numpy(y).cuda()
+    if k > 5:                                                            # extra right-hand sides: probe-like columns
+        B[5:] = torch.from_numpy(np.random.default_rng(SEED + 5).standard_normal((k - 5, Nrec))).cuda()
     Xs = torch.zeros_like(B)
     stream = torch.cuda.ExternalStream(ctx.stream)
     opts = dict(tol=0.0, maxit=args.iters, rule=G.RULE_AIREML, x0mode=G.X0_ZERO, precision=prec)
@@ -344,7 +381,7 @@ def run_ours(args, cfg):
 
     # FP64-plain comparison on the same data (one iteration per step)
     fp64 = None
-    if prec != G.PREC_FP64 and not args.no_fp64:
+    if prec != G.PREC_FP64 and not args.no_fp64 and not dense:
         o64 = dict(opts, precision=G.PREC_FP64, maxit=1)
         ctx.pcg_dev(B.data_ptr(), Xs.data_ptr(), k, **o64)
         barrier()
@@ -366,19 +403,26 @@ def run_ours(args, cfg):
         t0 = time.perf_counter()
         r = ctx.aireml_run(theta0=AIREML_THETA0, maxiter=50, tol=1e-3, numMC=15, precision=prec, seed=SEED)
         t_air = time.perf_counter() - t0
-        aireml = {"workload": args.config + " (same genotypes and records)", "precision": args.precision,
+        aireml = {"workload": args.config + " (same genetic source and records)",
+                  "precision": "fp64 (dense GRM)" if dense else args.precision,
                   "seconds_to_converge": t_air, "converged": bool(r["converged"]), "iterations": r["iterations"],
                   "grad_evals": r["grad_evals"], "pcg_rhs_iters": r["pcg_rhs_iters"],
                   "theta": [float(v) for v in r["theta"]], "numMC": 15, "tol": 1e-3}
 
-    # roofline of the dominant GRM kernel (one genotype pass per launch)
+    # roofline of the dominant GRM kernel (one genotype pass per launch; the dense product per launch)
     hbm, bf16, peak_src = load_peaks()
     n1, ms1 = prof[G._lib.PROF_GRM_PASS1]
     n2, ms2 = prof[G._lib.PROF_GRM_PASS2]
-    tcname = "k_tc_gemm" if prec == G.PREC_MIXED else "k_geno"
-    dom = (tcname + "(pass 2: Zs'w)", n2, ms2) if ms2 >= ms1 else (tcname + "(pass 1: Zs v)", n1, ms1)
-    # algorithmic bytes of one pass: the packed genotypes once + the k right-hand sides in and out (FP32-equivalent)
-    bytes_per_launch = Mk * bps + (N + Mk) * k * 4
+    if dense:
+        ng, msg = prof[G._lib.PROF_GRM]
+        dom = ("k_dense_f64 (sig2g A Z, packed lower triangle)", ng, msg)
+        # the packed float32 triangle once + the k right-hand sides in and out (FP64)
+        bytes_per_launch = N * (N + 1) // 2 * 4 + 2 * N * k * 8
+    else:
+        tcname = "k_tc_gemm" if prec == G.PREC_MIXED else "k_geno"
+        dom = (tcname + "(pass 2: Zs'w)", n2, ms2) if ms2 >= ms1 else (tcname + "(pass 1: Zs v)", n1, ms1)
+        # algorithmic bytes of one pass: the packed genotypes once + the k right-hand sides in and out (FP32-equivalent)
+        bytes_per_launch = Mk * bps + (N + Mk) * k * 4
     avg_s = dom[2] / 1000.0 / max(dom[1], 1)
     achieved = bytes_per_launch / avg_s / 1e9
     traffic = None
@@ -392,22 +436,27 @@ def run_ours(args, cfg):
             "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_s * 1000.0, "launches": dom[1],
             "grm_product_share_of_iteration": (msgrm / msiter) if msiter else None,
             "pass_ms": {"pass1": ms1 / max(n1, 1), "pass2": ms2 / max(n2, 1)}}
+    if dense:
+        roof["fp64_tflops_achieved"] = 2.0 * N * N * k / avg_s / 1e12   # symmetric product: N^2 k FMAs
     line = {"metric": METRIC, "value": value, "unit": "RHS*iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == G.PREC_FP64 else "e4m3 x e4m3 -> f32 (exact digits), f64 PCG",
-            "data": "synthetic (GPU counter-based genotypes, seeded numpy records)",
+            "vs_baseline": None,
+            "dtype": "f64" if (prec == G.PREC_FP64 or dense) else "e4m3 x e4m3 -> f32 (exact digits), f64 PCG",
+            "data": "synthetic (GPU counter-based genotypes%s, seeded numpy records)" % (
+                ", GRM built from them" if dense else ""),
             "config": {"workload": args.config, "shape": cfg["label"], "precision": args.precision,
                        "iters_per_step": args.iters, "kept_snps": Mk, "records": Nrec,
-                       "l2": "inputs larger than L2 (packed genotypes %.1f GB)" % (Mk * stride / 1e9),
+                       "l2": ("inputs larger than L2 (%s %.1f GB)" % (
+                           ("dense GRM", N * (N + 1) / 2 * 4 / 1e9) if dense else ("packed genotypes", Mk * stride / 1e9))),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches)}
     if fp64 is not None:
         line["fp64_plain"] = fp64
     if aireml is not None:
         line["aireml"] = aireml
-    if rank == 0 and world == 1 and not args.no_aireml and prec != G.PREC_FP64:
+    if rank == 0 and world == 1 and not args.no_aireml and prec != G.PREC_FP64 and not dense:
         line["aireml_mixed_vs_fp64"] = aireml_compare(G)
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and not dense:
         from oracle import oracle
         alt, miss, maf, _, keep = oracle.bed_stats(sample_rows, N)
         v, desc, threads = cpu_baseline(indiv, X, N, Mk, k, sample_rows[keep], maf[keep])

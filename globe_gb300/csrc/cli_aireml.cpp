@@ -7,6 +7,10 @@
 // Extra flags: --precision fp64|mixed, --pcgTol <v> (default 1e-5),
 // --device <id>, --seed <n> (GPU probe stream), --probes <file> (float64
 // standard normal draws consumed in the reference's sample_Yvs order).
+// --geno <plink_prefix> [--minMAF v] [--maxMissingRate v] takes the genetic
+// relationships from PLINK genotypes, as runPCGsolver --geno does
+// (PCGsolver.cpp:615-763), instead of <grm_prefix>; the reference's
+// runAIREML reads only a dense GRM.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -29,7 +33,8 @@ int main(int argc, char** argv) {
                      argv[0]);
         return EXIT_FAILURE;
     }
-    std::string input = argv[1], grm = argv[2], outp = argv[3], probes_file;
+    std::string input = argv[1], grm = argv[2], outp = argv[3], probes_file, geno;
+    float min_maf = 0.01f, max_miss = 0.2f;   // runPCGsolver's defaults (PCGsolver.cpp:34-35)
     int maxiter = 50, numMC = 15, precision = GLOBE_PREC_FP64, device = 0;
     float tol = 1e-3f;
     // defaults of VarCompDataStruct (varCompEst.cpp:48-52), as float
@@ -52,6 +57,9 @@ int main(int argc, char** argv) {
         else if (a == "--device" && has) device = std::atoi(argv[++i]);
         else if (a == "--seed" && has) seed = std::strtoull(argv[++i], nullptr, 10);
         else if (a == "--probes" && has) probes_file = argv[++i];
+        else if (a == "--geno" && has) geno = argv[++i];
+        else if (a == "--minMAF" && has) min_maf = std::strtof(argv[++i], nullptr);
+        else if (a == "--maxMissingRate" && has) max_miss = std::strtof(argv[++i], nullptr);
         else {
             for (int q = 0; q < 5; ++q)
                 if (a == vcflag[q] && has) th[q] = std::strtof(argv[++i], nullptr);
@@ -67,8 +75,17 @@ int main(int argc, char** argv) {
         return fail(err);
     std::printf("Found N = %d indivuduals, \n      p = %d fixed effects (in addition to TIME), and\n      Nrec = %lld "
                 "records in the input file.\n", N, p, (long long)Nrec);
-    std::vector<float> A((size_t)N * (N + 1) / 2);
-    if (globe_read_grm(grm.c_str(), N, A.data(), err, sizeof err)) return fail(err);
+    std::vector<float> A;
+    std::vector<uint8_t> bed;
+    int64_t M = 0;
+    if (geno.empty()) {
+        A.resize((size_t)N * (N + 1) / 2);
+        if (globe_read_grm(grm.c_str(), N, A.data(), err, sizeof err)) return fail(err);
+    } else {
+        if (globe_bed_dims(geno.c_str(), N, &M, err, sizeof err)) return fail(err);
+        bed.resize((size_t)M * ((N + 3) / 4));
+        if (globe_read_bed(geno.c_str(), N, M, bed.data(), err, sizeof err)) return fail(err);
+    }
     std::vector<double> probes;
     if (!probes_file.empty()) {
         FILE* f = std::fopen(probes_file.c_str(), "rb");
@@ -86,7 +103,16 @@ int main(int argc, char** argv) {
         return EXIT_FAILURE;
     };
     if (globe_load_records(ctx, Nrec, N, p, indiv.data(), X.data(), y.data())) return die("records");
-    if (globe_load_grm(ctx, A.data(), N)) return die("GRM");
+    if (geno.empty()) {
+        if (globe_load_grm(ctx, A.data(), N)) return die("GRM");
+    } else {
+        globe_bed_info info{};
+        if (globe_load_bed(ctx, bed.data(), M, min_maf, max_miss, nullptr, nullptr, nullptr, nullptr, nullptr, &info))
+            return die("genotypes");
+        std::printf("%lld of %lld SNPs pass the MAF / missingness filter.\n", (long long)info.kept, (long long)M);
+        bed.clear();
+        bed.shrink_to_fit();
+    }
     std::printf("Input files read and processed successfully.\nRunning AI-REML...\n");
     globe_aireml_opts o{};
     o.maxiter = maxiter;

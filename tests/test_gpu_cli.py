@@ -68,3 +68,26 @@ def test_runaireml_with_injected_probes(tmp_path):
     line = [l for l in log.splitlines() if l.startswith("Estimated variance components")][-1]
     th = [float(x.split("=")[1]) for x in line.split(":", 1)[1].split(",")]
     assert rel(th, ref["iterations"][-1]["theta"]) < 1e-5
+
+
+def _final_theta(log_path):
+    log = open(log_path).read()
+    line = [l for l in log.splitlines() if l.startswith("Estimated variance components")][-1]
+    return [float(x.split("=")[1]) for x in line.split(":", 1)[1].split(",")]
+
+
+def test_runaireml_geno_matches_grm_input(tmp_path):
+    """runAIREML --geno (genetic relationships from the PLINK genotypes, on the fly)
+    against runAIREML on the .grm.bin built from the same genotypes; FP64 and mixed."""
+    c = golden_case("geno_small")
+    common = ["--numMC", "5", "--maxiter", "6", "--seed", "5", "--pcgTol", "1e-10"]
+    th = {}
+    for name, extra in (("dense", []), ("geno", ["--geno", c["prefix"]]),
+                        ("geno_mixed", ["--geno", c["prefix"], "--precision", "mixed"])):
+        out = os.path.join(str(tmp_path), name)
+        grm_arg = c["prefix"] if name == "dense" else "-"
+        r = _run([os.path.join(BIN, "runAIREML"), c["prefix"] + ".txt", grm_arg, out] + common + extra)
+        assert r.returncode == 0, r.stderr
+        th[name] = _final_theta(out + ".log")
+    assert rel(th["geno"], th["dense"]) < 1e-4          # float32 rounding of the .grm.bin
+    assert rel(th["geno_mixed"], th["geno"]) < 1e-6
