@@ -381,7 +381,7 @@ def run_ours(args, cfg):
 
     # FP64-plain comparison on the same data (one iteration per step)
     fp64 = None
-    if prec != G.PREC_FP64 and not args.no_fp64 and not dense:
+    if prec != G.PREC_FP64 and not args.no_fp64:
         o64 = dict(opts, precision=G.PREC_FP64, maxit=1)
         ctx.pcg_dev(B.data_ptr(), Xs.data_ptr(), k, **o64)
         barrier()
@@ -404,7 +404,7 @@ def run_ours(args, cfg):
         r = ctx.aireml_run(theta0=AIREML_THETA0, maxiter=50, tol=1e-3, numMC=15, precision=prec, seed=SEED)
         t_air = time.perf_counter() - t0
         aireml = {"workload": args.config + " (same genetic source and records)",
-                  "precision": "fp64 (dense GRM)" if dense else args.precision,
+                  "precision": args.precision,
                   "seconds_to_converge": t_air, "converged": bool(r["converged"]), "iterations": r["iterations"],
                   "grad_evals": r["grad_evals"], "pcg_rhs_iters": r["pcg_rhs_iters"],
                   "theta": [float(v) for v in r["theta"]], "numMC": 15, "tol": 1e-3}
@@ -415,7 +415,8 @@ def run_ours(args, cfg):
     n2, ms2 = prof[G._lib.PROF_GRM_PASS2]
     if dense:
         ng, msg = prof[G._lib.PROF_GRM]
-        dom = ("k_dense_f64 (sig2g A Z, packed lower triangle)", ng, msg)
+        dom = ("%s (sig2g A Z, packed lower triangle)" % ("k_dense_df" if prec == G.PREC_MIXED else "k_dense_f64"),
+               ng, msg)
         # the packed float32 triangle once + the k right-hand sides in and out (FP64)
         bytes_per_launch = N * (N + 1) // 2 * 4 + 2 * N * k * 8
     else:
@@ -437,11 +438,13 @@ def run_ours(args, cfg):
             "grm_product_share_of_iteration": (msgrm / msiter) if msiter else None,
             "pass_ms": {"pass1": ms1 / max(n1, 1), "pass2": ms2 / max(n2, 1)}}
     if dense:
-        roof["fp64_tflops_achieved"] = 2.0 * N * N * k / avg_s / 1e12   # symmetric product: N^2 k FMAs
+        roof["fma_tflops_achieved"] = 2.0 * N * N * k / avg_s / 1e12    # N^2 k multiply-adds per product
     line = {"metric": METRIC, "value": value, "unit": "RHS*iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64" if (prec == G.PREC_FP64 or dense) else "e4m3 x e4m3 -> f32 (exact digits), f64 PCG",
+            "dtype": ("f64" if prec == G.PREC_FP64 else
+                      "f32 double-float (~48-bit) dense product, f64 PCG" if dense else
+                      "e4m3 x e4m3 -> f32 (exact digits), f64 PCG"),
             "data": "synthetic (GPU counter-based genotypes%s, seeded numpy records)" % (
                 ", GRM built from them" if dense else ""),
             "config": {"workload": args.config, "shape": cfg["label"], "precision": args.precision,

@@ -221,6 +221,7 @@ int geno_diag(globe_ctx* ctx, double* d);
 
 // k_grm_dense.cu
 int dense_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
+int dense_apply_df(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 int dense_diag(globe_ctx* ctx, double* d);
 
 // k_tc_geno.cu

@@ -86,3 +86,25 @@ def test_mixed_precision_covers_every_grm_product(gctx, orc):
                                     pcg_tol=1e-10, precision=prec, seed=7)
     assert res[G.PREC_MIXED]["iterations"] == res[G.PREC_FP64]["iterations"]
     assert rel(res[G.PREC_MIXED]["theta"], res[G.PREC_FP64]["theta"]) < 1e-6
+
+
+@pytest.mark.parametrize("N", [203, 2000])
+def test_dense_mixed_matches_fp64(gctx, orc, N):
+    """Dense GRM under GLOBE_PREC_MIXED (double-float FP32 arithmetic) vs the FP64 oracle,
+    per column; N=2000 exercises the split J range, k=20 two column chunks."""
+    coh = cohort(31 + N, N, 600, recs=("uniform", 1, 3), miss=0.02)
+    grm = synth.grm_from_packed(coh["packed"], N)
+    indiv = coh["indiv"].astype(np.int32)
+    gctx.load_records(indiv, coh["X"], coh["y"], N)
+    gctx.load_grm(grm, N)
+    gctx.set_vc(VC_F)
+    s = orc.Solver(indiv, coh["X"], coh["y"], N, VC_F, grm_lt=grm)
+    rng = np.random.default_rng(N)
+    try:
+        gctx.set_precision(G.PREC_MIXED)
+        for k in (1, 5, 16, 20):
+            Z = rng.standard_normal((N, k)) * np.logspace(-3, 3, k)
+            got, ref = gctx.grm_apply(Z), s.grm_apply(Z)
+            assert max(rel(got[:, c], ref[:, c]) for c in range(k)) < 1e-11, k
+    finally:
+        gctx.set_precision(G.PREC_FP64)
