@@ -238,6 +238,17 @@ def aireml_compare(G):
             "theta_fp64": [float(v) for v in rf["theta"]]}
 
 
+def aggregate_replicas(torch, t_ms, units, device):
+    """Whole-job figures of independent replicas: the slowest rank's time and the
+    units of all ranks (an initialised process group; any backend)."""
+    import torch.distributed as dist
+    tt = torch.tensor([float(t_ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    uu = torch.tensor([float(units)], device=device, dtype=torch.float64)
+    dist.all_reduce(uu, op=dist.ReduceOp.SUM)
+    return float(tt.item()), float(uu.item())
+
+
 def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -354,12 +365,7 @@ def run_ours(args, cfg):
     t_max = t_ms
     total_units = rhs_iters
     if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        uu = torch.tensor([rhs_iters], device="cuda", dtype=torch.float64)
-        dist.all_reduce(uu, op=dist.ReduceOp.SUM)
-        t_max, total_units = float(tt.item()), float(uu.item())
+        t_max, total_units = aggregate_replicas(torch, t_ms, rhs_iters, "cuda")
     value = total_units / (t_max / 1000.0)
 
     # e2e through the public API with pinned host buffers
