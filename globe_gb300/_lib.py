@@ -36,7 +36,8 @@ class BedInfo(C.Structure):
 class AiremlOpts(C.Structure):
     _fields_ = [("maxiter", C.c_int), ("tol", C.c_double), ("numMC", C.c_int), ("theta0", C.c_double * 5),
                 ("pcg_tol", C.c_double), ("pcg_maxit", C.c_int), ("precision", C.c_int), ("mask", C.c_int),
-                ("seed", C.c_uint64), ("probes", C.POINTER(C.c_double)), ("probes_len", C.c_int64)]
+                ("seed", C.c_uint64), ("probes", C.POINTER(C.c_double)), ("probes_len", C.c_int64),
+                ("fuse", C.c_int)]
 
 
 class AiremlResult(C.Structure):
@@ -79,6 +80,8 @@ SIGNATURES = {
     "globe_pcg_dev": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(PcgOpts), C.POINTER(PcgInfo)]),
     "globe_mme": (C.c_int, [_vp, C.POINTER(PcgOpts), _dp, _dp, _dp, _dp, C.POINTER(PcgInfo)]),
     "globe_aireml_grad": (C.c_int, [_vp, _dp, C.c_int, C.c_uint64, C.POINTER(PcgOpts), _dp, _dp, _dp, _dp,
+                                    C.POINTER(PcgInfo)]),
+    "globe_aireml_eval": (C.c_int, [_vp, _dp, C.c_int, C.c_uint64, C.POINTER(PcgOpts), _dp, _dp, _dp,
                                     C.POINTER(PcgInfo)]),
     "globe_aireml_ai": (C.c_int, [_vp, C.POINTER(PcgOpts), _dp, C.POINTER(PcgInfo)]),
     "globe_trust_region_step": (C.c_int, [_dp, _dp, _dp, C.c_double, _dp, C.POINTER(C.c_int)]),

@@ -215,6 +215,19 @@ class Context:
                                            _p(first), _p(trace), _p(grad), C.byref(info)))
         return dict(f_theta=fth, first=first, trace=trace, grad=grad, **self.info_dict(info))
 
+    def aireml_eval(self, numMC, probes=None, seed=0, **kw):
+        """MME + score with one block solve of [X y | probes] (globe_aireml_eval)."""
+        kw.setdefault("rule", L.RULE_AIREML)
+        o = self.opts(**kw)
+        info = PcgInfo()
+        pr = None if probes is None else np.ascontiguousarray(probes, dtype=np.float64)
+        if pr is not None:
+            assert pr.size == numMC * (3 * self.N + self.Nrec)
+        first, trace, grad = np.zeros(5), np.zeros(5), np.zeros(5)
+        self._ck(self._L.globe_aireml_eval(self.h, _p(pr), numMC, C.c_uint64(seed), C.byref(o), _p(first),
+                                           _p(trace), _p(grad), C.byref(info)))
+        return dict(first=first, trace=trace, grad=grad, **self.info_dict(info))
+
     def aireml_ai(self, **kw):
         kw.setdefault("rule", L.RULE_AIREML)
         o = self.opts(**kw)
@@ -224,12 +237,14 @@ class Context:
         return np.array(ai)
 
     def aireml_run(self, theta0=(0.5, 0.3, 0.2, 0.1, 0.1), maxiter=50, tol=1e-3, numMC=15, pcg_tol=1e-5,
-                   pcg_maxit=1000, precision=L.PREC_FP64, mask=False, seed=12345, probes=None, log_path=None):
+                   pcg_maxit=1000, precision=L.PREC_FP64, mask=False, seed=12345, probes=None, log_path=None,
+                   fuse=True):
         o = L.AiremlOpts()
         o.maxiter, o.tol, o.numMC = maxiter, tol, numMC
         for k in range(5):
             o.theta0[k] = theta0[k]
         o.pcg_tol, o.pcg_maxit, o.precision, o.mask, o.seed = pcg_tol, pcg_maxit, precision, int(mask), seed
+        o.fuse = int(bool(fuse))
         pr = None
         if probes is not None:
             pr = np.ascontiguousarray(probes, dtype=np.float64)

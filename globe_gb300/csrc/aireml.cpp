@@ -316,13 +316,6 @@ struct Driver {
         globe_pcg_opts m = pcg;
         m.rule = GLOBE_RULE_AIREML;
         m.x0mode = GLOBE_X0_PRECOND;  // fitMME: use_initial_guess (varCompEst.cpp:642)
-        log.printf("Solving MME... ");
-        rc = globe_mme(ctx, &m, nullptr, nullptr, nullptr, nullptr, &info);
-        if (rc) return rc;
-        rhs_iters += info.rhs_iters;
-        log.printf("Converged at iteration %d\nMME solved successfully.\nComputing derivatives.\n", info.iters);
-        const int32_t N = 0;
-        (void)N;
         const double* pr = nullptr;
         if (o->probes) {
             int64_t per = probes_per_eval();
@@ -334,11 +327,24 @@ struct Driver {
             probe_pos += per;
         }
         double first[5], trace[5];
-        rc = globe_aireml_grad(ctx, pr, o->numMC, o->seed + 0x1000003ull * (uint64_t)evals, &m, nullptr, first, trace,
-                               grad, &info);
-        if (rc) return rc;
+        const uint64_t seed = o->seed + 0x1000003ull * (uint64_t)evals;
+        log.printf("Solving MME... ");
+        if (o->fuse) {
+            // one block solve of [X y | probes]
+            rc = globe_aireml_eval(ctx, pr, o->numMC, seed, &m, first, trace, grad, &info);
+            if (rc) return rc;
+            rhs_iters += info.rhs_iters;
+            log.printf("Converged at iteration %d\nMME solved successfully.\nComputing derivatives.\n", info.iters);
+        } else {
+            rc = globe_mme(ctx, &m, nullptr, nullptr, nullptr, nullptr, &info);
+            if (rc) return rc;
+            rhs_iters += info.rhs_iters;
+            log.printf("Converged at iteration %d\nMME solved successfully.\nComputing derivatives.\n", info.iters);
+            rc = globe_aireml_grad(ctx, pr, o->numMC, seed, &m, nullptr, first, trace, grad, &info);
+            if (rc) return rc;
+            rhs_iters += info.rhs_iters;
+        }
         ++evals;
-        rhs_iters += info.rhs_iters;
         log.printf("Estimating trace terms... Converged at iteration %d\n", info.iters);
         log.vec("Gradient:", grad, 5);
         return GLOBE_OK;

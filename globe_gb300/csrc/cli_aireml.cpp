@@ -11,6 +11,9 @@
 // relationships from PLINK genotypes, as runPCGsolver --geno does
 // (PCGsolver.cpp:615-763), instead of <grm_prefix>; the reference's
 // runAIREML reads only a dense GRM.
+// Each gradient evaluation solves the MME right-hand sides and the probes as
+// one block PCG (globe_aireml_eval); --separateSolves solves them one after
+// the other, as the reference does.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -35,6 +38,7 @@ int main(int argc, char** argv) {
     }
     std::string input = argv[1], grm = argv[2], outp = argv[3], probes_file, geno;
     float min_maf = 0.01f, max_miss = 0.2f;   // runPCGsolver's defaults (PCGsolver.cpp:34-35)
+    int fuse = 1;
     int maxiter = 50, numMC = 15, precision = GLOBE_PREC_FP64, device = 0;
     float tol = 1e-3f;
     // defaults of VarCompDataStruct (varCompEst.cpp:48-52), as float
@@ -58,6 +62,7 @@ int main(int argc, char** argv) {
         else if (a == "--seed" && has) seed = std::strtoull(argv[++i], nullptr, 10);
         else if (a == "--probes" && has) probes_file = argv[++i];
         else if (a == "--geno" && has) geno = argv[++i];
+        else if (a == "--separateSolves") fuse = 0;
         else if (a == "--minMAF" && has) min_maf = std::strtof(argv[++i], nullptr);
         else if (a == "--maxMissingRate" && has) max_miss = std::strtof(argv[++i], nullptr);
         else {
@@ -124,6 +129,7 @@ int main(int argc, char** argv) {
     o.precision = precision;
     o.mask = 0;
     o.seed = seed;
+    o.fuse = fuse;
     o.probes = probes.empty() ? nullptr : probes.data();
     o.probes_len = (int64_t)probes.size();
     globe_aireml_result r{};

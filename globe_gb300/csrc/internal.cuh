@@ -75,7 +75,7 @@ struct Slot {
 enum SlotId {
     WS_R, WS_Z, WS_P, WS_VP, WS_ZI, WS_GZ, WS_S1, WS_PART, WS_SCAL, WS_COLS, WS_W,
     WS_GPART, WS_B, WS_TMP1, WS_TMP2, WS_TMP3, WS_TMP4, WS_H, WS_HSTAR, WS_PROBE,
-    WS_UH, WS_SMALL, WS_IO1, WS_IO2,
+    WS_UH, WS_SMALL, WS_IO1, WS_IO2, WS_BHAT, WS_FB, WS_FX,
     WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_COUNT
 };
 

@@ -392,25 +392,36 @@ int globe_pcg(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg
     return GLOBE_OK;
 }
 
-static int mme_impl(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat,
-                    double* vinv_r, globe_pcg_info* info) {
-    if (!ctx || !opts) return GLOBE_ERR_ARG;
-    cudaSetDevice(ctx->device);
-    GLOBE_RET(check_ready(ctx));
+// ---- MME and AIREML score: right-hand sides, solves, and what follows them ----
+
+static int mme_prepare(globe_ctx* ctx) {
+    auto& c = ctx->coh;
+    const int64_t n = c.Nrec;
+    const int k = c.p + 2;
+    if (!ctx->vinv_X) GLOBE_RET(dalloc(ctx, &ctx->vinv_X, (size_t)n * k));
+    if (!ctx->vinv_r) GLOBE_RET(dalloc(ctx, &ctx->vinv_r, (size_t)n));
+    if (!ctx->uhat) GLOBE_RET(dalloc(ctx, &ctx->uhat, (size_t)c.N));
+    ctx->mme_ok = ctx->fth_ok = false;
+    return GLOBE_OK;
+}
+
+// B (Nrec x (p+2)) = [X y]
+static int mme_rhs(globe_ctx* ctx, double* B) {
+    auto& c = ctx->coh;
+    const int64_t n = c.Nrec;
+    const int p1 = c.p + 1;
+    GLOBE_CK(ctx, cudaMemcpyAsync(B, c.X, sizeof(double) * n * p1, cudaMemcpyDeviceToDevice, ctx->stream));
+    GLOBE_CK(ctx, cudaMemcpyAsync(B + (size_t)n * p1, c.y, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    return GLOBE_OK;
+}
+
+// From ctx->vinv_X = V^-1 [X y]: beta, V^-1 r, u-hat, b-hat (fitMME, varCompEst.cpp:587-685)
+static int mme_finish(globe_ctx* ctx, double* beta, double* uhat, double* bhat, double* vinv_r) {
     auto& c = ctx->coh;
     const int64_t n = c.Nrec;
     const int32_t N = c.N;
     const int p1 = c.p + 1, k = c.p + 2;
-    if (!ctx->vinv_X) GLOBE_RET(dalloc(ctx, &ctx->vinv_X, (size_t)n * k));
-    if (!ctx->vinv_r) GLOBE_RET(dalloc(ctx, &ctx->vinv_r, (size_t)n));
-    if (!ctx->uhat) GLOBE_RET(dalloc(ctx, &ctx->uhat, (size_t)N));
-    ctx->mme_ok = ctx->fth_ok = false;
-    double* B;
-    GLOBE_RET(ws(ctx, WS_B, (size_t)n * k, &B));
-    GLOBE_CK(ctx, cudaMemcpyAsync(B, c.X, sizeof(double) * n * p1, cudaMemcpyDeviceToDevice, ctx->stream));
-    GLOBE_CK(ctx, cudaMemcpyAsync(B + (size_t)n * p1, c.y, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     double* S = ctx->vinv_X;  // [V^-1 X | V^-1 y]
-    GLOBE_RET(pcg_dev(ctx, B, S, k, opts, info));
     double* small;
     GLOBE_RET(ws(ctx, WS_SMALL, (size_t)p1 * (p1 + 2) + 64, &small));
     GLOBE_RET(xt_mat(ctx, c.X, p1, S, k, small));  // [X'V^-1X | X'V^-1y]
@@ -433,7 +444,7 @@ static int mme_impl(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, do
     GLOBE_RET(ws(ctx, WS_S1, (size_t)N, &S1));
     GLOBE_RET(seg_sums(ctx, ctx->vinv_r, nullptr, nullptr, nullptr, nullptr, 1, Zi, S1));
     GLOBE_RET(grm_apply_dev(ctx, Zi, 1, ctx->uhat));
-    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)2 * N, &dbhat));
+    GLOBE_RET(ws(ctx, WS_BHAT, (size_t)2 * N, &dbhat));
     GLOBE_RET(bhat_kernel(ctx, ctx->vinv_r, dbhat));
     if (beta) std::memcpy(beta, b.data(), sizeof(double) * p1);
     if (uhat) GLOBE_CK(ctx, cudaMemcpyAsync(uhat, ctx->uhat, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
@@ -444,14 +455,61 @@ static int mme_impl(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, do
     return GLOBE_OK;
 }
 
-static int aireml_grad_impl(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
-                            double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
-    if (!ctx || !opts || numMC < 1) return GLOBE_ERR_ARG;
+static int mme_impl(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat,
+                    double* vinv_r, globe_pcg_info* info) {
+    if (!ctx || !opts) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
-    if (!ctx->mme_ok) return set_err(ctx, GLOBE_ERR_STATE, "call globe_mme at the current components first");
+    GLOBE_RET(mme_prepare(ctx));
+    const int64_t n = ctx->coh.Nrec;
+    const int k = ctx->coh.p + 2;
+    double* B;
+    GLOBE_RET(ws(ctx, WS_B, (size_t)n * k, &B));
+    GLOBE_RET(mme_rhs(ctx, B));
+    GLOBE_RET(pcg_dev(ctx, B, ctx->vinv_X, k, opts, info));
+    return mme_finish(ctx, beta, uhat, bhat, vinv_r);
+}
+
+static int grad_check(globe_ctx* ctx, int numMC) {
+    if (numMC < 1) return set_err(ctx, GLOBE_ERR_ARG, "numMC must be >= 1");
     if (!(ctx->vc[1] > 0.0) || !(ctx->vc[2] > 0.0))
         return set_err(ctx, GLOBE_ERR_ARG, "AIREML needs sig2g > 0 and sig2b0 > 0");
+    return GLOBE_OK;
+}
+
+// Probes Y_v ~ N(0, V*) and TY = V*^-1 Y (the PCG start), sample_Yvs and
+// estimateTrace_PdV (varCompEst.cpp:775-862)
+struct ProbeBufs {
+    double *Y, *TY, *VR, *UH, *Hs;
+};
+
+static int grad_probes(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, ProbeBufs& pb) {
+    const int64_t n = ctx->coh.Nrec;
+    const int32_t N = ctx->coh.N;
+    GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * numMC, &pb.Y));
+    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * numMC, &pb.TY));
+    GLOBE_RET(ws(ctx, WS_TMP4, (size_t)n * numMC, &pb.VR));
+    GLOBE_RET(ws(ctx, WS_UH, (size_t)N * numMC, &pb.UH));
+    GLOBE_RET(ws(ctx, WS_HSTAR, (size_t)N * 4, &pb.Hs));
+    if (probes) {
+        double* dd;
+        size_t cnt = (size_t)numMC * (3 * (size_t)N + n);
+        GLOBE_RET(ws(ctx, WS_PROBE, cnt, &dd));
+        GLOBE_CK(ctx, cudaMemcpyAsync(dd, probes, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->stream));
+        GLOBE_RET(probes_build(ctx, dd, numMC, seed, false, pb.Y));
+    } else {
+        GLOBE_RET(probes_build(ctx, nullptr, numMC, seed, true, pb.Y));
+    }
+    // V*^-1 Y by the Woodbury block inverse with g = sig2g (varCompEst.cpp:839-862)
+    GLOBE_RET(build_H(ctx, nullptr, ctx->vc[1], pb.Hs));
+    GLOBE_RET(precond_apply(ctx, pb.Hs, pb.Y, pb.TY, nullptr, numMC, nullptr));
+    return GLOBE_OK;
+}
+
+// From the MME (V^-1 r, u-hat) and VY = V^-1 Y: f_theta, the first-order terms, the
+// Monte-Carlo trace and the score (computeDerivative_first, varCompEst.cpp:693-1012)
+static int grad_finish(globe_ctx* ctx, int numMC, const double* VY, const ProbeBufs& pb, double* f_theta,
+                       double* first, double* trace, double* grad) {
     auto& c = ctx->coh;
     const int64_t n = c.Nrec;
     const int32_t N = c.N;
@@ -463,38 +521,14 @@ static int aireml_grad_impl(globe_ctx* ctx, const double* probes, int numMC, uin
     GLOBE_RET(xt_mat(ctx, ctx->vinv_r, 1, fth, 5, small));
     double h_first[5];
     GLOBE_RET(d2h(ctx, h_first, small, 5));
-    // probes Y_v ~ N(0, V*)
-    double *Y, *TY, *VY, *VR, *UH, *Hs, *Zi, *S1;
-    GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * numMC, &Y));
-    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * numMC, &TY));
-    GLOBE_RET(ws(ctx, WS_TMP3, (size_t)n * numMC, &VY));
-    GLOBE_RET(ws(ctx, WS_TMP4, (size_t)n * numMC, &VR));
-    GLOBE_RET(ws(ctx, WS_UH, (size_t)N * numMC, &UH));
-    GLOBE_RET(ws(ctx, WS_HSTAR, (size_t)N * 4, &Hs));
-    if (probes) {
-        double* dd;
-        size_t cnt = (size_t)numMC * (3 * (size_t)N + n);
-        GLOBE_RET(ws(ctx, WS_PROBE, cnt, &dd));
-        GLOBE_CK(ctx, cudaMemcpyAsync(dd, probes, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->stream));
-        GLOBE_RET(probes_build(ctx, dd, numMC, seed, false, Y));
-    } else {
-        GLOBE_RET(probes_build(ctx, nullptr, numMC, seed, true, Y));
-    }
-    // V*^-1 Y by the Woodbury block inverse with g = sig2g (varCompEst.cpp:839-862)
-    GLOBE_RET(build_H(ctx, nullptr, ctx->vc[1], Hs));
-    GLOBE_RET(precond_apply(ctx, Hs, Y, TY, nullptr, numMC, nullptr));
-    GLOBE_CK(ctx, cudaMemcpyAsync(VY, TY, sizeof(double) * n * numMC, cudaMemcpyDeviceToDevice, ctx->stream));
-    globe_pcg_opts o = *opts;
-    o.rule = GLOBE_RULE_AIREML;
-    o.x0mode = GLOBE_X0_GIVEN;
-    GLOBE_RET(pcg_dev(ctx, Y, VY, numMC, &o, info));
-    GLOBE_RET(project_dev(ctx, VY, numMC, VR));
+    GLOBE_RET(project_dev(ctx, VY, numMC, pb.VR));
+    double *Zi, *S1;
     GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * numMC, &Zi));
     GLOBE_RET(ws(ctx, WS_S1, (size_t)N * numMC, &S1));
-    GLOBE_RET(seg_sums(ctx, VR, nullptr, nullptr, nullptr, nullptr, numMC, Zi, S1));
-    GLOBE_RET(grm_apply_dev(ctx, Zi, numMC, UH));
+    GLOBE_RET(seg_sums(ctx, pb.VR, nullptr, nullptr, nullptr, nullptr, numMC, Zi, S1));
+    GLOBE_RET(grm_apply_dev(ctx, Zi, numMC, pb.UH));
     GLOBE_RET(ws(ctx, WS_SMALL, (size_t)numMC * 5 + 64, &small));
-    GLOBE_RET(trace_terms(ctx, VR, UH, TY, numMC, small));
+    GLOBE_RET(trace_terms(ctx, pb.VR, pb.UH, pb.TY, numMC, small));
     std::vector<double> tt((size_t)numMC * 5);
     GLOBE_RET(d2h(ctx, tt.data(), small, tt.size()));
     double h_trace[5], h_grad[5];
@@ -510,6 +544,59 @@ static int aireml_grad_impl(globe_ctx* ctx, const double* probes, int numMC, uin
     if (f_theta) GLOBE_RET(d2h(ctx, f_theta, fth, (size_t)n * 5));
     ctx->fth_ok = true;
     return GLOBE_OK;
+}
+
+static int aireml_grad_impl(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
+                            double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
+    if (!ctx || !opts || numMC < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    if (!ctx->mme_ok) return set_err(ctx, GLOBE_ERR_STATE, "call globe_mme at the current components first");
+    GLOBE_RET(grad_check(ctx, numMC));
+    ProbeBufs pb;
+    GLOBE_RET(grad_probes(ctx, probes, numMC, seed, pb));
+    const int64_t n = ctx->coh.Nrec;
+    double* VY;
+    GLOBE_RET(ws(ctx, WS_TMP3, (size_t)n * numMC, &VY));
+    GLOBE_CK(ctx, cudaMemcpyAsync(VY, pb.TY, sizeof(double) * n * numMC, cudaMemcpyDeviceToDevice, ctx->stream));
+    globe_pcg_opts o = *opts;
+    o.rule = GLOBE_RULE_AIREML;
+    o.x0mode = GLOBE_X0_GIVEN;
+    GLOBE_RET(pcg_dev(ctx, pb.Y, VY, numMC, &o, info));
+    return grad_finish(ctx, numMC, VY, pb, f_theta, first, trace, grad);
+}
+
+// MME and score with one block solve of [X y | probes]: the MME columns start from
+// Q^-1 b (fitMME's use_initial_guess), the probe columns from V*^-1 Y.
+static int aireml_eval_impl(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed,
+                            const globe_pcg_opts* opts, double* first, double* trace, double* grad,
+                            globe_pcg_info* info) {
+    if (!ctx || !opts || numMC < 1) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    GLOBE_RET(check_ready(ctx));
+    GLOBE_RET(grad_check(ctx, numMC));
+    GLOBE_RET(mme_prepare(ctx));
+    ProbeBufs pb;
+    GLOBE_RET(grad_probes(ctx, probes, numMC, seed, pb));
+    const int64_t n = ctx->coh.Nrec;
+    const int k = ctx->coh.p + 2, kt = k + numMC;
+    double *FB, *FX;
+    GLOBE_RET(ws(ctx, WS_FB, (size_t)n * kt, &FB));
+    GLOBE_RET(ws(ctx, WS_FX, (size_t)n * kt, &FX));
+    GLOBE_RET(mme_rhs(ctx, FB));
+    GLOBE_CK(ctx, cudaMemcpyAsync(FB + (size_t)n * k, pb.Y, sizeof(double) * n * numMC, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    GLOBE_RET(ensure_precond(ctx));
+    GLOBE_RET(precond_apply(ctx, Hptr(ctx), FB, FX, nullptr, k, nullptr));
+    GLOBE_CK(ctx, cudaMemcpyAsync(FX + (size_t)n * k, pb.TY, sizeof(double) * n * numMC, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    globe_pcg_opts o = *opts;
+    o.rule = GLOBE_RULE_AIREML;
+    o.x0mode = GLOBE_X0_GIVEN;
+    GLOBE_RET(pcg_dev(ctx, FB, FX, kt, &o, info));
+    GLOBE_CK(ctx, cudaMemcpyAsync(ctx->vinv_X, FX, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
+    GLOBE_RET(mme_finish(ctx, nullptr, nullptr, nullptr, nullptr));
+    return grad_finish(ctx, numMC, FX + (size_t)n * k, pb, nullptr, first, trace, grad);
 }
 
 // The GRM products outside the PCG solves (u-hat, the probes' u-hat) run at the
@@ -548,6 +635,19 @@ int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t 
     {
         PrecScope ps(ctx, opts->precision);
         rc = aireml_grad_impl(ctx, probes, numMC, seed, opts, f_theta, first, trace, grad, info);
+    }
+    if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
+    return rc;
+}
+
+int globe_aireml_eval(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
+                      double* first, double* trace, double* grad, globe_pcg_info* info) {
+    if (!ctx || !opts) return GLOBE_ERR_ARG;
+    GLOBE_RET(check_prec(ctx, opts));
+    int rc;
+    {
+        PrecScope ps(ctx, opts->precision);
+        rc = aireml_eval_impl(ctx, probes, numMC, seed, opts, first, trace, grad, info);
     }
     if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
     return rc;

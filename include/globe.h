@@ -43,8 +43,9 @@ extern "C" {
 /* precision of the GRM product inside the solver */
 #define GLOBE_PREC_FP64 0   /* plain FP64 everywhere (the drop-in path) */
 #define GLOBE_PREC_MIXED 1  /* genotype GRM product on the FP8 tensor cores with exact
-                               base-16 digit slicing of the right-hand sides (matches
-                               FP64 to ~1e-14); the dense GRM stays FP64 */
+                               base-32 digit slicing of the right-hand sides (45 bits,
+                               matches FP64 to ~1e-13); dense GRM in double-float FP32
+                               arithmetic (~48 bits) */
 
 /* PCG stopping rules */
 #define GLOBE_RULE_PCGSOLVER 0 /* max_j |r_j|/|b_j| < tol, or 10 iterations with
@@ -213,6 +214,16 @@ int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* 
 int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed,
                       const globe_pcg_opts* opts, double* f_theta, double* first,
                       double* trace, double* grad, globe_pcg_info* info);
+
+/* globe_mme followed by globe_aireml_grad's score, with the MME right-hand sides
+ * [X y] and the numMC probes solved as one block PCG of p+2+numMC columns (MME
+ * columns start from Q^-1 b, probe columns from V*^-1 Y).  The reference solves
+ * them one after the other (fitMME, varCompEst.cpp:587-685, then
+ * computeDerivative_first, :980-1012); the two solves are independent.  Leaves
+ * the same state as globe_mme + globe_aireml_grad, so globe_aireml_ai may
+ * follow. */
+int globe_aireml_eval(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
+                      double* first, double* trace, double* grad, globe_pcg_info* info);
 /* Average-information matrix AI = 1/2 f' P f (5 x 5) for the f_theta of the
  * last globe_aireml_grad (computeDerivative_AImat, varCompEst.cpp:1015-1041). */
 int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai,
@@ -240,6 +251,8 @@ typedef struct {
     uint64_t seed;     /* probe seed when probes == NULL */
     const double* probes;  /* optional injected draws, consumed in order */
     int64_t probes_len;
+    int fuse;          /* 1: one block solve of MME + probes per gradient evaluation
+                          (globe_aireml_eval); 0: two solves, as the reference */
 } globe_aireml_opts;
 
 typedef struct {

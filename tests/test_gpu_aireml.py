@@ -58,3 +58,32 @@ def test_loop_follows_reference_trajectory(gctx, case, tmp_path):
     assert rel(r["se"], [f[1] for f in ref["final"]]) < 1e-4
     text = open(log).read()
     assert "Final variance components" in text and text.count("Rho:") == sum(len(i["rho"]) for i in ref["iterations"])
+
+
+def test_fused_evaluation_matches_separate_solves(gctx, case):
+    """globe_aireml_eval (one block solve of [X y | probes]) against globe_mme followed
+    by globe_aireml_grad on the same probes; the AI matrix after either."""
+    ref = case["ref"]
+    probes, per = aireml_probes(case, 1)
+    tol = 1e-12
+    gctx.set_vc(ref["theta0"])
+    gctx.mme(tol=tol, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND)
+    g = gctx.aireml_grad(ref["numMC"], probes=probes, tol=tol)
+    ai = gctx.aireml_ai(tol=tol)
+    gctx.set_vc(ref["theta0"])
+    f = gctx.aireml_eval(ref["numMC"], probes=probes, tol=tol)
+    ai_f = gctx.aireml_ai(tol=tol)
+    for v in ("first", "trace", "grad"):
+        assert rel(f[v], g[v]) < 1e-9, v
+    assert rel(ai_f, ai) < 1e-9
+    assert rel(f["grad"], ref["iterations"][0]["gradients"][0]) < 1e-8
+
+
+def test_loop_fused_and_separate_agree(gctx, case):
+    ref = case["ref"]
+    probes, per = aireml_probes(case, 60)
+    kw = dict(theta0=ref["theta0"], maxiter=ref["maxiter"], numMC=ref["numMC"], pcg_tol=ref["pcg_tol"], probes=probes)
+    a = gctx.aireml_run(fuse=True, **kw)
+    b = gctx.aireml_run(fuse=False, **kw)
+    assert a["iterations"] == b["iterations"]
+    assert rel(a["theta"], b["theta"]) < 1e-6
