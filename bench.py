@@ -56,6 +56,12 @@ CONFIGS = {
     # dense .grm.bin path: the GRM is built on the GPU from 50k synthetic SNPs (float32 packed lower triangle)
     "c2": dict(N=20_000, M=50_000, recs=("poisson", 5), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.0, dense=True, k=16,
                label="N=20k indiv, ~120k records, dense float32 GRM (800 MB) from M=50k SNPs, k=16 RHS"),
+    # batching shape: y + 64 probe-like columns as one 65-RHS block
+    "c4": dict(N=200_000, M=300_000, recs=("fixed", 6), T=10.0, maf_lo=0.01, maf_hi=0.5, miss=0.02, k=65,
+               label="N=200k indiv, M=300k 2-bit SNPs (15 GB), 1.2M records, k=65 RHS"),
+    # biobank shape: 60 GB of packed genotypes, geometric record counts 1-200
+    "c5": dict(N=400_000, M=600_000, recs=("geometric", 0.1, 1, 200), T=15.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
+               label="N=400k indiv, M=600k 2-bit SNPs (60 GB), ~4M records (geometric 1-200), k=5 RHS"),
     "c1": dict(N=2_000, M=10_000, recs=("uniform", 3, 10), T=5.0, maf_lo=0.05, maf_hi=0.5, miss=0.01,
                label="N=2000 indiv, M=10k SNPs, ~13k records, k=5"),
 }

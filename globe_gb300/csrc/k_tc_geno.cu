@@ -900,8 +900,11 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
         return GLOBE_OK;
     }
     GLOBE_RET(ensure_gt(ctx));
-    // near-equal groups of <= MAX_RHS_GROUP columns (e.g. 65 -> 22 + 22 + 21)
-    const int ng = (k + MAX_RHS_GROUP - 1) / MAX_RHS_GROUP;
+    // near-equal groups of <= MAX_RHS_GROUP columns.  Groups wider than 21 (NMMA > 192)
+    // run one row tile per CTA, which costs more per column than two groups of two
+    // tiles once k > MAX_RHS_GROUP: then groups of <= 21 (e.g. 65 -> 17 + 16 + 16 + 16).
+    int ng = (k + MAX_RHS_GROUP - 1) / MAX_RHS_GROUP;
+    if (ng > 1) ng = (k + 20) / 21;
     for (int gi = 0, c0 = 0; gi < ng; ++gi) {
         const int kg = k / ng + (gi < k % ng ? 1 : 0);
         GLOBE_RET(tc_group(ctx, Z + (size_t)c0 * N, kg, scale, out + (size_t)c0 * N));
