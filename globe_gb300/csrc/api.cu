@@ -122,7 +122,7 @@ void prof_end(globe_ctx* ctx, int h) {
 static void free_cohort(globe_ctx* ctx) {
     auto& c = ctx->coh;
     for (void* p : {(void*)c.X, (void*)c.y, (void*)c.bstart, (void*)c.bind, (void*)c.rind, (void*)c.bn,
-                    (void*)c.bt, (void*)c.btt})
+                    (void*)c.bt, (void*)c.btt, (void*)c.lblk})
         dfree(ctx, p);
     c = Cohort();
     for (void* p : {(void*)ctx->vinv_X, (void*)ctx->vinv_r, (void*)ctx->uhat, (void*)ctx->f_theta}) dfree(ctx, p);
@@ -291,6 +291,16 @@ int globe_load_records(globe_ctx* ctx, int64_t Nrec, int32_t N, int32_t p, const
     GLOBE_RET(dalloc(ctx, &c.bn, (size_t)N));
     GLOBE_RET(dalloc(ctx, &c.bt, (size_t)N));
     GLOBE_RET(dalloc(ctx, &c.btt, (size_t)N));
+    // blocks longer than SHORT_BLOCK records: the record kernels give each of them a warp
+    std::vector<int32_t> lblk;
+    for (int32_t b = 0; b < N; ++b)
+        if (bstart[b + 1] - bstart[b] > SHORT_BLOCK) lblk.push_back(b);
+    c.nlong = (int32_t)lblk.size();
+    if (c.nlong > 0) {
+        GLOBE_RET(dalloc(ctx, &c.lblk, (size_t)c.nlong));
+        GLOBE_CK(ctx, cudaMemcpyAsync(c.lblk, lblk.data(), sizeof(int32_t) * c.nlong, cudaMemcpyHostToDevice,
+                                      ctx->stream));
+    }
     GLOBE_CK(ctx, cudaMemcpyAsync(c.X, X, sizeof(double) * Nrec * (p + 1), cudaMemcpyHostToDevice, ctx->stream));
     GLOBE_CK(ctx, cudaMemcpyAsync(c.y, y, sizeof(double) * Nrec, cudaMemcpyHostToDevice, ctx->stream));
     GLOBE_CK(ctx, cudaMemcpyAsync(c.bstart, bstart.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice,

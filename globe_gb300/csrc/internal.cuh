@@ -25,6 +25,8 @@ namespace globe {
 //             2-bit codes; per-SNP zs table zs[s*4 + code] (double) with
 //             zs = (g - 2f) * inv_std, missing -> g = 0
 //   dense:    packed lower triangle float32, N(N+1)/2
+constexpr int SHORT_BLOCK = 48;   // longest record block handled by one thread in the record kernels
+
 struct Cohort {
     int64_t Nrec = 0;
     int32_t N = 0, p = 0;
@@ -37,6 +39,8 @@ struct Cohort {
     double* bt = nullptr;
     double* btt = nullptr;
     int32_t max_block = 0;
+    int32_t* lblk = nullptr;   // blocks with more than SHORT_BLOCK records (device list)
+    int32_t nlong = 0;
     const double* times() const { return X + (size_t)p * Nrec; }
 };
 

@@ -3,9 +3,9 @@
 // Records of one individual form one contiguous block.  All record-level
 // work is per block, so segment sums, the 2x2 random intercept/slope term and
 // the block preconditioner fuse without atomics.  Two layouts of the same
-// kernels: when every block holds at most SHORT_BLOCK records one thread owns
-// a (block, column) pair (grid.y = column); longer blocks use one warp per
-// block and loop over the columns.
+// kernels run side by side: one thread owns a (block, column) pair for blocks of
+// at most SHORT_BLOCK records (grid.y = column); each longer block gets one warp
+// that loops over the columns.
 //
 //   V x   = J (sig2g A J' x) + U D U' x + sig2e x          (PCGsolver.cpp:1095-1266)
 //   U D U' x on block b = (D00 s0 + D01 s1) + t (D01 s0 + D11 s1),
@@ -24,9 +24,21 @@ namespace globe {
 constexpr int RB_THREADS = 256;  // 8 warps, one block of records per warp
 constexpr int RB_WARPS = RB_THREADS / 32;
 constexpr int TB_THREADS = 256;  // thread-per-block layout
-constexpr int SHORT_BLOCK = 48;  // longest block handled by one thread
 
-static bool short_blocks(const globe_ctx* ctx) { return ctx->coh.max_block <= SHORT_BLOCK; }
+// Launch shape of the record kernels: one thread per (block of <= SHORT_BLOCK records,
+// column) over all blocks -- nbt CTAs per column, longer blocks skipped -- and one
+// warp per longer block over the list coh.lblk (nbl CTAs).  Per-CTA partial sums of
+// both go to part[slot + q * S], thread-layout CTAs first.
+struct RecShape {
+    int nbt, nbl, S;
+};
+static RecShape rec_shape(const globe_ctx* ctx) {
+    RecShape r;
+    r.nbt = div_up(ctx->coh.N, TB_THREADS);
+    r.nbl = ctx->coh.nlong > 0 ? div_up(ctx->coh.nlong, RB_WARPS) : 0;
+    r.S = r.nbt + r.nbl;
+    return r;
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -39,22 +51,22 @@ struct VC {
 };
 __device__ __forceinline__ VC load_vc(const double* vc) { return VC{vc[0], vc[1], vc[2], vc[3], vc[4]}; }
 
-// CTA-level reduction of per-warp values: vals[warp][q] -> part[blockIdx.x + q*gridDim.x]
+// CTA-level reduction of per-warp values: vals[warp][q] -> part[slot + q*stride]
 // smem layout: sm[q * RB_WARPS + warp]
-__device__ __forceinline__ void cta_partials(double* sm, int nq, double* part) {
+__device__ __forceinline__ void cta_partials(double* sm, int nq, double* part, int slot, int stride) {
     __syncthreads();
     for (int q = threadIdx.x; q < nq; q += blockDim.x) {
         double a = 0.0;
 #pragma unroll
         for (int w = 0; w < RB_WARPS; ++w) a += sm[q * RB_WARPS + w];
-        part[blockIdx.x + (size_t)q * gridDim.x] = a;
+        part[slot + (size_t)q * stride] = a;
     }
 }
 
 // CTA sums of NQ values per thread (thread-per-block layout):
-// sum over the CTA of v[j] -> part[blockIdx.x + q[j] * gridDim.x]
+// sum over the CTA of v[j] -> part[blockIdx.x + q[j] * stride]
 template <int NQ>
-__device__ __forceinline__ void cta_sums(const double (&v)[NQ], const int (&q)[NQ], double* part) {
+__device__ __forceinline__ void cta_sums(const double (&v)[NQ], const int (&q)[NQ], double* part, int stride) {
     __shared__ double sm[NQ][TB_THREADS / 32];
 #pragma unroll
     for (int j = 0; j < NQ; ++j) {
@@ -68,7 +80,7 @@ __device__ __forceinline__ void cta_sums(const double (&v)[NQ], const int (&q)[N
             double a = 0.0;
 #pragma unroll
             for (int w = 0; w < TB_THREADS / 32; ++w) a += sm[j][w];
-            part[blockIdx.x + (size_t)q[j] * gridDim.x] = a;
+            part[blockIdx.x + (size_t)q[j] * stride] = a;
         }
     }
 }
@@ -140,10 +152,11 @@ __global__ void k_seg_sums(int32_t nblk, int64_t ld, int32_t N, const int32_t* _
                            const int32_t* __restrict__ bind, const double* __restrict__ t,
                            double* x, const double* __restrict__ z, const double* __restrict__ beta,
                            const int32_t* __restrict__ cols, int kact, double* __restrict__ Zi,
-                           double* __restrict__ S1) {
+                           double* __restrict__ S1, const int32_t* __restrict__ bl) {
     const int lane = threadIdx.x & 31;
-    const int b = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
-    if (b >= nblk) return;
+    const int idx = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (idx >= nblk) return;
+    const int b = bl ? bl[idx] : idx;
     const int st = bstart[b], en = bstart[b + 1];
     const int i = bind[b];
     for (int c = 0; c < kact; ++c) {
@@ -185,6 +198,7 @@ __global__ void k_seg_sums_t(int32_t nblk, int64_t ld, int32_t N, const int32_t*
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     const int st = bstart[b], en = bstart[b + 1];
+    if (en - st > SHORT_BLOCK) return;   // a warp per long block handles it
     double* xc = x + (size_t)col * ld;
     double s0 = 0, s1 = 0;
     if (beta) {
@@ -215,15 +229,15 @@ int seg_sums(globe_ctx* ctx, const double* x, const double* z, const double* bet
     auto& c = ctx->coh;
     // in-place p update: xout must alias x when beta is given
     double* xx = beta ? xout : const_cast<double*>(x);
-    if (short_blocks(ctx)) {
-        k_seg_sums_t<<<dim3(div_up(c.N, TB_THREADS), kact), TB_THREADS, 0, ctx->stream>>>(
-            c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), xx, z, beta, cols, Zi, S1);
-        GLOBE_LAUNCHED(ctx, "k_seg_sums_t");
-        return GLOBE_OK;
+    const RecShape rs = rec_shape(ctx);
+    k_seg_sums_t<<<dim3(rs.nbt, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(),
+                                                                       xx, z, beta, cols, Zi, S1);
+    GLOBE_LAUNCHED(ctx, "k_seg_sums_t");
+    if (rs.nbl) {
+        k_seg_sums<<<rs.nbl, RB_THREADS, 0, ctx->stream>>>(c.nlong, c.Nrec, c.N, c.bstart, c.bind, c.times(), xx, z,
+                                                            beta, cols, kact, Zi, S1, c.lblk);
+        GLOBE_LAUNCHED(ctx, "k_seg_sums");
     }
-    k_seg_sums<<<div_up(c.N, RB_WARPS), RB_THREADS, 0, ctx->stream>>>(
-        c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), xx, z, beta, cols, kact, Zi, S1);
-    GLOBE_LAUNCHED(ctx, "k_seg_sums");
     return GLOBE_OK;
 }
 
@@ -235,11 +249,12 @@ __global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t
                               const double* __restrict__ x, const double* __restrict__ GZ,
                               const double* __restrict__ Zi, const double* __restrict__ S1,
                               const int32_t* __restrict__ cols, int kact, double* __restrict__ out,
-                              double* __restrict__ part) {
+                              double* __restrict__ part, const int32_t* __restrict__ bl, int slot0, int pstride) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b = blockIdx.x * RB_WARPS + warp;
-    const bool live = b < nblk;
+    const int idx = blockIdx.x * RB_WARPS + warp;
+    const bool live = idx < nblk;
+    const int b = live ? (bl ? bl[idx] : idx) : 0;
     int st = 0, en = 0, i = 0;
     if (live) { st = bstart[b]; en = bstart[b + 1]; i = bind[b]; }
     for (int c = 0; c < kact; ++c) {
@@ -264,7 +279,7 @@ __global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t
             if (lane == 0) sm[c * RB_WARPS + warp] = dot;
         }
     }
-    if (part) cta_partials(sm, kact, part);
+    if (part) cta_partials(sm, kact, part, slot0 + blockIdx.x, pstride);
 }
 
 __global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32_t* __restrict__ bstart,
@@ -272,12 +287,12 @@ __global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32
                                 const double* __restrict__ x, const double* __restrict__ GZ,
                                 const double* __restrict__ Zi, const double* __restrict__ S1,
                                 const int32_t* __restrict__ cols, double* __restrict__ out,
-                                double* __restrict__ part) {
+                                double* __restrict__ part, int pstride) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     double dot[1] = {0.0};
-    if (b < nblk) {
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK) {   // long blocks: a warp each
         const int st = bstart[b], en = bstart[b + 1], i = bind[b];
         const double s0 = Zi[i + (size_t)c * N], s1 = S1[i + (size_t)c * N];
         const double g = GZ ? GZ[i + (size_t)c * N] : 0.0;
@@ -295,7 +310,7 @@ __global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32
     }
     if (part) {
         const int q[1] = {c};
-        cta_sums<1>(dot, q, part);
+        cta_sums<1>(dot, q, part, pstride);
     }
 }
 
@@ -303,24 +318,20 @@ int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double*
                 const int32_t* cols, int kact, double* out, double* dot_out) {
     auto& c = ctx->coh;
     VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
-    if (short_blocks(ctx)) {
-        const int nb = div_up(c.N, TB_THREADS);
-        double* part = nullptr;
-        if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
-        k_vx_assemble_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind,
-                                                                        c.times(), v, x, GZ, Zi, S1, cols, out, part);
-        GLOBE_LAUNCHED(ctx, "k_vx_assemble_t");
-        if (dot_out) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, dot_out));
-        return GLOBE_OK;
-    }
-    int nb = div_up(c.N, RB_WARPS);
+    const RecShape rs = rec_shape(ctx);
     double* part = nullptr;
-    if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
-    size_t sm = dot_out ? sizeof(double) * RB_WARPS * kact : 0;
-    k_vx_assemble<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(), v, x,
-                                                       GZ, Zi, S1, cols, kact, out, part);
-    GLOBE_LAUNCHED(ctx, "k_vx_assemble");
-    if (dot_out) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, dot_out));
+    if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)rs.S * kact * 2, &part));
+    k_vx_assemble_t<<<dim3(rs.nbt, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(),
+                                                                          v, x, GZ, Zi, S1, cols, out, part, rs.S);
+    GLOBE_LAUNCHED(ctx, "k_vx_assemble_t");
+    if (rs.nbl) {
+        const size_t sm = dot_out ? sizeof(double) * RB_WARPS * kact : 0;
+        k_vx_assemble<<<rs.nbl, RB_THREADS, sm, ctx->stream>>>(c.nlong, c.Nrec, c.N, c.bstart, c.bind, c.times(), v,
+                                                                x, GZ, Zi, S1, cols, kact, out, part, c.lblk, rs.nbt,
+                                                                rs.S);
+        GLOBE_LAUNCHED(ctx, "k_vx_assemble");
+    }
+    if (dot_out) GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, dot_out));
     return GLOBE_OK;
 }
 
@@ -332,11 +343,12 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
                              const double* __restrict__ alpha, double* __restrict__ x, double* __restrict__ r,
                              const double* __restrict__ p, const double* __restrict__ Vp,
                              double* __restrict__ z, const int32_t* __restrict__ cols, int kact,
-                             double* __restrict__ part) {
+                             double* __restrict__ part, const int32_t* __restrict__ bl, int slot0, int pstride) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b = blockIdx.x * RB_WARPS + warp;
-    const bool live = b < nblk;
+    const int idx = blockIdx.x * RB_WARPS + warp;
+    const bool live = idx < nblk;
+    const int b = live ? (bl ? bl[idx] : idx) : 0;
     int st = 0, en = 0;
     double h00 = 0, h01 = 0, h10 = 0, h11 = 0;
     if (live) {
@@ -383,19 +395,20 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
             sm[(kact + c) * RB_WARPS + warp] = rz;
         }
     }
-    cta_partials(sm, 2 * kact, part);
+    cta_partials(sm, 2 * kact, part, slot0 + blockIdx.x, pstride);
 }
 
 __global__ void k_pcg_update_t(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
                                const double* __restrict__ t, double inv_e, const double* __restrict__ H,
                                const double* __restrict__ alpha, double* __restrict__ x, double* __restrict__ r,
                                const double* __restrict__ p, const double* __restrict__ Vp, double* __restrict__ z,
-                               const int32_t* __restrict__ cols, int kact, double* __restrict__ part) {
+                               const int32_t* __restrict__ cols, int kact, double* __restrict__ part,
+                               int pstride) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     double acc[2] = {0.0, 0.0};   // |r|^2, r'z
-    if (b < nblk) {
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK) {
         const int st = bstart[b], en = bstart[b + 1];
         const double a = alpha[col];
         double* xc = x + (size_t)col * ld;
@@ -423,33 +436,28 @@ __global__ void k_pcg_update_t(int32_t nblk, int64_t ld, const int32_t* __restri
         }
     }
     const int qi[2] = {c, kact + c};
-    cta_sums<2>(acc, qi, part);
+    cta_sums<2>(acc, qi, part, pstride);
 }
 
 int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, double* r, const double* p,
                const double* Vp, double* z, const int32_t* cols, int kact, double* rr, double* rz) {
     auto& c = ctx->coh;
-    if (short_blocks(ctx)) {
-        const int nb = div_up(c.N, TB_THREADS);
-        double* part;
-        GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
-        k_pcg_update_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
-                                                                       1.0 / ctx->vc[0], H, alpha, x, r, p, Vp, z,
-                                                                       cols, kact, part);
-        GLOBE_LAUNCHED(ctx, "k_pcg_update_t");
-        GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rr));
-        GLOBE_RET(reduce_cols(ctx, part + (size_t)nb * kact, nb, kact, cols, rz));
-        return GLOBE_OK;
-    }
-    int nb = div_up(c.N, RB_WARPS);
+    const RecShape rs = rec_shape(ctx);
     double* part;
-    GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
-    size_t sm = sizeof(double) * RB_WARPS * kact * 2;
-    k_pcg_update<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0], H,
-                                                      alpha, x, r, p, Vp, z, cols, kact, part);
-    GLOBE_LAUNCHED(ctx, "k_pcg_update");
-    GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rr));
-    GLOBE_RET(reduce_cols(ctx, part + (size_t)nb * kact, nb, kact, cols, rz));
+    GLOBE_RET(ws(ctx, WS_PART, (size_t)rs.S * kact * 2, &part));
+    k_pcg_update_t<<<dim3(rs.nbt, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
+                                                                         1.0 / ctx->vc[0], H, alpha, x, r, p, Vp, z,
+                                                                         cols, kact, part, rs.S);
+    GLOBE_LAUNCHED(ctx, "k_pcg_update_t");
+    if (rs.nbl) {
+        const size_t sm = sizeof(double) * RB_WARPS * kact * 2;
+        k_pcg_update<<<rs.nbl, RB_THREADS, sm, ctx->stream>>>(c.nlong, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0],
+                                                               H, alpha, x, r, p, Vp, z, cols, kact, part, c.lblk,
+                                                               rs.nbt, rs.S);
+        GLOBE_LAUNCHED(ctx, "k_pcg_update");
+    }
+    GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, rr));
+    GLOBE_RET(reduce_cols(ctx, part + (size_t)rs.S * kact, rs.S, kact, cols, rz));
     return GLOBE_OK;
 }
 
@@ -457,11 +465,13 @@ int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, 
 __global__ void k_precond_apply(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
                                 const double* __restrict__ t, double inv_e, const double* __restrict__ H,
                                 const double* __restrict__ r, double* __restrict__ z,
-                                const int32_t* __restrict__ cols, int kact, double* __restrict__ part) {
+                                const int32_t* __restrict__ cols, int kact, double* __restrict__ part,
+                                const int32_t* __restrict__ bl, int slot0, int pstride) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b = blockIdx.x * RB_WARPS + warp;
-    const bool live = b < nblk;
+    const int idx = blockIdx.x * RB_WARPS + warp;
+    const bool live = idx < nblk;
+    const int b = live ? (bl ? bl[idx] : idx) : 0;
     int st = 0, en = 0;
     double h00 = 0, h01 = 0, h10 = 0, h11 = 0;
     if (live) {
@@ -497,18 +507,18 @@ __global__ void k_precond_apply(int32_t nblk, int64_t ld, const int32_t* __restr
             if (lane == 0) sm[c * RB_WARPS + warp] = rz;
         }
     }
-    if (part) cta_partials(sm, kact, part);
+    if (part) cta_partials(sm, kact, part, slot0 + blockIdx.x, pstride);
 }
 
 __global__ void k_precond_apply_t(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
                                   const double* __restrict__ t, double inv_e, const double* __restrict__ H,
                                   const double* __restrict__ r, double* __restrict__ z,
-                                  const int32_t* __restrict__ cols, double* __restrict__ part) {
+                                  const int32_t* __restrict__ cols, double* __restrict__ part, int pstride) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     double rz[1] = {0.0};
-    if (b < nblk) {
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK) {
         const int st = bstart[b], en = bstart[b + 1];
         const double* rc = r + (size_t)col * ld;
         double s0 = 0, s1 = 0;
@@ -528,31 +538,36 @@ __global__ void k_precond_apply_t(int32_t nblk, int64_t ld, const int32_t* __res
     }
     if (part) {
         const int qi[1] = {c};
-        cta_sums<1>(rz, qi, part);
+        cta_sums<1>(rz, qi, part, pstride);
     }
+}
+
+// z = Q^-1 r (+ r'z partials into part[slot + c * rs.S]): one thread per short block,
+// one warp per long block
+static int precond_launch(globe_ctx* ctx, const double* H, const double* r, double* z, const int32_t* cols, int kact,
+                          double* part, const RecShape& rs) {
+    auto& c = ctx->coh;
+    k_precond_apply_t<<<dim3(rs.nbt, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
+                                                                            1.0 / ctx->vc[0], H, r, z, cols, part,
+                                                                            rs.S);
+    GLOBE_LAUNCHED(ctx, "k_precond_apply_t");
+    if (rs.nbl) {
+        const size_t sm = part ? sizeof(double) * RB_WARPS * kact : 0;
+        k_precond_apply<<<rs.nbl, RB_THREADS, sm, ctx->stream>>>(c.nlong, c.Nrec, c.bstart, c.times(),
+                                                                  1.0 / ctx->vc[0], H, r, z, cols, kact, part, c.lblk,
+                                                                  rs.nbt, rs.S);
+        GLOBE_LAUNCHED(ctx, "k_precond_apply");
+    }
+    return GLOBE_OK;
 }
 
 int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z, const int32_t* cols, int kact,
                   double* rz) {
-    auto& c = ctx->coh;
-    if (short_blocks(ctx)) {
-        const int nb = div_up(c.N, TB_THREADS);
-        double* part = nullptr;
-        if (rz) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
-        k_precond_apply_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
-                                                                          1.0 / ctx->vc[0], H, r, z, cols, part);
-        GLOBE_LAUNCHED(ctx, "k_precond_apply_t");
-        if (rz) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rz));
-        return GLOBE_OK;
-    }
-    int nb = div_up(c.N, RB_WARPS);
+    const RecShape rs = rec_shape(ctx);
     double* part = nullptr;
-    if (rz) GLOBE_RET(ws(ctx, WS_PART, (size_t)nb * kact * 2, &part));
-    size_t sm = rz ? sizeof(double) * RB_WARPS * kact : 0;
-    k_precond_apply<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0], H,
-                                                         r, z, cols, kact, part);
-    GLOBE_LAUNCHED(ctx, "k_precond_apply");
-    if (rz) GLOBE_RET(reduce_cols(ctx, part, nb, kact, cols, rz));
+    if (rz) GLOBE_RET(ws(ctx, WS_PART, (size_t)rs.S * kact * 2, &part));
+    GLOBE_RET(precond_launch(ctx, H, r, z, cols, kact, part, rs));
+    if (rz) GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, rz));
     return GLOBE_OK;
 }
 
@@ -561,25 +576,13 @@ int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z, c
 // partial slot, so the scratch needs no clearing.
 int precond_apply_scratch(globe_ctx* ctx, const double* H, const double* r, double* z, int kact, double* part,
                           size_t part_cap, double* rz) {
-    auto& c = ctx->coh;
-    const bool thr = short_blocks(ctx);
-    const int nb = thr ? div_up(c.N, TB_THREADS) : div_up(c.N, RB_WARPS);
-    if (rz && (size_t)nb * kact > part_cap)
+    const RecShape rs = rec_shape(ctx);
+    if (rz && (size_t)rs.S * kact > part_cap)
         return set_err(ctx, GLOBE_ERR_ARG,
                        "r'z partials need %zu doubles of scratch (%d CTAs x %d columns); the static buffer holds %zu",
-                       (size_t)nb * kact, nb, kact, part_cap);
-    double* pp = rz ? part : nullptr;
-    if (thr) {
-        k_precond_apply_t<<<dim3(nb, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(),
-                                                                          1.0 / ctx->vc[0], H, r, z, nullptr, pp);
-        GLOBE_LAUNCHED(ctx, "k_precond_apply_t");
-    } else {
-        const size_t sm = rz ? sizeof(double) * RB_WARPS * kact : 0;
-        k_precond_apply<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0], H,
-                                                             r, z, nullptr, kact, pp);
-        GLOBE_LAUNCHED(ctx, "k_precond_apply");
-    }
-    if (rz) GLOBE_RET(reduce_cols(ctx, part, nb, kact, nullptr, rz));
+                       (size_t)rs.S * kact, rs.S, kact, part_cap);
+    GLOBE_RET(precond_launch(ctx, H, r, z, nullptr, kact, rz ? part : nullptr, rs));
+    if (rz) GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, nullptr, rz));
     return GLOBE_OK;
 }
 
@@ -880,7 +883,7 @@ __global__ void k_trace_terms(int32_t nblk, int64_t n, int32_t N, const int32_t*
             if (lane == 0) sm[(j * 5 + k) * RB_WARPS + warp] = s;
         }
     }
-    cta_partials(sm, numMC * 5, part);
+    cta_partials(sm, numMC * 5, part, blockIdx.x, gridDim.x);
 }
 
 int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double* TY, int numMC, double* out) {

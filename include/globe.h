@@ -174,9 +174,9 @@ int globe_genetic_diag(globe_ctx* ctx, double* diag);
  * capture, or where the implicit device synchronisation of an allocation is
  * not allowed).
  *  - The r'z partials use one static 2 MiB device buffer (2^18 doubles).  A
- *    call needing more (about k x N/256 doubles, or k x N/8 when an individual
- *    has more than 48 records) returns GLOBE_ERR_ARG before launching
- *    anything.  Nothing in the buffer needs to start at zero.
+ *    call needing more -- k x (ceil(N/256) + ceil(L/8)) doubles, L the number
+ *    of individuals with more than 48 records -- returns GLOBE_ERR_ARG before
+ *    launching anything.  Nothing in the buffer needs to start at zero.
  *  - The buffer is shared by every context on a device: calls that overlap
  *    on the GPU (other streams or contexts on the same device) race on it.
  *  - The preconditioner must already be built at the current components

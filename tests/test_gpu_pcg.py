@@ -83,3 +83,26 @@ def test_dense_and_odd_sizes(gctx, orc):
     X, info = gctx.pcg(B, tol=1e-12, rule=G.RULE_PCGSOLVER)
     Xo, it = s.pcg(B, 1e-12, rule=0)
     assert rel(X, Xo) < 1e-9
+
+
+@pytest.mark.parametrize("precision", [G.PREC_FP64, G.PREC_MIXED])
+def test_mixed_block_lengths(gctx, orc, precision):
+    """Record blocks of 1-150 records: one thread per block of <= 48 records and one
+    warp per longer block, side by side in every record kernel."""
+    coh = cohort(23, 300, 400, recs=("geometric", 0.04, 1, 150), T=10.0, miss=0.02)
+    counts = np.bincount(coh["indiv"])
+    assert counts.max() > 48 and counts.min() <= 48
+    indiv = coh["indiv"].astype(np.int32)
+    gctx.load_records(indiv, coh["X"], coh["y"], 300)
+    gctx.load_bed(coh["packed"])
+    gctx.set_vc(VC_F)
+    s = orc.Solver(indiv, coh["X"], coh["y"], 300, VC_F, packed=coh["packed"])
+    s.precond_build()
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((len(indiv), 4))
+    assert rel(gctx.vx(x), s.vx(x)) < 1e-11
+    assert rel(gctx.precond_apply(x), s.precond_apply(x)) < 1e-12
+    B = np.column_stack([coh["X"], coh["y"]])
+    X, info = gctx.pcg(B, tol=1e-12, rule=G.RULE_PCGSOLVER, precision=precision)
+    Xo, it = s.pcg(B, 1e-12, rule=0)
+    assert rel(X, Xo) < 1e-9

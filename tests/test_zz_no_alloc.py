@@ -20,9 +20,18 @@ GLOBE_ERR_ARG, GLOBE_ERR_STATE = -1, -3
 def _counts(layout, rng):
     if layout == "short_blocks":             # every block <= 48 records: one thread per (block, column)
         return rng.integers(1, 11, size=3000)
-    c = rng.integers(1, 6, size=2000)          # a few blocks > 48 records: one warp per block
+    if layout == "all_long":                 # every block > 48 records: one warp per block
+        return np.full(2000, 49)
+    c = rng.integers(1, 6, size=2000)          # a few blocks > 48 records get a warp each, the rest a thread
     c[[5, 777, 1999]] = (60, 49, 120)
     return c
+
+
+def _partial_slots(counts):
+    """CTAs writing r'z partials per column: one per 256 blocks (thread layout) plus one
+    per 8 blocks longer than 48 records (warp layout)."""
+    nlong = int((np.asarray(counts) > 48).sum())
+    return (len(counts) + 255) // 256 + (nlong + 7) // 8
 
 
 def _setup(ctx, layout, seed):
@@ -80,10 +89,10 @@ def test_matches_precond_apply_on_two_calls(layout):
 def test_rejects_sizes_beyond_static_buffer():
     torch = pytest.importorskip("torch")
     with G.Context(0) as ctx:
-        N, Nrec, rng = _setup(ctx, "long_blocks", 12)
-        nb = (N + 7) // 8                      # CTAs of the one-warp-per-block layout
-        k = PART_DOUBLES // nb + 1             # first width whose partials do not fit
-        r = rng.standard_normal((Nrec, k))
+        N, Nrec, rng = _setup(ctx, "all_long", 12)
+        k = PART_DOUBLES // _partial_slots(np.full(N, 49)) + 1    # first width whose partials do not fit
+        r = np.zeros((Nrec, k))
+        r[:, :2] = rng.standard_normal((Nrec, 2))
         z_ref = ctx.precond_apply(r[:, :2])
         dr = _dev(torch, r)
         dz = torch.zeros_like(dr)
