@@ -68,6 +68,8 @@ SIGNATURES = {
                                  C.POINTER(BedInfo)]),
     "globe_load_bed_dev": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, C.c_float, C.c_float, _vp, _vp, _vp, _vp,
                                      _vp, C.POINTER(BedInfo)]),
+    "globe_load_bed_file": (C.c_int, [_vp, C.c_char_p, C.c_float, C.c_float, C.c_int64, _i64p, _i64p, _fp, _fp,
+                                      _u8p, C.POINTER(BedInfo)]),
     "globe_load_grm": (C.c_int, [_vp, _fp, C.c_int32]),
     "globe_set_vc": (C.c_int, [_vp, _dp]),
     "globe_grm_apply": (C.c_int, [_vp, _dp, _dp, C.c_int]),

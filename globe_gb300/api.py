@@ -113,6 +113,26 @@ class Context:
                                         C.byref(info)))
         return dict(alt=alt, miss=miss, maf=maf, miss_rate=mr, keep=keep.astype(bool), kept=info.kept)
 
+    def load_bed_file(self, prefix, min_maf=0.01, max_miss=0.2, chunk_bytes=0):
+        """Stream <prefix>.bed from disk (globe_load_bed_file); same result as load_bed."""
+        lib = self._L
+        err = C.create_string_buffer(1024)
+        M = C.c_int64()
+        rc = lib.globe_bed_dims(prefix.encode(), self.N, C.byref(M), err, 1024)
+        if rc:
+            raise GlobeError(rc, err.value.decode())
+        M = M.value
+        alt = np.zeros(M, np.int64)
+        miss = np.zeros(M, np.int64)
+        maf = np.zeros(M, np.float32)
+        mr = np.zeros(M, np.float32)
+        keep = np.zeros(M, np.uint8)
+        info = L.BedInfo()
+        self._ck(lib.globe_load_bed_file(self.h, prefix.encode(), C.c_float(min_maf), C.c_float(max_miss),
+                                         int(chunk_bytes), _p(alt, C.c_int64), _p(miss, C.c_int64),
+                                         _p(maf, C.c_float), _p(mr, C.c_float), _p(keep, C.c_uint8), C.byref(info)))
+        return dict(alt=alt, miss=miss, maf=maf, miss_rate=mr, keep=keep.astype(bool), kept=info.kept)
+
     def load_bed_dev(self, d_ptr, M, stride, min_maf=0.01, max_miss=0.2):
         info = L.BedInfo()
         self._ck(self._L.globe_load_bed_dev(self.h, C.c_void_p(d_ptr), M, stride, C.c_float(min_maf),

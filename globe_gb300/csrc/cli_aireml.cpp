@@ -81,15 +81,9 @@ int main(int argc, char** argv) {
     std::printf("Found N = %d indivuduals, \n      p = %d fixed effects (in addition to TIME), and\n      Nrec = %lld "
                 "records in the input file.\n", N, p, (long long)Nrec);
     std::vector<float> A;
-    std::vector<uint8_t> bed;
-    int64_t M = 0;
     if (geno.empty()) {
         A.resize((size_t)N * (N + 1) / 2);
         if (globe_read_grm(grm.c_str(), N, A.data(), err, sizeof err)) return fail(err);
-    } else {
-        if (globe_bed_dims(geno.c_str(), N, &M, err, sizeof err)) return fail(err);
-        bed.resize((size_t)M * ((N + 3) / 4));
-        if (globe_read_bed(geno.c_str(), N, M, bed.data(), err, sizeof err)) return fail(err);
     }
     std::vector<double> probes;
     if (!probes_file.empty()) {
@@ -111,12 +105,13 @@ int main(int argc, char** argv) {
     if (geno.empty()) {
         if (globe_load_grm(ctx, A.data(), N)) return die("GRM");
     } else {
+        // streamed from disk in chunks (globe_load_bed_file)
         globe_bed_info info{};
-        if (globe_load_bed(ctx, bed.data(), M, min_maf, max_miss, nullptr, nullptr, nullptr, nullptr, nullptr, &info))
+        if (globe_load_bed_file(ctx, geno.c_str(), min_maf, max_miss, 0, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                &info))
             return die("genotypes");
-        std::printf("%lld of %lld SNPs pass the MAF / missingness filter.\n", (long long)info.kept, (long long)M);
-        bed.clear();
-        bed.shrink_to_fit();
+        std::printf("%lld of %lld SNPs pass the MAF / missingness filter.\n", (long long)info.kept,
+                    (long long)info.M);
     }
     std::printf("Input files read and processed successfully.\nRunning AI-REML...\n");
     globe_aireml_opts o{};

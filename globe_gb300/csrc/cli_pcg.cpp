@@ -133,21 +133,14 @@ int main(int argc, char** argv) {
     };
     if (globe_load_records(ctx, Nrec, N, p, indiv.data(), X.data(), y.data())) return die("records");
     if (!geno.empty()) {
-        int64_t M = 0;
-        if (globe_bed_dims(geno.c_str(), N, &M, err, sizeof err)) {
-            globe_destroy(ctx);
-            return fail(err);
-        }
-        std::vector<uint8_t> bed((size_t)M * ((N + 3) / 4));
-        if (globe_read_bed(geno.c_str(), N, M, bed.data(), err, sizeof err)) {
-            globe_destroy(ctx);
-            return fail(err);
-        }
+        // streamed from disk in chunks (globe_load_bed_file): the file never sits whole in host memory
         globe_bed_info bi{};
-        if (globe_load_bed(ctx, bed.data(), M, min_maf, max_miss, nullptr, nullptr, nullptr, nullptr, nullptr, &bi))
+        if (globe_load_bed_file(ctx, geno.c_str(), min_maf, max_miss, 0, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                &bi))
             return die("genotypes");
-        std::printf("[prepGenotypeInput] Processed %lld / %lld SNPs.\n", (long long)M, (long long)M);
-        if (debug) std::printf("[prepGenotypeInput] Filtered SNPs = %lld / %lld\n", (long long)bi.kept, (long long)M);
+        const long long M = (long long)bi.M;
+        std::printf("[prepGenotypeInput] Processed %lld / %lld SNPs.\n", M, M);
+        if (debug) std::printf("[prepGenotypeInput] Filtered SNPs = %lld / %lld\n", (long long)bi.kept, M);
     } else {
         std::vector<float> A((size_t)N * (N + 1) / 2);
         if (globe_read_grm(grm.c_str(), N, A.data(), err, sizeof err)) {

@@ -133,6 +133,15 @@ int globe_load_bed(globe_ctx* ctx, const uint8_t* bed, int64_t M, float min_maf,
 int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride,
                        float min_maf, float max_miss, int64_t* d_alt, int64_t* d_miss,
                        float* d_maf, float* d_miss_rate, uint8_t* d_keep, globe_bed_info* info);
+/* Same from <prefix>.bed on disk, streamed: whole SNP rows are read in chunks
+ * of about chunk_bytes (0: 256 MB) into two pinned host buffers taken in turn,
+ * each copied to the device while the next is read; host memory stays at two
+ * chunks.  M is the number of lines of <prefix>.bim.  Replaces the serial
+ * whole-file read of prepGenotypeInput (PCGsolver.cpp:706-749).  Per-SNP
+ * outputs are host pointers (may be NULL), as in globe_load_bed. */
+int globe_load_bed_file(globe_ctx* ctx, const char* prefix, float min_maf, float max_miss, int64_t chunk_bytes,
+                        int64_t* alt_count, int64_t* miss_count, float* maf, float* miss_rate, uint8_t* keep,
+                        globe_bed_info* info);
 
 /* Dense GRM: float32 packed lower triangle, row major with the diagonal,
  * N(N+1)/2 values (.grm.bin payload).  Replaces readFullGRM

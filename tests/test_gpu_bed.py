@@ -40,3 +40,39 @@ def test_no_snp_passes(gctx):
     gctx.load_records(coh["indiv"], coh["X"], coh["y"], 40)
     st = gctx.load_bed(coh["packed"], 0.5, 0.0)   # maf must be exactly 0.5
     assert st["kept"] == int(st["keep"].sum())
+
+
+@pytest.mark.parametrize("chunk", [0, 1, 3 * 13, 1000])
+def test_streamed_file_matches_in_memory(gctx, tmp_path, chunk):
+    """globe_load_bed_file (chunked reads through pinned buffers, 2-D copies into padded
+    device rows) gives the in-memory load's statistics and the same genetic source;
+    chunk sizes of one row, a few rows with a ragged tail, and the default."""
+    from globe_gb300 import synth
+    coh = cohort(71, 51, 211, recs=("uniform", 1, 3), miss=0.05, edge=True)
+    pre = synth.write_cohort(str(tmp_path), "s", coh)
+    gctx.load_records(coh["indiv"], coh["X"], coh["y"], 51)
+    ref = gctx.load_bed(coh["packed"])
+    z = np.random.default_rng(1).standard_normal((51, 3))
+    g_ref = gctx.grm_apply(z)
+    st = gctx.load_bed_file(pre, chunk_bytes=chunk)
+    for k in ("alt", "miss", "keep"):
+        assert np.array_equal(st[k], ref[k]), k
+    assert np.array_equal(st["maf"].view(np.uint32), ref["maf"].view(np.uint32))
+    assert st["kept"] == ref["kept"]
+    assert np.array_equal(gctx.grm_apply(z), g_ref)
+
+
+def test_streamed_file_errors(gctx, tmp_path):
+    import globe_gb300 as G
+    from globe_gb300 import synth
+    coh = cohort(72, 40, 30, recs=("uniform", 1, 2))
+    pre = synth.write_cohort(str(tmp_path), "e", coh)
+    gctx.load_records(coh["indiv"], coh["X"], coh["y"], 40)
+    with open(pre + ".bed", "r+b") as f:                 # drop the last SNP row
+        f.truncate(3 + 29 * 10)
+    with pytest.raises(G.GlobeError) as e:
+        gctx.load_bed_file(pre)
+    assert e.value.code == -5
+    with pytest.raises(G.GlobeError) as e:
+        gctx.load_bed_file(str(tmp_path / "missing"))
+    assert e.value.code == -4
