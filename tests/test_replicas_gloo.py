@@ -37,9 +37,9 @@ def _rank(rank, world, port, out):
 def test_two_rank_aggregation():
     pytest.importorskip("torch.distributed")
     world, port = 2, _free_port()
-    with mp.Manager() as m:
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as m:
         out = m.dict()
-        ctx = mp.get_context("spawn")
         procs = [ctx.Process(target=_rank, args=(r, world, port, out)) for r in range(world)]
         for p in procs:
             p.start()
