@@ -15,6 +15,7 @@ ERRORS = {-1: "GLOBE_ERR_ARG", -2: "GLOBE_ERR_CUDA", -3: "GLOBE_ERR_STATE", -4: 
           -5: "GLOBE_ERR_FORMAT", -6: "GLOBE_ERR_NOMEM", -7: "GLOBE_ERR_NUMERIC", -8: "GLOBE_ERR_UNSUPPORTED"}
 PREC_FP64, PREC_MIXED = 0, 1
 RULE_PCGSOLVER, RULE_AIREML = 0, 1
+MODEL_FULL, MODEL_NO_TIME = 0, 1
 X0_ZERO, X0_PRECOND, X0_GIVEN = 0, 1, 2
 PROF_GRM, PROF_GRM_PASS1, PROF_GRM_PASS2, PROF_PCG_ITER = 0, 1, 2, 3
 
@@ -95,6 +96,11 @@ SIGNATURES = {
     "globe_read_bed": (C.c_int, [C.c_char_p, C.c_int32, C.c_int64, _u8p, C.c_char_p, C.c_int]),
     "globe_read_grm": (C.c_int, [C.c_char_p, C.c_int32, _fp, C.c_char_p, C.c_int]),
     "globe_set_precision": (C.c_int, [_vp, C.c_int]),
+    "globe_set_model": (C.c_int, [_vp, C.c_int]),
+    "globe_get_model": (C.c_int, [_vp]),
+    "globe_trust_region_step_no_time": (C.c_int, [_dp, _dp, _dp, C.c_double, _dp, C.POINTER(C.c_int)]),
+    "globe_read_records_no_time": (C.c_int, [C.c_char_p, _i64p, _i32p, _i32p, _i32p, _dp, _dp, C.c_char_p,
+                                             C.c_int]),
     "globe_prof_enable": (C.c_int, [_vp, C.c_int]),
     "globe_prof_query": (C.c_int, [_vp, C.c_int, _i64p, _dp]),
     "globe_precond_apply_dev_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),

@@ -151,6 +151,15 @@ class Context:
     def set_precision(self, precision):
         self._ck(self._L.globe_set_precision(self.h, precision))
 
+    def _probe_draws(self):
+        """Normal draws per probe: Z1 (N), Z2 (2N, time effects only), Z3 (Nrec)."""
+        no_time = self._L.globe_get_model(self.h) == L.MODEL_NO_TIME
+        return (1 if no_time else 3) * self.N + self.Nrec
+
+    def set_model(self, model):
+        """MODEL_FULL (default) or MODEL_NO_TIME (components sig2e, sig2g only)."""
+        self._ck(self._L.globe_set_model(self.h, model))
+
     def set_vc(self, vc):
         v = np.ascontiguousarray(vc, dtype=np.float64)
         self._ck(self._L.globe_set_vc(self.h, _p(v)))
@@ -228,7 +237,7 @@ class Context:
         info = PcgInfo()
         pr = None if probes is None else np.ascontiguousarray(probes, dtype=np.float64)
         if pr is not None:
-            assert pr.size == numMC * (3 * self.N + self.Nrec)
+            assert pr.size == numMC * self._probe_draws()
         fth = np.zeros((self.Nrec, 5), order="F")
         first, trace, grad = np.zeros(5), np.zeros(5), np.zeros(5)
         self._ck(self._L.globe_aireml_grad(self.h, _p(pr), numMC, C.c_uint64(seed), C.byref(o), _p(fth),
@@ -242,7 +251,7 @@ class Context:
         info = PcgInfo()
         pr = None if probes is None else np.ascontiguousarray(probes, dtype=np.float64)
         if pr is not None:
-            assert pr.size == numMC * (3 * self.N + self.Nrec)
+            assert pr.size == numMC * self._probe_draws()
         first, trace, grad = np.zeros(5), np.zeros(5), np.zeros(5)
         self._ck(self._L.globe_aireml_eval(self.h, _p(pr), numMC, C.c_uint64(seed), C.byref(o), _p(first),
                                            _p(trace), _p(grad), C.byref(info)))
@@ -290,6 +299,20 @@ def trust_region_step(theta, grad, ai, delta):
     return p, st.value
 
 
+def trust_region_step_no_time(theta, grad, ai, delta):
+    """Step of the model without time effects (two components;
+    varCompEst_reducedModel_noTime.cpp:782-830)."""
+    th = np.ascontiguousarray(theta[:2], np.float64)
+    g = np.ascontiguousarray(grad[:2], np.float64)
+    A = np.asfortranarray(np.asarray(ai)[:2, :2], np.float64).ravel(order="F").copy()
+    p = np.zeros(2)
+    st = C.c_int(0)
+    rc = L.lib().globe_trust_region_step_no_time(_p(th), _p(g), _p(A), C.c_double(delta), _p(p), C.byref(st))
+    if rc != L.GLOBE_OK:
+        raise GlobeError(rc, "trust-region step")
+    return p, st.value
+
+
 # ---- files ---------------------------------------------------------------
 
 def read_records(path):
@@ -306,6 +329,26 @@ def read_records(path):
     y = np.zeros(Nrec.value)
     rc = lib.globe_read_records(path.encode(), C.byref(Nrec), C.byref(N), C.byref(p), _p(indiv, C.c_int32), _p(X),
                                 _p(y), err, 1024)
+    if rc:
+        raise GlobeError(rc, err.value.decode())
+    return indiv, X, y, N.value
+
+
+def read_records_no_time(path):
+    """Record table of the model without time effects: INDIV, PHENO and covariates
+    in file order.  Returns indiv, X (Nrec x p), y, N."""
+    lib = L.lib()
+    err = C.create_string_buffer(1024)
+    Nrec, N, p = C.c_int64(), C.c_int32(), C.c_int32()
+    rc = lib.globe_read_records_no_time(path.encode(), C.byref(Nrec), C.byref(N), C.byref(p), None, None, None,
+                                        err, 1024)
+    if rc:
+        raise GlobeError(rc, err.value.decode())
+    indiv = np.zeros(Nrec.value, np.int32)
+    X = np.zeros((Nrec.value, p.value), order="F")
+    y = np.zeros(Nrec.value)
+    rc = lib.globe_read_records_no_time(path.encode(), C.byref(Nrec), C.byref(N), C.byref(p), _p(indiv, C.c_int32),
+                                        _p(X), _p(y), err, 1024)
     if rc:
         raise GlobeError(rc, err.value.decode())
     return indiv, X, y, N.value

@@ -26,7 +26,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", os.path.join(ROOT, "include"),
           "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 LIB_SOURCES = ["api.cu", "k_bed.cu", "k_records.cu", "k_grm_geno.cu", "k_grm_dense.cu", "k_tc_geno.cu", "solver.cu", "noalloc.cu", "ingest.cu",
                "aireml.cpp", "io.cpp"]
-CLI = {"runPCGsolver": "cli_pcg.cpp", "runAIREML": "cli_aireml.cpp"}
+# program -> (source, extra flags)
+CLI = {"runPCGsolver": ("cli_pcg.cpp", []), "runAIREML": ("cli_aireml.cpp", []),
+       "runAIREML_reducedModel": ("cli_aireml.cpp", ["-DGLOBE_NO_TIME"])}
 
 
 def _newer(target, deps):
@@ -63,11 +65,11 @@ def build(verbose=True):
     if _newer(LIB, objs):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
         subprocess.check_call(cmd)
-    for name, src in (CLI.items() if not TAG else []):
+    for name, (src, flags) in (CLI.items() if not TAG else []):
         s = os.path.join(SRC, src)
         exe = os.path.join(BIN, name)
         if os.path.exists(s) and _newer(exe, [s, LIB] + _headers()):
-            cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), s, "-o", exe,
+            cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include")] + flags + [s, "-o", exe,
                    "-L", HERE, "-lglobe_gb300", "-Wl,-rpath,$ORIGIN/.."]
             subprocess.check_call(cmd)
     if verbose:

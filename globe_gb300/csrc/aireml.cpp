@@ -1,4 +1,8 @@
-// aireml.cpp -- AIREML outer loop (host C++) and its trust-region step.
+// aireml.cpp -- AIREML outer loop (host C++) and its trust-region steps.
+//
+// Two models: runAIREML's five components, and runAIREML_reducedModel's two
+// (sig2e, sig2g; no time effects, varCompEst_reducedModel_noTime.cpp:782-1090),
+// chosen by globe_set_model on the context.
 //
 // The loop mirrors runAIREML's main and oneIter_AIREML
 // (varCompEst.cpp:1148-1344, :1415-1491): gradient from the Monte-Carlo score,
@@ -242,6 +246,101 @@ extern "C" int globe_trust_region_step(const double theta[5], const double grad[
 }
 
 // ---------------------------------------------------------------------------
+// Step of the model without time effects: two components, linear constraints only
+//
+//   max  g'p - p'Ap/2  s.t.  |p_k| <= 10,  A_00 p_0 + A_11 p_1 <= Delta,
+//        theta_k + p_k >= 1e-5                (varCompEst_reducedModel_noTime.cpp:782-830)
+//
+// In two variables the maximiser is a stationary point of the objective restricted
+// to the intersection of at most two active constraints (interior, an edge, or a
+// vertex); every such candidate is formed and the best feasible one is kept.
+
+namespace {
+
+int solve_tr2(const double* th, const double* g, const double* A, double delta, double* pout) {
+    const double S00 = A[0], S11 = A[3], S01 = 0.5 * (A[1] + A[2]);   // symmetric part
+    struct Row {
+        double a0, a1, b;   // a . p <= b
+    };
+    std::vector<Row> rows = {{1, 0, 10}, {-1, 0, 10}, {0, 1, 10}, {0, -1, 10}, {A[0], A[3], delta},
+                             {-1, 0, th[0] - 1e-5}, {0, -1, th[1] - 1e-5}};
+    auto feasible = [&](double p0, double p1) {
+        for (const Row& r : rows) {
+            const double lhs = r.a0 * p0 + r.a1 * p1;
+            const double tol = 1e-12 * std::fmax(1.0, std::fmax(std::fabs(r.b), std::fabs(r.a0 * p0) + std::fabs(r.a1 * p1)));
+            if (lhs > r.b + tol) return false;
+        }
+        return true;
+    };
+    auto obj = [&](double p0, double p1) {
+        return g[0] * p0 + g[1] * p1 - 0.5 * (S00 * p0 * p0 + 2.0 * S01 * p0 * p1 + S11 * p1 * p1);
+    };
+    bool found = false;
+    double best = -INFINITY, b0 = 0, b1 = 0;
+    auto consider = [&](double p0, double p1) {
+        if (!std::isfinite(p0) || !std::isfinite(p1) || !feasible(p0, p1)) return;
+        const double f = obj(p0, p1);
+        if (!found || f > best) {
+            found = true;
+            best = f;
+            b0 = p0;
+            b1 = p1;
+        }
+    };
+    // interior: S p = g
+    const double det = S00 * S11 - S01 * S01;
+    if (det != 0.0) consider((S11 * g[0] - S01 * g[1]) / det, (S00 * g[1] - S01 * g[0]) / det);
+    const int m = (int)rows.size();
+    for (int i = 0; i < m; ++i) {
+        // one active row: stationary point of the objective on the line a.p = b
+        // [S a; a' 0] [p; lam] = [g; b]
+        const Row& r = rows[i];
+        const double M[3][3] = {{S00, S01, r.a0}, {S01, S11, r.a1}, {r.a0, r.a1, 0.0}};
+        const double rhs[3] = {g[0], g[1], r.b};
+        const double d3 = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                          M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                          M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+        if (d3 != 0.0) {
+            double x[3];
+            for (int c = 0; c < 3; ++c) {   // Cramer's rule
+                double T[3][3];
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) T[a][b] = b == c ? rhs[a] : M[a][b];
+                x[c] = (T[0][0] * (T[1][1] * T[2][2] - T[1][2] * T[2][1]) -
+                        T[0][1] * (T[1][0] * T[2][2] - T[1][2] * T[2][0]) +
+                        T[0][2] * (T[1][0] * T[2][1] - T[1][1] * T[2][0])) / d3;
+            }
+            consider(x[0], x[1]);
+        }
+        for (int j = i + 1; j < m; ++j) {   // two active rows: their intersection
+            const Row& q = rows[j];
+            const double d2 = r.a0 * q.a1 - r.a1 * q.a0;
+            if (d2 == 0.0) continue;
+            consider((r.b * q.a1 - r.a1 * q.b) / d2, (r.a0 * q.b - r.b * q.a0) / d2);
+        }
+    }
+    if (!found) return 1;
+    pout[0] = b0;
+    pout[1] = b1;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int globe_trust_region_step_no_time(const double theta[2], const double grad[2], const double ai[4],
+                                               double delta, double p[2], int* status) {
+    if (!theta || !grad || !ai || !p) return GLOBE_ERR_ARG;
+    for (int k = 0; k < 2; ++k)
+        if (!std::isfinite(theta[k]) || !std::isfinite(grad[k])) return GLOBE_ERR_ARG;
+    for (int e = 0; e < 4; ++e)
+        if (!std::isfinite(ai[e])) return GLOBE_ERR_ARG;
+    const int st = solve_tr2(theta, grad, ai, delta, p);
+    if (st != 0) p[0] = p[1] = 0.0;
+    if (status) *status = st;
+    return GLOBE_OK;
+}
+
+// ---------------------------------------------------------------------------
 // AIREML loop
 
 namespace {
@@ -350,7 +449,8 @@ struct Driver {
         return GLOBE_OK;
     }
     int64_t n_rec = 0, n_ind = 0;
-    int64_t probes_per_eval() const { return (int64_t)o->numMC * (3 * n_ind + n_rec); }
+    int nc = 5;   // components of the model (2 without time effects)
+    int64_t probes_per_eval() const { return (int64_t)o->numMC * ((nc == 5 ? 3 : 1) * n_ind + n_rec); }
 
     int eval_ai(double* ai) {
         globe_pcg_info info{};
@@ -390,11 +490,19 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
         if (!d.log.f) return GLOBE_ERR_IO;
     }
     std::memset(res, 0, sizeof(*res));
+    // model: runAIREML (5 components) or runAIREML_reducedModel (sig2e, sig2g; no time effects)
+    const int nc = globe_get_model(ctx) == GLOBE_MODEL_NO_TIME ? 2 : 5;
+    d.nc = nc;
     double theta[5], grad[5], ai[25];
     std::memcpy(theta, o->theta0, sizeof(theta));
-    d.log.printf("Running AI-REML...\nInitial variance components: \n  sig2e = %.17g, \n  sig2g = %.17g, \n"
-                 "  sig2b0 = %.17g, \n  sigb01 = %.17g, \n  sig2b1 = %.17g\n",
-                 theta[0], theta[1], theta[2], theta[3], theta[4]);
+    for (int k = nc; k < 5; ++k) theta[k] = 0.0;
+    if (nc == 5)
+        d.log.printf("Running AI-REML...\nInitial variance components: \n  sig2e = %.17g, \n  sig2g = %.17g, \n"
+                     "  sig2b0 = %.17g, \n  sigb01 = %.17g, \n  sig2b1 = %.17g\n",
+                     theta[0], theta[1], theta[2], theta[3], theta[4]);
+    else
+        d.log.printf("Running AI-REML...\nInitial variance components: \n  sig2e = %.17g, \n  sig2g = %.17g\n",
+                     theta[0], theta[1]);
     double Delta = 1e20;
     bool dangerous = false, converged = false;
     int num_rej = 0;
@@ -423,12 +531,13 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
             // varCompEst.cpp:1431-1451 draws the restart with rand(); here a
             // seeded stream (same distribution, U[0.1, 0.9])
             d.log.printf("Too many rejections at current point. Re-initalizing optimization.\n");
-            for (int k = 0; k < 5; ++k) {
+            for (int k = 0; k < nc; ++k) {
                 restart_state = smix(restart_state);
                 theta[k] = 0.1 + 0.8 * ((double)(restart_state >> 11) * (1.0 / 9007199254740992.0));
             }
-            if (theta[3] > std::sqrt(theta[2] * theta[4])) theta[3] = std::sqrt(theta[2] * theta[4]) - 1e-3;
-            d.log.vec("Re-initialized variance components:", theta, 5);
+            if (nc == 5 && theta[3] > std::sqrt(theta[2] * theta[4]))
+                theta[3] = std::sqrt(theta[2] * theta[4]) - 1e-3;
+            d.log.vec("Re-initialized variance components:", theta, nc);
             TRY(d.eval_grad(theta, grad));
             TRY(d.eval_ai(ai));
             num_rej = 0;
@@ -437,9 +546,14 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
         std::memcpy(theta_old, theta, sizeof(theta));
         {
             // ---- oneIter_AIREML (varCompEst.cpp:1148-1344) ----
-            double p[5];
+            double p[5] = {0, 0, 0, 0, 0};
             int st = 0;
-            TRY(globe_trust_region_step(theta, grad, ai, Delta, p, &st));
+            if (nc == 5) {
+                TRY(globe_trust_region_step(theta, grad, ai, Delta, p, &st));
+            } else {
+                const double ai2[4] = {ai[0], ai[1], ai[5], ai[6]};
+                TRY(globe_trust_region_step_no_time(theta, grad, ai2, Delta, p, &st));
+            }
             if (st != 0) {
                 d.log.printf("Step solver failed (status %d). Reducing trust region radius.\n", st);
                 Delta *= 0.75;
@@ -448,7 +562,7 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
             } else {
                 const double pred = dot5(grad, p) - 0.5 * quad5(ai, p);
                 d.log.printf("Predicted change in log-likelihood: %.17g\n", pred);
-                d.log.vec("Predicted step:", p, 5);
+                d.log.vec("Predicted step:", p, nc);
                 double scale = 1.0;
                 bool accepted = false, conv_here = false;
                 int red = 0;
@@ -459,13 +573,13 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
                         tn[k] = theta[k] + sp[k];
                     }
                     d.log.printf("Trying step with scale %.17g\n", scale);
-                    d.log.vec("theta_new:", tn, 5);
+                    d.log.vec("theta_new:", tn, nc);
                     bool violated = false;
-                    for (int k = 0; k < 5; ++k) {
+                    for (int k = 0; k < nc; ++k) {
                         if (k != 3 && tn[k] < 1e-6) { tn[k] = 1e-6; violated = true; }
                         if (tn[k] > 10.0) { tn[k] = 10.0; violated = true; }
                     }
-                    if (tn[3] > std::sqrt(tn[2] * tn[4])) {
+                    if (nc == 5 && tn[3] > std::sqrt(tn[2] * tn[4])) {
                         tn[3] = std::sqrt(tn[2] * tn[4]) - 1e-6;
                         violated = true;
                     }
@@ -523,8 +637,11 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
                 }
             }
         }
-        d.log.printf("Estimated variance components:  sig2e = %.17g, sig2g = %.17g, sig2b0 = %.17g, sigb01 = %.17g, "
-                     "sig2b1 = %.17g\n", theta[0], theta[1], theta[2], theta[3], theta[4]);
+        if (nc == 5)
+            d.log.printf("Estimated variance components:  sig2e = %.17g, sig2g = %.17g, sig2b0 = %.17g, "
+                         "sigb01 = %.17g, sig2b1 = %.17g\n", theta[0], theta[1], theta[2], theta[3], theta[4]);
+        else
+            d.log.printf("Estimated variance components:  sig2e = %.17g, sig2g = %.17g\n", theta[0], theta[1]);
         {
             double dif[5];
             for (int k = 0; k < 5; ++k) dif[k] = theta[k] - theta_old[k];
@@ -545,11 +662,13 @@ extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, cons
         }
     }
     {
-        double inv[25];
-        bool ok = inv5(ai, inv);
+        double inv[25], aii[25];
+        std::memcpy(aii, ai, sizeof(aii));
+        for (int k = nc; k < 5; ++k) aii[k * 5 + k] = 1.0;   // block-diagonal: the model's block inverts alone
+        bool ok = inv5(aii, inv);
         const char* nm[5] = {"   sig2e", "   sig2g", "  sig2b0", "  sigb01", "  sig2b1"};
         d.log.printf("Final variance components \xc2\xb1 SEs:\n");
-        for (int k = 0; k < 5; ++k) {
+        for (int k = 0; k < nc; ++k) {
             res->se[k] = ok ? std::sqrt(inv[k * 5 + k]) : NAN;
             d.log.printf("%s = %.17g \xc2\xb1 %.17g\n", nm[k], theta[k], res->se[k]);
         }

@@ -458,15 +458,34 @@ int globe_set_vc(globe_ctx* ctx, const double vc[5]) {
     for (int k = 0; k < 5; ++k)
         if (!std::isfinite(vc[k])) return set_err(ctx, GLOBE_ERR_ARG, "variance component %d is not finite", k);
     if (!(vc[0] > 0.0)) return set_err(ctx, GLOBE_ERR_ARG, "sig2e must be > 0 (got %g)", vc[0]);
+    double v[5];
+    std::memcpy(v, vc, sizeof(v));
+    if (ctx->model == GLOBE_MODEL_NO_TIME) v[2] = v[3] = v[4] = 0.0;   // no time effects
     bool same = ctx->vc_set;
-    for (int k = 0; k < 5; ++k) same = same && ctx->vc[k] == vc[k];
+    for (int k = 0; k < 5; ++k) same = same && ctx->vc[k] == v[k];
     if (same) return GLOBE_OK;
-    std::memcpy(ctx->vc, vc, sizeof(double) * 5);
+    std::memcpy(ctx->vc, v, sizeof(double) * 5);
     ctx->vc_set = true;
     ctx->precond_ok = false;
     ctx->mme_ok = ctx->fth_ok = false;
     return GLOBE_OK;
 }
+
+int globe_set_model(globe_ctx* ctx, int model) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (model != GLOBE_MODEL_FULL && model != GLOBE_MODEL_NO_TIME)
+        return set_err(ctx, GLOBE_ERR_ARG, "unknown model %d", model);
+    if (ctx->model == model) return GLOBE_OK;
+    ctx->model = model;
+    if (ctx->vc_set && model == GLOBE_MODEL_NO_TIME) {
+        ctx->vc[2] = ctx->vc[3] = ctx->vc[4] = 0.0;
+        ctx->precond_ok = false;
+    }
+    ctx->mme_ok = ctx->fth_ok = false;
+    return GLOBE_OK;
+}
+
+int globe_get_model(const globe_ctx* ctx) { return ctx ? ctx->model : GLOBE_MODEL_FULL; }
 
 int globe_set_precision(globe_ctx* ctx, int precision) {
     if (!ctx) return GLOBE_ERR_ARG;

@@ -1,4 +1,8 @@
-// runAIREML -- drop-in for the reference program of the same name
+// runAIREML -- drop-in for the reference program of the same name.  Built a
+// second time with GLOBE_NO_TIME defined, it is runAIREML_reducedModel
+// (varCompEst_reducedModel_noTime.cpp:93-129, :967-1106): no time effects,
+// components sig2e and sig2g (defaults 0.5, 0.5), record table of INDIV,
+// PHENO and covariates.
 // (varCompEst.cpp:103-133, :1347-1500): positional <input> <grm_prefix>
 // <output_prefix>, optional --maxiter --tol --numMC --sig2e --sig2g --sig2b0
 // --sigb01 --sig2b1 (unknown flags ignored, as in the reference), progress
@@ -22,6 +26,12 @@
 
 #include "globe.h"
 
+#ifdef GLOBE_NO_TIME
+constexpr int NVC = 2;
+#else
+constexpr int NVC = 5;
+#endif
+
 static int fail(const char* msg) {
     std::fprintf(stderr, "Error: %s\n", msg);
     return EXIT_FAILURE;
@@ -29,11 +39,18 @@ static int fail(const char* msg) {
 
 int main(int argc, char** argv) {
     if (argc < 4) {
+#ifdef GLOBE_NO_TIME
+        std::fprintf(stderr,
+                     "Usage: %s <input_filename> <grm_prefix> <output_prefix> [--maxiter <int>] [--tol <float>] "
+                     "[--numMC <int>] [--sig2e <float>] [--sig2g <float>]\n",
+                     argv[0]);
+#else
         std::fprintf(stderr,
                      "Usage: %s <input_filename> <grm_prefix> <output_prefix> [--maxiter: optional] [--tol: optional] "
                      "[--numMC: optional] [--sig2e: optional] [--sig2g: optional] [--sig2b0: optional] [--sigb01: "
                      "optional] [--sig2b1: optional]\n",
                      argv[0]);
+#endif
         return EXIT_FAILURE;
     }
     std::string input = argv[1], grm = argv[2], outp = argv[3], probes_file, geno;
@@ -41,8 +58,13 @@ int main(int argc, char** argv) {
     int fuse = 1;
     int maxiter = 50, numMC = 15, precision = GLOBE_PREC_FP64, device = 0;
     float tol = 1e-3f;
+#ifdef GLOBE_NO_TIME
+    // defaults of the reduced VarCompDataStruct (varCompEst_reducedModel_noTime.cpp:43-45)
+    float th[5] = {0.5f, 0.5f, 0.0f, 0.0f, 0.0f};
+#else
     // defaults of VarCompDataStruct (varCompEst.cpp:48-52), as float
     float th[5] = {0.5f, 0.3f, 0.2f, 0.1f, 0.1f};
+#endif
     const char* vcflag[5] = {"--sig2e", "--sig2g", "--sig2b0", "--sigb01", "--sig2b1"};
     double pcg_tol = 1e-5;
     unsigned long long seed = 12345;
@@ -66,13 +88,27 @@ int main(int argc, char** argv) {
         else if (a == "--minMAF" && has) min_maf = std::strtof(argv[++i], nullptr);
         else if (a == "--maxMissingRate" && has) max_miss = std::strtof(argv[++i], nullptr);
         else {
-            for (int q = 0; q < 5; ++q)
+            for (int q = 0; q < NVC; ++q)
                 if (a == vcflag[q] && has) th[q] = std::strtof(argv[++i], nullptr);
         }
     }
     char err[1024] = {0};
     int64_t Nrec = 0;
     int32_t N = 0, p = 0;
+#ifdef GLOBE_NO_TIME
+    // every column but INDIV and PHENO is a covariate; the last one stands in for time,
+    // which this model does not use (its time-effect components are zero)
+    if (globe_read_records_no_time(input.c_str(), &Nrec, &N, &p, nullptr, nullptr, nullptr, err, sizeof err))
+        return fail(err);
+    if (p < 1) return fail("the record table needs at least one covariate column (e.g. an intercept)");
+    std::vector<int32_t> indiv(Nrec);
+    std::vector<double> X((size_t)Nrec * p), y(Nrec);
+    if (globe_read_records_no_time(input.c_str(), &Nrec, &N, &p, indiv.data(), X.data(), y.data(), err, sizeof err))
+        return fail(err);
+    std::printf("Found N = %d indivuduals, \n      p = %d fixed effects, and\n      Nrec = %lld records in the "
+                "input file.\n", N, p, (long long)Nrec);
+    p -= 1;
+#else
     if (globe_read_records(input.c_str(), &Nrec, &N, &p, nullptr, nullptr, nullptr, err, sizeof err)) return fail(err);
     std::vector<int32_t> indiv(Nrec);
     std::vector<double> X((size_t)Nrec * (p + 1)), y(Nrec);
@@ -80,6 +116,7 @@ int main(int argc, char** argv) {
         return fail(err);
     std::printf("Found N = %d indivuduals, \n      p = %d fixed effects (in addition to TIME), and\n      Nrec = %lld "
                 "records in the input file.\n", N, p, (long long)Nrec);
+#endif
     std::vector<float> A;
     if (geno.empty()) {
         A.resize((size_t)N * (N + 1) / 2);
@@ -101,6 +138,9 @@ int main(int argc, char** argv) {
         globe_destroy(ctx);
         return EXIT_FAILURE;
     };
+#ifdef GLOBE_NO_TIME
+    if (globe_set_model(ctx, GLOBE_MODEL_NO_TIME)) return die("model");
+#endif
     if (globe_load_records(ctx, Nrec, N, p, indiv.data(), X.data(), y.data())) return die("records");
     if (geno.empty()) {
         if (globe_load_grm(ctx, A.data(), N)) return die("GRM");
@@ -133,7 +173,7 @@ int main(int argc, char** argv) {
     const char* nm[5] = {"   sig2e", "   sig2g", "  sig2b0", "  sigb01", "  sig2b1"};
     std::printf("Final variance components +- SEs (%d iterations%s):\n", r.iterations,
                 r.converged ? ", converged" : "");
-    for (int k = 0; k < 5; ++k) std::printf("%s = %.9g +- %.9g\n", nm[k], r.theta[k], r.se[k]);
+    for (int k = 0; k < NVC; ++k) std::printf("%s = %.9g +- %.9g\n", nm[k], r.theta[k], r.se[k]);
     globe_destroy(ctx);
     return 0;
 }

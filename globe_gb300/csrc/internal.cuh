@@ -107,6 +107,8 @@ struct globe_ctx {
     double vc[5] = {0, 0, 0, 0, 0};
     bool vc_set = false;
     int prec = GLOBE_PREC_FP64;   // precision of operator calls (globe_set_precision / PCG options)
+    int model = GLOBE_MODEL_FULL; // GLOBE_MODEL_NO_TIME: components (sig2e, sig2g) only
+    int nvc() const { return model == GLOBE_MODEL_NO_TIME ? 2 : 5; }
     bool precond_ok = false;      // H built for the current vc
     globe::Slot ws[globe::WS_COUNT];
     // MME state (V^-1 X, (X'V^-1X)^-1, V^-1 r, uhat) kept for AIREML terms

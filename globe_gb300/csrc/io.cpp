@@ -66,8 +66,11 @@ bool blank(const std::string& s) {
 
 }  // namespace
 
-extern "C" int globe_read_records(const char* path, int64_t* Nrec_out, int32_t* N_out, int32_t* p_out,
-                                  int32_t* indiv, double* X, double* y, char* err, int errlen) {
+// no_time: INDIV and PHENO are required and every other column, in file order, is
+// a covariate (the reduced model's readInputData, varCompEst_reducedModel_noTime.cpp:191-247);
+// otherwise TIMES is required too and becomes the last column of X.
+static int read_records(const char* path, bool no_time, int64_t* Nrec_out, int32_t* N_out, int32_t* p_out,
+                        int32_t* indiv, double* X, double* y, char* err, int errlen) {
     if (!path || !Nrec_out || !N_out || !p_out) return GLOBE_ERR_ARG;
     FILE* f = std::fopen(path, "r");
     if (!f) {
@@ -88,13 +91,15 @@ extern "C" int globe_read_records(const char* path, int64_t* Nrec_out, int32_t* 
         else if (tok[c] == "PHENO") cp = c;
         else if (tok[c] == "TIMES") ct = c;
     }
-    if (ci < 0 || cp < 0 || ct < 0) {
+    if (no_time) ct = -1;   // a TIMES column, if any, is an ordinary covariate
+    if (ci < 0 || cp < 0 || (!no_time && ct < 0)) {
         std::fclose(f);
-        put_err(err, errlen, "Missing required columns in header (INDIV, PHENO, TIMES).");
+        put_err(err, errlen, no_time ? "Missing required columns in header (INDIV, PHENO)."
+                                     : "Missing required columns in header (INDIV, PHENO, TIMES).");
         return GLOBE_ERR_FORMAT;
     }
     const int ncol = (int)tok.size();
-    const int p = ncol - 3;
+    const int p = ncol - (no_time ? 2 : 3);
     std::vector<int> covpos(ncol, -1);
     for (int c = 0, q = 0; c < ncol; ++c)
         if (c != ci && c != cp && c != ct) covpos[c] = q++;
@@ -146,7 +151,7 @@ extern "C" int globe_read_records(const char* path, int64_t* Nrec_out, int32_t* 
             }
             raw_ids.push_back(id);
             y[row] = vals[cp];
-            X[(size_t)p * cap + row] = vals[ct];
+            if (ct >= 0) X[(size_t)p * cap + row] = vals[ct];
             for (int c = 0; c < ncol; ++c)
                 if (covpos[c] >= 0) X[(size_t)covpos[c] * cap + row] = vals[c];
         }
@@ -179,6 +184,16 @@ extern "C" int globe_read_records(const char* path, int64_t* Nrec_out, int32_t* 
     *N_out = N;
     *p_out = p;
     return GLOBE_OK;
+}
+
+extern "C" int globe_read_records(const char* path, int64_t* Nrec_out, int32_t* N_out, int32_t* p_out,
+                                  int32_t* indiv, double* X, double* y, char* err, int errlen) {
+    return read_records(path, false, Nrec_out, N_out, p_out, indiv, X, y, err, errlen);
+}
+
+extern "C" int globe_read_records_no_time(const char* path, int64_t* Nrec_out, int32_t* N_out, int32_t* p_out,
+                                          int32_t* indiv, double* X, double* y, char* err, int errlen) {
+    return read_records(path, true, Nrec_out, N_out, p_out, indiv, X, y, err, errlen);
 }
 
 static int save_vec(const char* path, const void* payload, int32_t n, size_t esz) {

@@ -803,12 +803,26 @@ __device__ double stream_normal(uint64_t seed, uint64_t idx) {
 
 __global__ void k_probes(int64_t n, int32_t N, const int32_t* __restrict__ rind, const double* __restrict__ t,
                          double sg, double se, double L00, double L10, double L11,
-                         const double* __restrict__ draws, uint64_t seed, int numMC, double* __restrict__ Y) {
+                         const double* __restrict__ draws, uint64_t seed, int numMC, int no_time,
+                         double* __restrict__ Y) {
     const int j = blockIdx.y;
-    const size_t per = 3 * (size_t)N + n;
+    const size_t per = (no_time ? 1 : 3) * (size_t)N + n;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         const int i = rind[r];
         double z1, z2a, z2b, z3;
+        if (no_time) {   // Y = sqrt(sig2g) Z1 + sqrt(sig2e) Z3 (varCompEst_reducedModel_noTime.cpp:563-577)
+            if (draws) {
+                const double* d = draws + (size_t)j * per;
+                z1 = d[i];
+                z3 = d[(size_t)N + r];
+            } else {
+                const uint64_t base = (uint64_t)j * per;
+                z1 = stream_normal(seed, base + i);
+                z3 = stream_normal(seed, base + (uint64_t)N + r);
+            }
+            Y[r + (size_t)j * n] = sg * z1 + se * z3;
+            continue;
+        }
         if (draws) {
             const double* d = draws + (size_t)j * per;
             z1 = d[i];
@@ -830,15 +844,20 @@ __global__ void k_probes(int64_t n, int32_t N, const int32_t* __restrict__ rind,
 int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen, double* Y) {
     auto& c = ctx->coh;
     const double* v = ctx->vc;
-    // compute_chol_2x2 (varCompEst.cpp:800-813)
-    double L00 = sqrt(v[2]), L10 = v[3] / L00;
-    double d11 = v[4] - v[3] * v[3] / v[2];
-    if (d11 < 0) d11 = 0;
-    double L11 = sqrt(d11);
+    // compute_chol_2x2 (varCompEst.cpp:800-813); unused without time effects
+    const int no_time = ctx->model == GLOBE_MODEL_NO_TIME ? 1 : 0;
+    double L00 = 0, L10 = 0, L11 = 0;
+    if (!no_time) {
+        L00 = sqrt(v[2]);
+        L10 = v[3] / L00;
+        double d11 = v[4] - v[3] * v[3] / v[2];
+        if (d11 < 0) d11 = 0;
+        L11 = sqrt(d11);
+    }
     int nb = div_up(c.Nrec, 256);
     if (nb > 1216) nb = 1216;
     k_probes<<<dim3(nb, numMC), 256, 0, ctx->stream>>>(c.Nrec, c.N, c.rind, c.times(), sqrt(v[1]), sqrt(v[0]),
-                                                       L00, L10, L11, gen ? nullptr : draws, seed, numMC, Y);
+                                                       L00, L10, L11, gen ? nullptr : draws, seed, numMC, no_time, Y);
     GLOBE_LAUNCHED(ctx, "k_probes");
     return GLOBE_OK;
 }

@@ -472,8 +472,9 @@ static int mme_impl(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, do
 
 static int grad_check(globe_ctx* ctx, int numMC) {
     if (numMC < 1) return set_err(ctx, GLOBE_ERR_ARG, "numMC must be >= 1");
-    if (!(ctx->vc[1] > 0.0) || !(ctx->vc[2] > 0.0))
-        return set_err(ctx, GLOBE_ERR_ARG, "AIREML needs sig2g > 0 and sig2b0 > 0");
+    if (!(ctx->vc[1] > 0.0)) return set_err(ctx, GLOBE_ERR_ARG, "AIREML needs sig2g > 0");
+    if (ctx->model == GLOBE_MODEL_FULL && !(ctx->vc[2] > 0.0))
+        return set_err(ctx, GLOBE_ERR_ARG, "AIREML needs sig2b0 > 0 (the time effects' probe Cholesky factor)");
     return GLOBE_OK;
 }
 
@@ -493,7 +494,7 @@ static int grad_probes(globe_ctx* ctx, const double* probes, int numMC, uint64_t
     GLOBE_RET(ws(ctx, WS_HSTAR, (size_t)N * 4, &pb.Hs));
     if (probes) {
         double* dd;
-        size_t cnt = (size_t)numMC * (3 * (size_t)N + n);
+        size_t cnt = (size_t)numMC * ((ctx->model == GLOBE_MODEL_NO_TIME ? 1 : 3) * (size_t)N + n);
         GLOBE_RET(ws(ctx, WS_PROBE, cnt, &dd));
         GLOBE_CK(ctx, cudaMemcpyAsync(dd, probes, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->stream));
         GLOBE_RET(probes_build(ctx, dd, numMC, seed, false, pb.Y));
@@ -532,11 +533,13 @@ static int grad_finish(globe_ctx* ctx, int numMC, const double* VY, const ProbeB
     std::vector<double> tt((size_t)numMC * 5);
     GLOBE_RET(d2h(ctx, tt.data(), small, tt.size()));
     double h_trace[5], h_grad[5];
+    const int nc = ctx->nvc();
     for (int q = 0; q < 5; ++q) {
         double a = 0;
         for (int j = 0; j < numMC; ++j) a += tt[(size_t)j * 5 + q];
         h_trace[q] = a / numMC;
         h_grad[q] = 0.5 * (h_first[q] - h_trace[q]);  // varCompEst.cpp:1006-1010
+        if (q >= nc) h_first[q] = h_trace[q] = h_grad[q] = 0.0;   // no such component in this model
     }
     if (first) std::memcpy(first, h_first, sizeof(h_first));
     if (trace) std::memcpy(trace, h_trace, sizeof(h_trace));
@@ -659,19 +662,22 @@ int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai, glob
     GLOBE_RET(check_ready(ctx));
     if (!ctx->fth_ok) return set_err(ctx, GLOBE_ERR_STATE, "call globe_aireml_grad first");
     const int64_t n = ctx->coh.Nrec;
+    const int nc = ctx->nvc();   // f_theta columns of this model
     double *Vf, *Pf, *small;
-    GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * 5, &Vf));
-    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * 5, &Pf));
+    GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * nc, &Vf));
+    GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * nc, &Pf));
     globe_pcg_opts o = *opts;
     o.rule = GLOBE_RULE_AIREML;
     o.x0mode = GLOBE_X0_PRECOND;
-    GLOBE_RET(pcg_dev(ctx, ctx->f_theta, Vf, 5, &o, info));
-    GLOBE_RET(project_dev(ctx, Vf, 5, Pf));
+    GLOBE_RET(pcg_dev(ctx, ctx->f_theta, Vf, nc, &o, info));
+    GLOBE_RET(project_dev(ctx, Vf, nc, Pf));
     GLOBE_RET(ws(ctx, WS_SMALL, 64, &small));
-    GLOBE_RET(xt_mat(ctx, ctx->f_theta, 5, Pf, 5, small));
+    GLOBE_RET(xt_mat(ctx, ctx->f_theta, nc, Pf, nc, small));
     double h[25];
-    GLOBE_RET(d2h(ctx, h, small, 25));
-    for (int e = 0; e < 25; ++e) ai[e] = 0.5 * h[e];  // varCompEst.cpp:1038
+    GLOBE_RET(d2h(ctx, h, small, (size_t)nc * nc));
+    for (int e = 0; e < 25; ++e) ai[e] = 0.0;
+    for (int c = 0; c < nc; ++c)
+        for (int r = 0; r < nc; ++r) ai[c * 5 + r] = 0.5 * h[c * nc + r];  // varCompEst.cpp:1038
     return GLOBE_OK;
 }
 

@@ -47,6 +47,11 @@ extern "C" {
                                matches FP64 to ~1e-13); dense GRM in double-float FP32
                                arithmetic (~48 bits) */
 
+/* models (globe_set_model) */
+#define GLOBE_MODEL_FULL 0     /* random intercept and slope per individual (runAIREML) */
+#define GLOBE_MODEL_NO_TIME 1  /* no time effects: V = sig2g J A J' + sig2e I, components
+                                  (sig2e, sig2g) (runAIREML_reducedModel) */
+
 /* PCG stopping rules */
 #define GLOBE_RULE_PCGSOLVER 0 /* max_j |r_j|/|b_j| < tol, or 10 iterations with
                                   < 0.5% improvement (PCGsolver.cpp:1381-1415) */
@@ -152,6 +157,16 @@ int globe_load_grm(globe_ctx* ctx, const float* grm_lt, int32_t N);
  * > 0 (the block preconditioner is singular otherwise). */
 int globe_set_vc(globe_ctx* ctx, const double vc[5]);
 
+/* Model of the variance components (GLOBE_MODEL_FULL by default).  Under
+ * GLOBE_MODEL_NO_TIME -- varCompEst_reducedModel_noTime.cpp, the reference's
+ * runAIREML_reducedModel -- the time effects are absent: globe_set_vc keeps
+ * vc[0..1] and sets vc[2..4] = 0, the AIREML probes are Y = sqrt(sig2g) J Z1 +
+ * sqrt(sig2e) Z3 (Z1 over individuals, Z3 over records, in that order per
+ * probe; :563-577), and globe_aireml_grad / _eval / _ai fill components 0..1
+ * only (the AI matrix in the top-left 2x2 of its 5x5 array). */
+int globe_set_model(globe_ctx* ctx, int model);
+int globe_get_model(const globe_ctx* ctx);
+
 /* Precision of the operator calls below (globe_grm_apply, globe_vx):
  * GLOBE_PREC_FP64 (default) or GLOBE_PREC_MIXED (genotype GRM on the FP8
  * tensor cores with exact digit slicing; see globe_pcg_opts.precision).
@@ -247,6 +262,12 @@ int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai,
  * 2 not converged. */
 int globe_trust_region_step(const double theta[5], const double grad[5], const double ai[25],
                             double delta, double p[5], int* status);
+/* Step of the reduced model (oneIter_AIREML, varCompEst_reducedModel_noTime.cpp:782-830):
+ * maximise g'p - p'Ap/2 over 2 components s.t. |p_k| <= 10,
+ * A_00 p_0 + A_11 p_1 <= delta, theta_k + p_k >= 1e-5; ai is 2x2 column-major.
+ * Solved exactly by enumerating active sets.  status: 0 solved, 1 infeasible. */
+int globe_trust_region_step_no_time(const double theta[2], const double grad[2], const double ai[4], double delta,
+                                    double p[2], int* status);
 
 typedef struct {
     int maxiter;       /* --maxiter (varCompEst.cpp:21, default 50) */
@@ -288,6 +309,13 @@ int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* opts, const char* 
  * (0-based), X (Nrec x (p+1), time last) and y. */
 int globe_read_records(const char* path, int64_t* Nrec, int32_t* N, int32_t* p, int32_t* indiv,
                        double* X, double* y, char* err, int errlen);
+/* Record table of the model without time effects (readInputData,
+ * varCompEst_reducedModel_noTime.cpp:191-247): INDIV and PHENO by name, every
+ * other column in file order a covariate; p = number of covariates and X is
+ * Nrec x p.  To load it, pass p - 1 to globe_load_records (its last covariate
+ * then takes the place of time, which the model does not use). */
+int globe_read_records_no_time(const char* path, int64_t* Nrec, int32_t* N, int32_t* p, int32_t* indiv,
+                               double* X, double* y, char* err, int errlen);
 /* saveVector (utils.cpp:18-34): int32 length + float32 payload. */
 int globe_save_vector_f32(const char* path, const double* v, int32_t n);
 /* Same layout with a float64 payload (what the float->double build of the

@@ -29,6 +29,9 @@ Variants:
   printing.  Links the bundled NLopt, which is an x86-64 binary: this
   variant is skipped on other hosts.
 * ``runAIREML``           -- FP32 as shipped (x86-64 only, bundled NLopt).
+* ``runAIREML_reduced64`` -- FP64 ``src/varCompEst_reducedModel_noTime.cpp``
+  (the reference's ``runAIREML_reducedModel``) with the same three patches as
+  ``runAIREML64`` (x86-64 only, bundled NLopt).
 """
 import os
 import platform
@@ -124,6 +127,40 @@ def _patch_aireml64(src):
     return s
 
 
+def _patch_reduced64(src):
+    """The reduced model (no time effects) with runAIREML64's patches: probes from
+    GLOBE_PROBE_FILE, PCG tolerance GLOBE_REF_TOL, 17-digit printing."""
+    s = _fp64(src)
+    s = _grm_read_f32(s, "file.read(reinterpret_cast<char*>(CohortData.A_vecLT.data()), nTri * sizeof(double));",
+                      "CohortData.A_vecLT", "nTri")
+    pat = re.compile(r"VecT generate_standard_normal\(int dimension\) \{.*?\n\}", re.S)
+    body = (
+        "static FILE* g_probe_fp = nullptr;\n"
+        "VecT generate_standard_normal(int dimension) {\n"
+        "    if (!g_probe_fp) {\n"
+        "        const char* fn = std::getenv(\"GLOBE_PROBE_FILE\");\n"
+        "        if (!fn || !(g_probe_fp = std::fopen(fn, \"rb\"))) {\n"
+        "            std::fprintf(stderr, \"GLOBE_PROBE_FILE missing\\n\"); std::exit(3); }\n"
+        "    }\n"
+        "    VecT z(dimension);\n"
+        "    if (std::fread(z.data(), sizeof(double), dimension, g_probe_fp) != (size_t)dimension) {\n"
+        "        std::fprintf(stderr, \"probe file exhausted\\n\"); std::exit(4); }\n"
+        "    return z;\n"
+        "}")
+    s, n = pat.subn(lambda m: body, s)
+    assert n == 1, "generate_standard_normal not found"
+    s = s.replace("double tol = 1e-5;", "double tol = GLOBE_REF_TOL;")
+    s = s.replace("Yvs, Vinv_Yvs, 1e-5, 1000, true, false", "Yvs, Vinv_Yvs, GLOBE_REF_TOL, 1000, true, false")
+    s = s.replace("f_theta, Vinv_f_theta, 1e-5, 1000, false, true",
+                  "f_theta, Vinv_f_theta, GLOBE_REF_TOL, 1000, false, true")
+    assert s.count("GLOBE_REF_TOL") == 3, s.count("GLOBE_REF_TOL")
+    anchor = "std::cout.rdbuf(&tee_streambuf);"
+    assert anchor in s
+    s = s.replace(anchor, anchor + "\n    std::cout << std::setprecision(17);")
+    s = "#include <iomanip>\n#include <cstdio>\n#ifndef GLOBE_REF_TOL\n#define GLOBE_REF_TOL 1e-12\n#endif\n" + s
+    return s
+
+
 def _compile(args):
     name, srcs, extra = args
     out = os.path.join(OUT, name)
@@ -147,6 +184,7 @@ def main():
     src = os.path.join(REF, "src")
     pcg = _read(os.path.join(src, "PCGsolver.cpp"))
     vce = _read(os.path.join(src, "varCompEst.cpp"))
+    red = _read(os.path.join(src, "varCompEst_reducedModel_noTime.cpp"))
     utc = _read(os.path.join(src, "utils.cpp"))
     uth = _read(os.path.join(src, "utils.hpp"))
     # FP32 stats variant
@@ -156,6 +194,7 @@ def main():
     _write(os.path.join(TMP, "f64", "utils.cpp"), _fp64(utc))
     _write(os.path.join(TMP, "f64", "PCGsolver.cpp"), _patch_pcg64(pcg))
     _write(os.path.join(TMP, "f64", "varCompEst.cpp"), _patch_aireml64(vce))
+    _write(os.path.join(TMP, "f64", "varCompEst_reduced.cpp"), _patch_reduced64(red))
     jobs = [
         ("runPCGsolver", [os.path.join(src, "PCGsolver.cpp"), os.path.join(src, "utils.cpp")], ["-I", src]),
         ("runPCGsolver_stats", [os.path.join(TMP, "f32s", "PCGsolver.cpp"), os.path.join(src, "utils.cpp")],
@@ -172,6 +211,9 @@ def main():
                      ["-I", os.path.join(TMP, "f64")] + nlf))
         jobs.append(("runAIREML", [os.path.join(src, "varCompEst.cpp"), os.path.join(src, "utils.cpp")],
                      ["-I", src] + nlf))
+        jobs.append(("runAIREML_reduced64", [os.path.join(TMP, "f64", "varCompEst_reduced.cpp"),
+                                             os.path.join(TMP, "f64", "utils.cpp")],
+                     ["-I", os.path.join(TMP, "f64")] + nlf))
     with ThreadPoolExecutor(len(jobs)) as ex:
         for n in ex.map(_compile, jobs):
             print("built", os.path.join(OUT, n))

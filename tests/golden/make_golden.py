@@ -15,6 +15,9 @@ seeds; the reference programs' outputs are stored next to them:
 * ``aireml_small_ref.json`` -- runAIREML (float->double build, PCG tol 1e-12,
   probe draws injected from globe_gb300.synth.normal_stream(PROBE_SEED)):
   per-iteration gradients, AI matrices, steps, rho, accepted components.
+* ``reduced_small.{txt,grm.bin}`` + ``reduced_small_ref.json`` -- the same for
+  runAIREML_reducedModel (no time effects, components sig2e and sig2g; one
+  record per individual; record table INDIV PHENO COV0 COV1 COV2).
 """
 import json
 import os
@@ -82,22 +85,25 @@ def _floats(s):
     return [float(x) for x in s.split()]
 
 
-def parse_aireml_log(text):
-    """Per-iteration blocks of the reference log (17-digit prints)."""
+def parse_aireml_log(text, nc=5):
+    """Per-iteration blocks of the reference log (17-digit prints); nc components."""
     its = []
     for blk in re.split(r"\n-+ Iteration \d+ -+\n", text)[1:]:
         d = {"gradients": [_floats(m) for m in re.findall(r"Gradient:\s*([^\n]+)", blk)],
              "ai": [[_floats(l) for l in m.strip().split("\n")] for m in
-                    re.findall(r"AI matrix: \n((?:[^\n]+\n){5})", blk)],
+                    re.findall(r"AI matrix: \n((?:[^\n]+\n){%d})" % nc, blk)],
              "steps": [_floats(m) for m in re.findall(r"Predicted step:\s*([^\n]+)", blk)],
              "nlopt": [int(m) for m in re.findall(r"NLopt result: (-?\d+)", blk)],
              "rho": [float(m) for m in re.findall(r"Rho: ([^\n]+)", blk)],
              "theta_new": [_floats(m) for m in re.findall(r"theta_new: ([^\n]+)", blk)]}
-        m = re.search(r"Estimated variance components:\s*sig2e = ([^,]+), sig2g = ([^,]+), sig2b0 = ([^,]+), "
-                      r"sigb01 = ([^,]+), sig2b1 = ([^\n]+)", blk)
-        d["theta"] = [float(m.group(k)) for k in range(1, 6)] if m else None
+        if nc == 5:
+            m = re.search(r"Estimated variance components:\s*sig2e = ([^,]+), sig2g = ([^,]+), sig2b0 = ([^,]+), "
+                          r"sigb01 = ([^,]+), sig2b1 = ([^\n]+)", blk)
+        else:
+            m = re.search(r"Estimated variance components:\s*sig2e = ([^,]+), sig2g = ([^\n]+)", blk)
+        d["theta"] = [float(m.group(k)) for k in range(1, nc + 1)] if m else None
         its.append(d)
-    fin = re.search(r"Final variance components[^\n]*\n((?:[^\n]+\n){5})", text)
+    fin = re.search(r"Final variance components[^\n]*\n((?:[^\n]+\n){%d})" % nc, text)
     final = []
     if fin:
         for ln in fin.group(1).strip().split("\n"):
@@ -130,6 +136,42 @@ def make_aireml_case(tmp):
     print(name, "N=%d Nrec=%d iterations=%d" % (coh["N"], coh["Nrec"], len(its)))
 
 
+def make_reduced_case(tmp):
+    """runAIREML_reducedModel: y = X b + g + e, V = sig2g A + sig2e I, one record per individual."""
+    name = "reduced_small"
+    rng = np.random.default_rng(31)
+    N, M = 300, 1500
+    G = synth.simulate_genotypes(rng, M, N, 0.01, 0.5, 0.0)
+    packed = synth.pack_genotypes(G)
+    Gf = np.where(G < 0, 0, G).astype(np.float64)
+    f = np.clip(Gf.mean(axis=1) / 2.0, 1e-3, 1 - 1e-3)
+    Zs = (Gf - 2 * f[:, None]) / np.sqrt(2 * f * (1 - f))[:, None]
+    s2e, s2g = 0.6, 0.4
+    u = Zs.T @ rng.standard_normal(M) * np.sqrt(s2g / M)
+    X = np.column_stack([np.ones(N)] + [np.round(rng.standard_normal(N) * 1024) / 1024 for _ in range(2)])
+    y = X @ np.array([1.0, 0.5, -0.3]) + u + rng.standard_normal(N) * np.sqrt(s2e)
+    y = np.round(y * 4096) / 4096
+    pre = os.path.join(HERE, name)
+    with open(pre + ".txt", "w") as fh:
+        fh.write("INDIV PHENO COV0 COV1 COV2\n")
+        for i in range(N):
+            fh.write("%d %.10g %.10g %.10g %.10g\n" % (i + 1, y[i], X[i, 0], X[i, 1], X[i, 2]))
+    synth.write_grm_bin(pre, synth.grm_from_packed(packed, N))
+    per = AIREML_NUMMC * 2 * N
+    probe_file = os.path.join(tmp, "probes_reduced.bin")
+    synth.normal_stream(PROBE_SEED, per * 200).tofile(probe_file)
+    env = dict(os.environ, GLOBE_PROBE_FILE=probe_file)
+    out = os.path.join(tmp, name)
+    subprocess.run([os.path.join(REF, "runAIREML_reduced64"), pre + ".txt", pre, out, "--numMC", str(AIREML_NUMMC),
+                    "--maxiter", str(AIREML_MAXITER)], env=env, capture_output=True, text=True, check=True)
+    text = open(out + ".log", encoding="utf-8", errors="replace").read()
+    its, final = parse_aireml_log(text, nc=2)
+    with open(os.path.join(HERE, name + "_ref.json"), "w") as fh:
+        json.dump({"numMC": AIREML_NUMMC, "maxiter": AIREML_MAXITER, "probe_seed": PROBE_SEED,
+                   "pcg_tol": 1e-12, "theta0": [0.5, 0.5], "N": N, "iterations": its, "final": final}, fh, indent=1)
+    print(name, "N=%d iterations=%d" % (N, len(its)))
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "runPCGsolver64")):
         sys.exit("build the reference first: python oracle/build_ref.py")
@@ -139,6 +181,8 @@ def main():
         make_pcg_case(name, *args, tmp)
     if os.path.exists(os.path.join(REF, "runAIREML64")):
         make_aireml_case(tmp)
+    if os.path.exists(os.path.join(REF, "runAIREML_reduced64")):
+        make_reduced_case(tmp)
 
 
 if __name__ == "__main__":
