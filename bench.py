@@ -162,29 +162,76 @@ def genetic_values(torch, raw, M, N, s2g, seed, chunk=2048):
     return (u * np.sqrt(s2g / max(kept, 1))).cpu().numpy()
 
 
-def dense_grm(torch, raw, M, N, chunk=2048):
-    """A = Zs'Zs / M_kept (float32 packed lower triangle, row-major with the diagonal: the
-    .grm.bin payload) from packed genotypes on the GPU, standardised as genetic_values does."""
+GRM_BUILD = dict(N=20_000, M=50_000, maf_lo=0.01, maf_hi=0.5, miss=0.02)
+GRM_KG, GRM_NMMA = 21, 192          # columns per tensor-core group and its MMA width (k_grm_build.cu)
+
+
+def grm_build_bench(G, torch, hbm, bf16, peak_src, raw=None, cfg=GRM_BUILD, fp64=True, device=0):
+    """globe_grm_build_dev (A = Zs'Zs / M_kept, float32 packed lower triangle) on the
+    dense-GRM shape: tensor-core and FP64 builds, their agreement, and the tensor-core
+    GEMM's issued FP8 rate.  Returns (record, lower triangle on the device)."""
+    N, M = cfg["N"], cfg["M"]
     bps = (N + 3) // 4
-    lut = torch.tensor([2.0, 0.0, 1.0, 0.0], device="cuda")
-    A = torch.zeros((N, N), dtype=torch.float32, device="cuda")
-    kept = 0
-    for s0 in range(0, M, chunk):
-        b = raw[s0:s0 + chunk, :bps]
-        codes = torch.stack([(b >> (2 * j)) & 3 for j in range(4)], dim=2).reshape(b.shape[0], bps * 4)[:, :N].long()
-        g = lut[codes]
-        nobs = (codes != 1).sum(1).clamp(min=1).float()
-        f = g.sum(1) / (2.0 * nobs)
-        keep = (f >= 0.01) & (f <= 0.99) & ((1.0 - nobs / N) <= 0.2)
-        z = ((g - 2.0 * f[:, None]) / torch.sqrt(2.0 * f * (1.0 - f)).clamp(min=1e-6)[:, None])[keep]
-        A.addmm_(z.t(), z)
-        kept += int(keep.sum())
-    A /= max(kept, 1)
-    r, c = torch.tril_indices(N, N, device="cuda")
-    lt = A[r, c].cpu().numpy()
-    del A, r, c
-    torch.cuda.empty_cache()
-    return lt, kept
+    stride = (bps + 15) // 16 * 16
+    cx = G.Context(device)
+    cx.set_individuals(N)
+    own = raw is None
+    if own:
+        raw = torch.empty((M, stride), dtype=torch.uint8, device="cuda")
+        cx.synth_bed_dev(raw.data_ptr(), M, N, stride, SEED + 11, cfg["maf_lo"], cfg["maf_hi"], cfg["miss"])
+    Mk = cx.load_bed_dev(raw.data_ptr(), M, stride)
+    if own:
+        del raw
+    lt = torch.empty(N * (N + 1) // 2, dtype=torch.float32, device="cuda")
+    rec = {"workload": "N=%d indiv, M=%d SNPs (%d kept) -> %.0f MB float32 packed lower triangle" % (
+        N, M, Mk, N * (N + 1) / 2 * 4 / 1e6), "kept_snps": int(Mk)}
+    cx.set_precision(G.PREC_MIXED)
+    t0 = time.perf_counter()
+    cx.grm_build_dev(lt.data_ptr())       # first call also lays out the individual-major tile-blocked codes
+    cx.synchronize()
+    rec["mixed_first_call_seconds"] = time.perf_counter() - t0
+    reps = 3
+    cx.prof_enable(True)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cx.grm_build_dev(lt.data_ptr())
+    cx.synchronize()
+    rec["mixed_seconds"] = (time.perf_counter() - t0) / reps
+    nb, msb = cx.prof_query(G._lib.PROF_GRM_BUILD)
+    ng, msg = cx.prof_query(G._lib.PROF_GRM_BUILD_GEMM)
+    cx.prof_enable(False)
+    rec["mixed_device_ms"] = msb / max(nb, 1)
+    rec["gemm_share"] = msg / msb if msb else None
+    # issued FP8 work: per group of 21 columns, the row tiles (256 rows) from its first column down,
+    # 192 digit columns, K = the padded SNP count
+    kpad = -(-((Mk + 3) // 4) // 32) * 32 * 4
+    rows = sum(-(-(N - (j0 // 256) * 256) // 256) * 256 for j0 in range(0, N, GRM_KG))
+    issued = 2.0 * rows * GRM_NMMA * kpad
+    t_gemm = msg / 1000.0 / reps
+    fp8_peak = 2.0 * bf16
+    rec["tensor"] = {"kernel": "k_tc_gemm<192> (e4m3 x e4m3 -> f32, 9 digits per column)",
+                     "issued_tflops": issued / t_gemm / 1e12, "peak_tflops": fp8_peak,
+                     "frac": issued / t_gemm / 1e12 / fp8_peak,
+                     "peak_source": "%s bf16 burst x 2 (FP8 dense rate)" % peak_src,
+                     "useful_tflops": 2.0 * N * (N + 1) / 2 * Mk / (rec["mixed_device_ms"] / 1000.0) / 1e12}
+    if fp64:
+        ref = lt.clone()
+        cx.set_precision(G.PREC_FP64)
+        t0 = time.perf_counter()
+        cx.grm_build_dev(lt.data_ptr())
+        cx.synchronize()
+        rec["fp64_seconds"] = time.perf_counter() - t0
+        rec["speedup"] = rec["fp64_seconds"] / rec["mixed_seconds"]
+        a = ref.view(torch.int32).to(torch.int64)
+        b = lt.view(torch.int32).to(torch.int64)
+        a = torch.where(a < 0, -(a & 0x7FFFFFFF), a)
+        b = torch.where(b < 0, -(b & 0x7FFFFFFF), b)
+        d = (a - b).abs()
+        rec["mixed_vs_fp64_max_ulp"] = int(d.max())
+        rec["mixed_vs_fp64_equal_fraction"] = float((d == 0).double().mean())
+        lt = ref
+    cx.close()
+    return rec, lt
 
 
 def cpu_reference_vx(indiv, X, packed_rows, maf_rows, N, k, rng):
@@ -317,10 +364,15 @@ def run_ours(args, cfg):
     y = y + genetic_values(torch, raw, M, N, VC[1], SEED + 1)[indiv]     # genotype-linked genetic term
     ctx.load_records(indiv, X, y, N)
     dense = bool(cfg.get("dense"))
+    grm_rec = None
     if dense:
-        grm_lt, Mk = dense_grm(torch, raw, M, N)
-        ctx.load_grm(grm_lt, N)
-        del grm_lt
+        # the dense input built on the GPU by globe_grm_build from the same genotypes
+        hbm0, bf160, src0 = load_peaks()
+        grm_rec, lt = grm_build_bench(G, torch, hbm0, bf160, src0, raw=raw, cfg=cfg, fp64=not args.no_fp64,
+                                      device=device)
+        Mk = grm_rec["kept_snps"]
+        ctx.load_grm(lt.cpu().numpy(), N)
+        del lt
         sample_rows = None
     else:
         Mk = ctx.load_bed_dev(raw.data_ptr(), M, stride)
@@ -472,6 +524,10 @@ def run_ours(args, cfg):
         line["aireml"] = aireml
     if rank == 0 and world == 1 and not args.no_aireml and prec != G.PREC_FP64 and not dense:
         line["aireml_mixed_vs_fp64"] = aireml_compare(G)
+    if grm_rec is None and rank == 0 and world == 1 and not args.no_grm_build and prec != G.PREC_FP64:
+        grm_rec, _ = grm_build_bench(G, torch, hbm, bf16, peak_src, fp64=not args.no_fp64)
+    if grm_rec is not None:
+        line["grm_build"] = grm_rec
     if rank == 0 and not args.no_cpu_baseline and not dense:
         from oracle import oracle
         alt, miss, maf, _, keep = oracle.bed_stats(sample_rows, N)
@@ -497,6 +553,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the in-run FP64-plain comparison")
     ap.add_argument("--no-aireml", action="store_true", help="skip the AIREML time-to-converge runs")
+    ap.add_argument("--no-grm-build", action="store_true", help="skip the GRM build (N=20k, M=50k) measurement")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     if args.iters <= 0:

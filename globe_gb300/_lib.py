@@ -18,6 +18,7 @@ RULE_PCGSOLVER, RULE_AIREML = 0, 1
 MODEL_FULL, MODEL_NO_TIME = 0, 1
 X0_ZERO, X0_PRECOND, X0_GIVEN = 0, 1, 2
 PROF_GRM, PROF_GRM_PASS1, PROF_GRM_PASS2, PROF_PCG_ITER = 0, 1, 2, 3
+PROF_GRM_BUILD, PROF_GRM_BUILD_GEMM = 4, 5
 
 
 class PcgOpts(C.Structure):
@@ -72,6 +73,10 @@ SIGNATURES = {
     "globe_load_bed_file": (C.c_int, [_vp, C.c_char_p, C.c_float, C.c_float, C.c_int64, _i64p, _i64p, _fp, _fp,
                                       _u8p, C.POINTER(BedInfo)]),
     "globe_load_grm": (C.c_int, [_vp, _fp, C.c_int32]),
+    "globe_set_individuals": (C.c_int, [_vp, C.c_int32]),
+    "globe_grm_build": (C.c_int, [_vp, _fp]),
+    "globe_grm_build_dev": (C.c_int, [_vp, _vp]),
+    "globe_write_grm": (C.c_int, [C.c_char_p, _fp, C.c_int32, C.c_char_p, C.c_int]),
     "globe_set_vc": (C.c_int, [_vp, _dp]),
     "globe_grm_apply": (C.c_int, [_vp, _dp, _dp, C.c_int]),
     "globe_grm_apply_dev": (C.c_int, [_vp, _vp, _vp, C.c_int]),

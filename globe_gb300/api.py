@@ -97,6 +97,22 @@ class Context:
         self._ck(self._L.globe_load_records(self.h, Nrec, N, p1 - 1, _p(indiv, C.c_int32), _p(X), _p(y)))
         self.N, self.Nrec, self.p = N, Nrec, p1 - 1
 
+    def set_individuals(self, N):
+        """Genotype-only context of N individuals (no record table), for grm_build."""
+        self._ck(self._L.globe_set_individuals(self.h, N))
+        self.N, self.Nrec, self.p = N, 0, 0
+
+    def grm_build_dev(self, d_ptr):
+        """grm_build into a device buffer of N(N+1)/2 float32 (globe_grm_build_dev)."""
+        self._ck(self._L.globe_grm_build_dev(self.h, C.c_void_p(d_ptr)))
+
+    def grm_build(self):
+        """A = Zs'Zs / M_kept of the loaded genotypes as the float32 packed lower
+        triangle (the .grm.bin payload), N(N+1)/2 values (globe_grm_build)."""
+        out = np.empty(self.N * (self.N + 1) // 2, np.float32)
+        self._ck(self._L.globe_grm_build(self.h, _p(out, C.c_float)))
+        return out
+
     def load_bed(self, payload, min_maf=0.01, max_miss=0.2):
         """payload: (M, ceil(N/4)) uint8 .bed bytes without the magic."""
         payload = np.ascontiguousarray(payload, dtype=np.uint8)
@@ -378,6 +394,17 @@ def read_grm(prefix, N):
     return g
 
 
+def write_grm(prefix, grm_lt, N):
+    """<prefix>.grm.bin from the packed lower triangle (globe_write_grm)."""
+    lib = L.lib()
+    err = C.create_string_buffer(1024)
+    g = np.ascontiguousarray(grm_lt, dtype=np.float32)
+    assert g.size == N * (N + 1) // 2
+    rc = lib.globe_write_grm(prefix.encode(), _p(g, C.c_float), N, err, 1024)
+    if rc:
+        raise GlobeError(rc, err.value.decode())
+
+
 def read_vector(path):
     """saveVector layout (utils.cpp:18-34): int32 n, then n values (float32,
     or float64 for the .f64.bin files)."""
@@ -393,6 +420,22 @@ def save_vector(path, v, f64=False):
     rc = fn(path.encode(), _p(v), v.size)
     if rc:
         raise GlobeError(rc, "cannot write %s" % path)
+
+
+def build_grm(geno, output, minMAF=0.01, maxMissingRate=0.2, precision=L.PREC_MIXED, device=0):
+    """buildGRM: <output>.grm.bin of the PLINK fileset <geno> (N = lines of the .fam),
+    the matrix runPCGsolver --geno applies.  Returns the packed lower triangle."""
+    if not (0 <= minMAF <= 0.5 and 0 <= maxMissingRate <= 1):
+        raise ValueError("Invalid MAF or missing rate thresholds.")
+    with open(geno + ".fam") as f:
+        N = sum(1 for line in f if line.split())
+    with Context(device) as ctx:
+        ctx.set_individuals(N)
+        ctx.set_precision(precision)
+        ctx.load_bed_file(geno, float(np.float32(minMAF)), float(np.float32(maxMissingRate)))
+        lt = ctx.grm_build()
+    write_grm(output, lt, N)
+    return lt
 
 
 def run_pcg_solver(input, output, sig2e, sig2g, sig2b0, sigb01, sig2b1, geno=None, grm=None, minMAF=0.01,

@@ -312,6 +312,16 @@ int globe_load_records(globe_ctx* ctx, int64_t Nrec, int32_t N, int32_t p, const
     return GLOBE_OK;
 }
 
+int globe_set_individuals(globe_ctx* ctx, int32_t N) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (N < 1) return set_err(ctx, GLOBE_ERR_ARG, "globe_set_individuals: N must be >= 1");
+    free_cohort(ctx);
+    free_genetic(ctx);
+    ctx->coh.N = N;
+    return GLOBE_OK;
+}
+
 int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf,
                        float max_miss, int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep,
                        globe_bed_info* info) {

@@ -11,6 +11,7 @@
 // parse is an error (the reference silently keeps the previous value).
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cstdarg>
 #include <cmath>
@@ -309,6 +310,30 @@ extern "C" int globe_read_grm(const char* prefix, int32_t N, float* grm_lt, char
     if (got != nelt) {
         put_err(err, errlen, "Error reading from file: %s (%zu of %zu values)", fn.c_str(), got, nelt);
         return GLOBE_ERR_FORMAT;
+    }
+    return GLOBE_OK;
+}
+
+extern "C" int globe_write_grm(const char* prefix, const float* grm_lt, int32_t N, char* err, int errlen) {
+    if (!prefix || N < 1 || !grm_lt) return GLOBE_ERR_ARG;
+    std::string fn = std::string(prefix) + ".grm.bin";
+    FILE* f = std::fopen(fn.c_str(), "wb");
+    if (!f) {
+        put_err(err, errlen, "Error opening %s for writing", fn.c_str());
+        return GLOBE_ERR_IO;
+    }
+    const size_t nelt = (size_t)N * ((size_t)N + 1) / 2;
+    size_t put = 0;
+    while (put < nelt) {
+        size_t w = std::fwrite(grm_lt + put, sizeof(float), std::min<size_t>(nelt - put, (size_t)1 << 26), f);
+        if (w == 0) break;
+        put += w;
+    }
+    const bool ok = put == nelt && std::fclose(f) == 0;
+    if (put != nelt) std::fclose(f);
+    if (!ok) {
+        put_err(err, errlen, "Error writing %s (%zu of %zu values)", fn.c_str(), put, nelt);
+        return GLOBE_ERR_IO;
     }
     return GLOBE_OK;
 }

@@ -32,18 +32,11 @@
 // tiles repeat (kpos()).
 // Every mbarrier wait is bounded (globaltimer); on timeout the CTA records
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-#include <cuda_fp8.h>
-
-#include "internal.cuh"
+#include "tc_common.cuh"
 
 namespace globe {
 namespace tc {
 
-constexpr int BM = 128;           // rows per MMA tile (TMEM lanes)
-constexpr int BK = 128;           // K elements per stage (one 128-byte swizzle panel of e4m3)
-constexpr int PKB = BK / 4;       // packed bytes per row per stage
 #ifndef TC_ASTAGES
 #define TC_ASTAGES 6
 #endif
@@ -83,10 +76,6 @@ struct Geo {
     static constexpr int DPT = MT >= 2 ? 4 : 8;            // warps of one set per tile (adfull count)
     static constexpr int ES = MT >= 2 ? 2 : 4;             // warps sharing a (tile, quadrant) epilogue
 };
-constexpr int DBITS = 5;          // digit base 32
-constexpr int DHALF = 1 << (DBITS - 1);   // 16: digits in [-16, 16]
-constexpr int NDIG = 9;           // digits per right-hand-side column (45 bits)
-constexpr int MAX_RHS_GROUP = 28; // 28 * 9 = 252 <= 256 MMA columns
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
 constexpr uint32_t LUT_G = 0x00380040u;  // code 00 -> 2.0 (0x40), 01 -> 0, 10 -> 1.0 (0x38), 11 -> 0
 
@@ -252,7 +241,8 @@ __device__ __forceinline__ void decode_word(uint32_t w, uint32_t& r0, uint32_t& 
 template <int NMMA>
 __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
     k_tc_gemm(const uint8_t* __restrict__ blk, const __grid_constant__ CUtensorMap tmB, int rows, int nchunks,
-              int cps, float* __restrict__ part, int64_t ldp, unsigned* __restrict__ err) {
+              int cps, float* __restrict__ part, int64_t ldp, int64_t pz, int skip0, int skipz,
+              unsigned* __restrict__ err) {
     using G = Geo<NMMA>;
     constexpr int MT = G::MT;
     static_assert(NMMA % 16 == 0 && NMMA >= 16 && NMMA <= 256, "NMMA");
@@ -263,7 +253,9 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
     extern __shared__ uint8_t smraw[];
     Smem<NMMA, MT>& S = *reinterpret_cast<Smem<NMMA, MT>*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row0 = blockIdx.x * ROWS, split = blockIdx.y;
+    const int row0 = blockIdx.x * ROWS, split = blockIdx.y, z = blockIdx.z;
+    if (row0 + ROWS <= skip0 + z * skipz) return;   // whole CTA, before any barrier or TMEM use
+    part += z * pz;
     const int c0 = split * cps;
     const int nloc = min(nchunks, c0 + cps) - c0;
 
@@ -320,7 +312,7 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
                 const int s = it % BSTAGES, n = it / BSTAGES;
                 if (n > 0 && !mbar_wait(&S.bempty[s], (n - 1) & 1, abort, err, 2u)) break;
                 mbar_expect_tx(&S.bfull[s], NMMA * BK);
-                tma_load_2d(S.bt[s], &tmB, (c0 + it) * BK, 0, &S.bfull[s]);
+                tma_load_2d(S.bt[s], &tmB, (c0 + it) * BK, z * NMMA, &S.bfull[s]);
                 issued = it + 1;
             }
             for (int it = issued - 1; it >= 0 && it >= issued - BSTAGES; --it)
@@ -434,11 +426,6 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
 
 // ---- digit and combine kernels ---------------------------------------------
 
-__device__ __forceinline__ int kpos(int64_t i) {
-    // K position of element i after the decode permutation within groups of 16
-    const int q = (int)(i & 15);
-    return (int)(i & ~15ll) + ((q & 1) ? 8 + (q >> 1) : (q >> 1));
-}
 
 
 // per-column max |x| and sum over n rows (partials per CTA)
@@ -494,33 +481,6 @@ __global__ void k_col_finish(const double* __restrict__ pmax, const double* __re
     }
 }
 
-// 2^e sum_j 32^-j P_j of one row.  Every FP32 partial is an exact integer (|P| < 2^24), so
-// the split partials are summed in int64 and the digits combined in two exact int64 halves
-// (hi = digits 0..4, lo = digits 5..8); the only rounding is the final FP64 addition.
-constexpr int NDIG_HI = (NDIG + 1) / 2;
-__device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
-                                           int64_t row, double s_hi, double s_lo) {
-    long long pj[NDIG];
-#pragma unroll
-    for (int j = 0; j < NDIG; ++j) pj[j] = (long long)__float2int_rn(part[((int64_t)c * NDIG + j) * ldp + row]);
-    for (int y = 1; y < nsplit; ++y) {
-#pragma unroll
-        for (int j = 0; j < NDIG; ++j)
-            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * NDIG + j) * ldp + row]);
-    }
-    long long hi = 0, lo = 0;
-#pragma unroll
-    for (int j = 0; j < NDIG_HI; ++j) hi = hi * (1 << DBITS) + pj[j];
-#pragma unroll
-    for (int j = NDIG_HI; j < NDIG; ++j) lo = lo * (1 << DBITS) + pj[j];
-    return (double)hi * s_hi + (double)lo * s_lo;
-}
-
-// scale factors of recombine for exponent e: 2^(e - 5 (NDIG_HI - 1)) and 2^(e - 5 (NDIG - 1))
-__device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_lo) {
-    s_hi = ldexp(1.0, e - DBITS * (NDIG_HI - 1));
-    s_lo = ldexp(1.0, e - DBITS * (NDIG - 1));
-}
 
 // digits of X (n x k, FP64) into D[(c*NDIG + j) * kpad + kpos(r)]  (e4m3); every position
 // in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
@@ -530,9 +490,6 @@ __device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_
 // balanced base-32 digits are peeled off from the least significant end in integer
 // arithmetic (d = ((I + 16) mod 32) - 16, in [-16, 15]); the leading digit is what
 // remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (NDIG-1) fraction bits.
-__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], exact in e4m3
-    return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
-}
 
 __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
                          uint8_t* __restrict__ D, int64_t kpad) {
@@ -705,7 +662,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-static int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t box_in,
+int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t box_in,
                     uint32_t box_out, bool sw128) {
     auto fn = encode_fn();
     if (!fn) return set_err(ctx, GLOBE_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -764,7 +721,7 @@ int ensure_gt(globe_ctx* ctx) {
 
 template <int NMMA>
 static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB, int rows, int nchunks, int splits,
-                       float* part, int64_t ldp, unsigned* err) {
+                       float* part, int64_t ldp, unsigned* err, const ZGrid& zg) {
     using G = Geo<NMMA>;
     const int cps = (nchunks + splits - 1) / splits;
     splits = (nchunks + cps - 1) / cps;
@@ -774,38 +731,39 @@ static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB
         GLOBE_CK(ctx, cudaFuncSetAttribute(k_tc_gemm<NMMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    dim3 grid((unsigned)((rows + G::MT * BM - 1) / (G::MT * BM)), (unsigned)splits);
-    k_tc_gemm<NMMA><<<grid, G::NTHREADS, smem, ctx->stream>>>(blk, mB, rows, nchunks, cps, part, ldp, err);
+    dim3 grid((unsigned)((rows + G::MT * BM - 1) / (G::MT * BM)), (unsigned)splits, (unsigned)zg.nz);
+    k_tc_gemm<NMMA><<<grid, G::NTHREADS, smem, ctx->stream>>>(blk, mB, rows, nchunks, cps, part, ldp, zg.pz,
+                                                               zg.skip0, zg.skipz, err);
     GLOBE_LAUNCHED(ctx, "k_tc_gemm");
     return GLOBE_OK;
 }
 
-static int rows_per_cta(int nmma) { return BM * (nmma <= 64 ? 4 : (nmma <= 192 ? 2 : 1)); }
+int rows_per_cta(int nmma) { return BM * (nmma <= 64 ? 4 : (nmma <= 192 ? 2 : 1)); }
 
-static int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* mA, const CUtensorMap& mB, int rows,
-                         int nchunks, int splits, float* part, int64_t ldp, unsigned* err) {
+int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* mA, const CUtensorMap& mB, int rows, int nchunks,
+                  int splits, float* part, int64_t ldp, unsigned* err, const ZGrid& zg) {
     switch (nmma) {
-        case 16: return launch_gemm<16>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 32: return launch_gemm<32>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 48: return launch_gemm<48>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 64: return launch_gemm<64>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 80: return launch_gemm<80>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 96: return launch_gemm<96>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 112: return launch_gemm<112>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 128: return launch_gemm<128>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 144: return launch_gemm<144>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 160: return launch_gemm<160>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 176: return launch_gemm<176>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 192: return launch_gemm<192>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 208: return launch_gemm<208>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 224: return launch_gemm<224>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 240: return launch_gemm<240>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
-        case 256: return launch_gemm<256>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err);
+        case 16: return launch_gemm<16>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 32: return launch_gemm<32>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 48: return launch_gemm<48>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 64: return launch_gemm<64>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 80: return launch_gemm<80>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 96: return launch_gemm<96>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 112: return launch_gemm<112>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 128: return launch_gemm<128>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 144: return launch_gemm<144>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 160: return launch_gemm<160>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 176: return launch_gemm<176>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 192: return launch_gemm<192>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 208: return launch_gemm<208>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 224: return launch_gemm<224>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 240: return launch_gemm<240>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 256: return launch_gemm<256>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
     }
     return set_err(ctx, GLOBE_ERR_ARG, "unsupported MMA width %d", nmma);
 }
 
-static int eff_splits(int nchunks, int splits) {
+int eff_splits(int nchunks, int splits) {
     const int cps = (nchunks + splits - 1) / splits;
     return (nchunks + cps - 1) / cps;
 }
@@ -867,7 +825,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     // ---- pass 1
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS1);
-        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err));
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, ZGrid()));
     }
     const int sp1e = eff_splits(nch1, sp1);
     k_combine1<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
@@ -883,7 +841,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     GLOBE_LAUNCHED(ctx, "k_digits");
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS2);
-        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, mB2, N, nch2, sp2, P2, ldp2, err));
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, mB2, N, nch2, sp2, P2, ldp2, err, ZGrid()));
     }
     const int sp2e = eff_splits(nch2, sp2);
     k_combine2<<<dim3(div_up(N, 256) < 1024 ? div_up(N, 256) : 1024, kg), 256, 0, ctx->stream>>>(

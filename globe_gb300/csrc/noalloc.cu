@@ -45,7 +45,7 @@ extern "C" int globe_precond_apply_dev_noalloc(globe_ctx* ctx, const double* d_r
     if (!ctx || !d_r || !d_z || k < 1) return GLOBE_ERR_ARG;
     const cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return set_err(ctx, GLOBE_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
-    if (ctx->coh.N < 1) return set_err(ctx, GLOBE_ERR_STATE, "no records loaded");
+    if (ctx->coh.Nrec < 1) return set_err(ctx, GLOBE_ERR_STATE, "no records loaded");
     if (!ctx->precond_ok)
         return set_err(ctx, GLOBE_ERR_STATE,
                        "preconditioner not built at the current components: call globe_precond_apply or globe_pcg "

@@ -12,7 +12,7 @@
 namespace globe {
 
 int check_ready(globe_ctx* ctx) {
-    if (ctx->coh.N < 1) return set_err(ctx, GLOBE_ERR_STATE, "no record table loaded");
+    if (ctx->coh.Nrec < 1) return set_err(ctx, GLOBE_ERR_STATE, "no record table loaded");
     if (ctx->gen.src == GSRC_NONE) return set_err(ctx, GLOBE_ERR_STATE, "no genotypes or GRM loaded");
     if (!ctx->vc_set) return set_err(ctx, GLOBE_ERR_STATE, "variance components not set");
     return GLOBE_OK;

@@ -1,0 +1,87 @@
+// tc_common.cuh -- what the tensor-core genotype kernels share: the tile and
+// digit constants, the K permutation of the decoded operand, the e4m3 digit
+// encoding, the exact recombination of split partials, and the host launch
+// of k_tc_gemm (defined in k_tc_geno.cu).
+#pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_fp8.h>
+
+#include "internal.cuh"
+
+namespace globe {
+namespace tc {
+
+constexpr int BM = 128;           // rows per MMA tile (TMEM lanes)
+constexpr int BK = 128;           // K elements per stage (one 128-byte swizzle panel of e4m3)
+constexpr int PKB = BK / 4;       // packed bytes per row per stage
+constexpr int DBITS = 5;          // digit base 32
+constexpr int DHALF = 1 << (DBITS - 1);   // 16: digits in [-16, 16]
+constexpr int NDIG = 9;           // digits per right-hand-side column (45 bits)
+constexpr int NDIG_HI = (NDIG + 1) / 2;
+constexpr int MAX_RHS_GROUP = 28; // 28 * 9 = 252 <= 256 MMA columns
+
+__device__ __forceinline__ int kpos(int64_t i) {
+    // K position of element i after the decode permutation within groups of 16
+    const int q = (int)(i & 15);
+    return (int)(i & ~15ll) + ((q & 1) ? 8 + (q >> 1) : (q >> 1));
+}
+
+__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], exact in e4m3
+    return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
+}
+
+// 2^e sum_j 32^-j P_j of one row.  Every FP32 partial is an exact integer (|P| < 2^24), so
+// the split partials are summed in int64 and the digits combined in two exact int64 halves
+// (hi = digits 0..4, lo = digits 5..8); the only rounding is the final FP64 addition.
+__device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
+                                           int64_t row, double s_hi, double s_lo) {
+    long long pj[NDIG];
+#pragma unroll
+    for (int j = 0; j < NDIG; ++j) pj[j] = (long long)__float2int_rn(part[((int64_t)c * NDIG + j) * ldp + row]);
+    for (int y = 1; y < nsplit; ++y) {
+#pragma unroll
+        for (int j = 0; j < NDIG; ++j)
+            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * NDIG + j) * ldp + row]);
+    }
+    long long hi = 0, lo = 0;
+#pragma unroll
+    for (int j = 0; j < NDIG_HI; ++j) hi = hi * (1 << DBITS) + pj[j];
+#pragma unroll
+    for (int j = NDIG_HI; j < NDIG; ++j) lo = lo * (1 << DBITS) + pj[j];
+    return (double)hi * s_hi + (double)lo * s_lo;
+}
+
+// scale factors of recombine for exponent e: 2^(e - 5 (NDIG_HI - 1)) and 2^(e - 5 (NDIG - 1))
+__device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_lo) {
+    s_hi = ldexp(1.0, e - DBITS * (NDIG_HI - 1));
+    s_lo = ldexp(1.0, e - DBITS * (NDIG - 1));
+}
+
+// per-column max |x| and sum over n rows (partials per CTA); colinfo[c] = {exponent e with
+// max |x 2^-e| < 16, column sum} from those partials (k_tc_geno.cu)
+__global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld, double* __restrict__ pmax,
+                             double* __restrict__ psum);
+__global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
+                             double* __restrict__ colinfo);
+
+}  // namespace tc
+
+// Extra launch dimension of k_tc_gemm: gridDim.z = nz independent digit
+// operands stacked in one tensor map (operand z = map rows z*NMMA ..), partials
+// of operand z at part + z * pz.  A CTA whose rows all lie below
+// skip0 + z * skipz does nothing (the lower-triangle GRM build uses this).
+struct ZGrid {
+    int nz = 1;
+    int64_t pz = 0;
+    int skip0 = 0, skipz = 0;
+};
+
+int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t box_in,
+             uint32_t box_out, bool sw128);
+int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* blk, const CUtensorMap& mB, int rows, int nchunks,
+                  int splits, float* part, int64_t ldp, unsigned* err, const ZGrid& zg);
+int rows_per_cta(int nmma);
+int eff_splits(int nchunks, int splits);
+
+}  // namespace globe

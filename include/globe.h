@@ -123,6 +123,13 @@ int globe_get_dims(const globe_ctx* ctx, int64_t* Nrec, int32_t* N, int32_t* p, 
 int globe_load_records(globe_ctx* ctx, int64_t Nrec, int32_t N, int32_t p,
                        const int32_t* indiv, const double* X, const double* y);
 
+/* Genotype-only context: N individuals (the lines of the .fam) and no record
+ * table, for building a GRM (globe_grm_build).  Drops any loaded records and
+ * genetic source.  The solver entry points still need globe_load_records.
+ * No reference counterpart: the reference takes N from the record table
+ * (PCGsolver.cpp:529-587) and has no GRM builder. */
+int globe_set_individuals(globe_ctx* ctx, int32_t N);
+
 /* PLINK .bed payload (the bytes after the 3-byte magic): M SNP rows of
  * ceil(N/4) bytes, N from globe_load_records.  Computes per-SNP A1 counts,
  * missing counts, the float32 A1 frequency and missing rate, applies the
@@ -152,6 +159,19 @@ int globe_load_bed_file(globe_ctx* ctx, const char* prefix, float min_maf, float
  * N(N+1)/2 values (.grm.bin payload).  Replaces readFullGRM
  * (PCGsolver.cpp:778-809) and readGRM (varCompEst.cpp:270-295). */
 int globe_load_grm(globe_ctx* ctx, const float* grm_lt, int32_t N);
+
+/* Genetic relationship matrix of the loaded genotypes, A = Zs'Zs / M_kept with
+ * zs = (g - 2f) inv_std and missing g -> 0 (getStdGenotype,
+ * PCGsolver.cpp:826-842: the matrix the --geno product applies), as the
+ * float32 packed lower triangle, row major with the diagonal, N(N+1)/2 values:
+ * the payload of <prefix>.grm.bin that readFullGRM (PCGsolver.cpp:778-809)
+ * and readGRM (varCompEst.cpp:270-295) read.  The reference has no builder.
+ * GLOBE_PREC_MIXED: tensor cores, each value the float32 rounding of an
+ * evaluation exact to ~2^-41 max|inv_std zs| per term; GLOBE_PREC_FP64: FP64
+ * arithmetic.  Needs at least one kept SNP (GLOBE_ERR_STATE otherwise). */
+int globe_grm_build(globe_ctx* ctx, float* grm_lt);
+/* Same into a device buffer of N(N+1)/2 floats. */
+int globe_grm_build_dev(globe_ctx* ctx, float* d_grm_lt);
 
 /* Variance components (sig2e, sig2g, sig2b0, sigb01, sig2b1).  sig2e must be
  * > 0 (the block preconditioner is singular otherwise). */
@@ -329,6 +349,9 @@ int globe_bed_dims(const char* prefix, int32_t N, int64_t* M, char* err, int err
 int globe_read_bed(const char* prefix, int32_t N, int64_t M, uint8_t* payload, char* err, int errlen);
 /* <prefix>.grm.bin: N(N+1)/2 float32 (readFullGRM, PCGsolver.cpp:778-809). */
 int globe_read_grm(const char* prefix, int32_t N, float* grm_lt, char* err, int errlen);
+/* Writes <prefix>.grm.bin: the N(N+1)/2 float32 values of grm_lt, no header
+ * (the layout globe_read_grm and readFullGRM read). */
+int globe_write_grm(const char* prefix, const float* grm_lt, int32_t N, char* err, int errlen);
 
 /* ---- profiling ---------------------------------------------------------- */
 
@@ -339,6 +362,8 @@ int globe_read_grm(const char* prefix, int32_t N, float* grm_lt, char* err, int 
 #define GLOBE_PROF_GRM_PASS1 1  /* genotype pass 1 (w = Zs v) / dense kernel */
 #define GLOBE_PROF_GRM_PASS2 2  /* genotype pass 2 (Zs' w) */
 #define GLOBE_PROF_PCG_ITER 3   /* one block-PCG iteration */
+#define GLOBE_PROF_GRM_BUILD 4  /* one globe_grm_build[_dev] (all its launches) */
+#define GLOBE_PROF_GRM_BUILD_GEMM 5  /* its GEMM launches (tensor-core or FP64) */
 #define GLOBE_PROF_KINDS 8
 /* on != 0 starts recording (and clears the counters); 0 stops. */
 int globe_prof_enable(globe_ctx* ctx, int on);

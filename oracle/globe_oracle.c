@@ -109,6 +109,31 @@ static double zs_of(const orc_model* m, int64_t s, int32_t i) {
     return ((double)g - 2.0 * m->f[s]) * m->inv_std[s];
 }
 
+void orc_grm_build(const uint8_t* geno, int64_t Mk, int64_t stride, int32_t N, const double* f,
+                   const double* inv_std, float* lt) {
+    /* individual-major zs, so that each A_ij is one contiguous dot product */
+    double* Z = (double*)malloc(sizeof(double) * (size_t)N * (size_t)(Mk > 0 ? Mk : 1));
+#pragma omp parallel for schedule(static)
+    for (int32_t i = 0; i < N; ++i)
+        for (int64_t s = 0; s < Mk; ++s) {
+            unsigned c = (geno[s * stride + i / 4] >> (2 * (i % 4))) & 3u;
+            int g = decode_code(c);
+            if (g < 0) g = 0;
+            Z[(size_t)i * Mk + s] = ((double)g - 2.0 * f[s]) * inv_std[s];
+        }
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int32_t i = 0; i < N; ++i) {
+        const double* zi = Z + (size_t)i * Mk;
+        for (int32_t j = 0; j <= i; ++j) {
+            const double* zj = Z + (size_t)j * Mk;
+            double acc = 0.0;
+            for (int64_t s = 0; s < Mk; ++s) acc += zi[s] * zj[s];
+            lt[(size_t)i * (i + 1) / 2 + j] = (float)(acc / (double)Mk);
+        }
+    }
+    free(Z);
+}
+
 orc_solver* orc_create(const orc_model* m) {
     orc_solver* s = (orc_solver*)calloc(1, sizeof(orc_solver));
     s->m = *m;

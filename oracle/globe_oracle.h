@@ -33,6 +33,14 @@ int64_t orc_bed_stats(const uint8_t* bed, int64_t M, int32_t N, float min_maf,
 void orc_std_params(const int64_t* alt, const int64_t* miss, int64_t M, int32_t N,
                     double* f, double* inv_std);
 
+/* A = Zs'Zs / Mk of the kept SNP rows (Mk rows of `stride` bytes), zs as
+ * getStdGenotype (PCGsolver.cpp:826-842, missing -> 0), summed in double in
+ * SNP order and rounded once to float32; written as the packed lower
+ * triangle lt[i(i+1)/2 + j], j <= i (the .grm.bin layout readFullGRM reads,
+ * PCGsolver.cpp:778-809). */
+void orc_grm_build(const uint8_t* geno, int64_t Mk, int64_t stride, int32_t N, const double* f,
+                   const double* inv_std, float* lt);
+
 typedef struct {
     int32_t N;            /* individuals */
     int64_t Nrec;         /* records */

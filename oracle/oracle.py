@@ -81,6 +81,26 @@ def std_params(alt, miss, N):
     return f, inv
 
 
+def grm_build(packed, N, min_maf=0.01, max_miss=0.2, freq="f64"):
+    """A = Zs'Zs / M_kept as the float32 packed lower triangle (orc_grm_build).
+    freq "f64": the allele frequency and inverse std of the float->double
+    reference build (std_params; what the product path uses).  freq "f32": the
+    FP32 program's float maf (PCGsolver.cpp:728) widened to double, with
+    inv_std = 1/sqrt(2f(1-f)) in double (1 when 2f(1-f) <= 1e-12)."""
+    alt, miss, maf, _, keep = bed_stats(packed, N, min_maf, max_miss)
+    kp = np.ascontiguousarray(np.asarray(packed, np.uint8)[keep])
+    if freq == "f64":
+        f, inv = std_params(alt[keep], miss[keep], N)
+    else:
+        f = maf[keep].astype(np.float64)
+        den = 2 * f * (1 - f)
+        inv = np.where(den > 1e-12, 1.0 / np.sqrt(np.where(den > 0, den, 1.0)), 1.0)
+    lt = np.zeros(N * (N + 1) // 2, np.float32)
+    lib().orc_grm_build(_p(kp, C.c_uint8), C.c_int64(kp.shape[0]), C.c_int64((N + 3) // 4), C.c_int32(N),
+                        _p(f), _p(inv), _p(lt, C.c_float))
+    return lt
+
+
 class Solver:
     """One cohort + one genetic source (kept genotypes or dense packed GRM)."""
 

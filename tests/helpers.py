@@ -69,3 +69,11 @@ def cohort(seed, N, M, recs=("uniform", 3, 10), T=5.0, miss=0.01, edge=False, ma
     coh = synth.simulate_cohort(seed, N, M, recs, T, maf_lo=maf_lo, miss_rate=miss, edge_snps=edge)
     coh["X"] = np.asfortranarray(np.column_stack([coh["cov"], coh["times"]]))
     return coh
+
+
+def f32_ulps(a, b):
+    """Distance in float32 units in the last place, elementwise."""
+    def key(x):
+        i = np.ascontiguousarray(x, np.float32).view(np.int32).astype(np.int64)
+        return np.where(i < 0, -(i & 0x7FFFFFFF), i)
+    return np.abs(key(a) - key(b))
