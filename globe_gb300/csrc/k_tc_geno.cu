@@ -351,14 +351,6 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
         for (int it = set; it < nloc && ok; it += G::NSET) {
             const int sa = it % ASTAGES, ds = it % DSTAGES;
             if (!mbar_wait<TC_SLEEP_DEC != 0>(&S.afull[sa], (it / ASTAGES) & 1, abort, err, 16u)) { ok = false; break; }
-            if (it >= DSTAGES) {
-#pragma unroll
-                for (int q = 0; q < G::TPW; ++q)
-                    if (ok && !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[t0 + q][ds], ((it / DSTAGES) - 1) & 1, abort,
-                                                            err, 32u))
-                        ok = false;
-                if (!ok) break;
-            }
             uint4 v[G::UPW];
 #pragma unroll
             for (int i = 0; i < G::UPW; ++i) {
@@ -375,6 +367,17 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.aempty[sa]);   // packed stage consumed
+            // the decoded slot is free once the MMAs of the stage DSTAGES back completed; the decode
+            // above already overlapped them
+            if (it >= DSTAGES) {
+#pragma unroll
+                for (int q = 0; q < G::TPW; ++q)
+                    if (ok && !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[t0 + q][ds], ((it / DSTAGES) - 1) & 1, abort,
+                                                            err, 32u))
+                        ok = false;
+                if (!ok) break;
+                tc_after();   // order the stores after the MMAs that read the slot
+            }
 #pragma unroll
             for (int i = 0; i < G::UPW; ++i) {
                 const int u = j * MT + i, m = u >> 1, h = u & 1;
@@ -768,12 +771,35 @@ int eff_splits(int nchunks, int splits) {
     return (nchunks + cps - 1) / cps;
 }
 
-static int pick_splits(int tiles, int nchunks) {
-    int want = (8 * 152 + tiles - 1) / tiles;        // >= ~8 CTA waves
-    int maxs = std::max(1, nchunks / 8);              // >= 8 stages per CTA
-    want = std::min(want, maxs);
-    want = std::max(want, (nchunks + 4095) / 4096);   // K per CTA <= 2^19 (exact FP32 sums)
-    return std::max(1, want);
+// Split-K count for `tiles` CTA row blocks of `nchunks` K stages.  One CTA runs per SM, so
+// the pass takes about ceil(CTAs / SMs) waves of (stages per CTA + a fixed CTA cost: setup,
+// pipeline fill and drain, epilogue).  The count minimising that estimate is taken, within
+// K per CTA <= 2^19 (exact FP32 sums) and >= 8 stages per CTA.  Example: 196 row blocks x
+// 3907 stages gives 10 splits (1960 CTAs, 12.9 waves on 152 SMs) where aiming at ~8 waves
+// gave 7 (1372 CTAs, 9.03 waves: a tenth wave of 4 CTAs).
+static int pick_splits(globe_ctx* ctx, int tiles, int nchunks) {
+    static int sms = 0;
+    if (sms == 0) {
+        int v = 0;
+        sms = (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, ctx->device) == cudaSuccess && v > 0) ? v
+                                                                                                             : 152;
+    }
+    constexpr int CTA_COST = 8;                       // fixed cost of a CTA, in stages
+    const int lo = std::max(1, (nchunks + 4095) / 4096);
+    const int hi = std::max(lo, std::min(64, nchunks / 8));
+    int best = lo;
+    double best_cost = 1e300;
+    for (int s = lo; s <= hi; ++s) {
+        const int cps = (nchunks + s - 1) / s;
+        const int se = (nchunks + cps - 1) / cps;
+        const double waves = std::ceil((double)tiles * se / sms);
+        const double cost = waves * (cps + CTA_COST);
+        if (cost < best_cost * 0.999) {
+            best_cost = cost;
+            best = s;
+        }
+    }
+    return best;
 }
 
 // out (N x k) = scale * Zs'(Zs Z) for one group of <= MAX_RHS_GROUP columns
@@ -788,7 +814,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     const int64_t kpad2 = (int64_t)nch2 * BK;
     const int rpc = rows_per_cta(nmma);
     const int tiles1 = (int)((g.Mk + rpc - 1) / rpc), tiles2 = (N + rpc - 1) / rpc;
-    const int sp1 = pick_splits(tiles1, nch1), sp2 = pick_splits(tiles2, nch2);
+    const int sp1 = pick_splits(ctx, tiles1, nch1), sp2 = pick_splits(ctx, tiles2, nch2);
     const int64_t ldp1 = (int64_t)tiles1 * rpc, ldp2 = (int64_t)tiles2 * rpc;
     uint8_t *D1, *D2;
     float *P1, *P2;

@@ -7,6 +7,9 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp8.h>
 
+#include <algorithm>
+#include <cmath>
+
 #include "internal.cuh"
 
 namespace globe {
