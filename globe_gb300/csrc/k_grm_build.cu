@@ -31,14 +31,14 @@ constexpr int GRM_KG = 21;                                  // columns per group
 constexpr int GRM_NMMA = (GRM_KG * NDIG + 15) / 16 * 16;    // 192
 static_assert(GRM_KG <= 28 && GRM_NMMA <= 256, "group width");
 
-// U4[4s + c] = inv_s zs_s[c]: the four values of u(s, .) by 2-bit code
+// U4[4s + t] = inv_s zs_s: the value of u(s, .) for tile code t (the codes of blk2)
 __global__ void k_grm_u4(const double* __restrict__ zs, const double* __restrict__ inv, int64_t Mk,
                          double* __restrict__ U4) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < 4 * Mk; e += (int64_t)gridDim.x * blockDim.x)
-        U4[e] = inv[e >> 2] * zs[e];
+        U4[e] = inv[e >> 2] * zs[(e & ~3ll) + tile_to_plink((int)(e & 3))];
 }
 
-// Per SNP s < kpad and code c: the 9 e4m3 digits of I = round(u 2^(40-e)) (bytes 0..8 of
+// Per SNP s < kpad and tile code c: the 9 e4m3 digits of I = round(u 2^(40-e)) (bytes 0..8 of
 // dig[4s+c], most significant first) and 2 f_s u~ with u~ = I 2^(e-40) the rounded value.
 // SNPs >= Mk (padding of the K range) get zero digits and zero.
 __global__ void k_grm_table(const double* __restrict__ U4, const double* __restrict__ f, int64_t Mk, int64_t kpad,
@@ -79,7 +79,7 @@ __device__ __forceinline__ uint32_t dig_byte(const uint4& v, int j) {
 // jj = z * GRM_KG + c goes to digit rows z * GRM_NMMA + c * NDIG + j, K positions in the
 // decode order of the A operand (position P of a group of 16 holds SNP 2P for P < 8,
 // 2(P-8)+1 otherwise).  The codes come from the individual-major tile-blocked copy
-// (blk2): 16 SNPs of individual i are one 32-bit word.  C2[jj] = sum_s 2 f_s u~(s, j).
+// (blk2, tile codes): 16 SNPs of individual i are one 32-bit word.  C2[jj] = sum_s 2 f_s u~(s, j).
 __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ blk2, int nch2, int32_t N, int jb,
                                                     const uint4* __restrict__ dig, const double* __restrict__ c2v,
                                                     int64_t kpad, uint8_t* __restrict__ D, double* __restrict__ C2) {

@@ -49,8 +49,17 @@ namespace tc {
 #ifndef TC_SLEEP
 #define TC_SLEEP 1       // producers / MMA issuer suspend in their waits
 #endif
+#ifndef TC_DEC_PRE
+#define TC_DEC_PRE 8     // 16-byte units a decoder warp decodes before it waits for its TMEM slot
+#endif
+#ifndef TC_STW
+#define TC_STW 16        // columns per tcgen05.st of a decoded unit (16, or 8 in two stores)
+#endif
+#ifndef TC_POLL8
+#define TC_POLL8 0       // polling waits make 8 try_waits per loop iteration
+#endif
 #ifndef TC_SLEEP_DEC
-#define TC_SLEEP_DEC 0   // decoders poll
+#define TC_SLEEP_DEC 1   // decoders suspend in their waits too
 #endif
 constexpr int ASTAGES = TC_ASTAGES;  // packed-genotype ring (keeps DRAM reads in flight)
 constexpr int BSTAGES = TC_BSTAGES;  // digit-tile ring (L2-resident operand)
@@ -77,7 +86,9 @@ struct Geo {
     static constexpr int ES = MT >= 2 ? 2 : 4;             // warps sharing a (tile, quadrant) epilogue
 };
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
-constexpr uint32_t LUT_G = 0x00380040u;  // code 00 -> 2.0 (0x40), 01 -> 0, 10 -> 1.0 (0x38), 11 -> 0
+// byte tables of the decode (prmt operands a, b): a = {2.0, 1.0, 0, 0}, b = {1.0, 0, 0, 0} in e4m3
+constexpr uint32_t LUT_A = 0x00003840u;
+constexpr uint32_t LUT_B = 0x00000038u;
 
 __host__ __device__ constexpr int ncols_alloc(int n) {
     return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
@@ -121,6 +132,19 @@ __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// up to 8 try_waits in straight-line PTX, leaving at the first that succeeds: one call
+// costs a few integer instructions however many polls it makes
+__device__ __forceinline__ bool mbar_try8(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+#define GLOBE_TRY1 " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n @p bra.uni DONE;\n"
+    asm volatile("{\n .reg .pred p;\n" GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1
+                 GLOBE_TRY1 " mov.u32 %0, 0;\n bra.uni END;\n DONE:\n mov.u32 %0, 1;\n END:\n}\n"
+                 : "=r"(ok)
+                 : "r"(saddr(b)), "r"(parity)
+                 : "memory");
+#undef GLOBE_TRY1
+    return ok != 0;
+}
 // try_wait that may suspend the thread until the phase completes (hint in ns)
 __device__ __forceinline__ bool mbar_try_sleep(uint64_t* b, uint32_t parity) {
     uint32_t ok;
@@ -138,7 +162,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* abo
     if (mbar_try(b, parity)) return true;
     uint64_t t0 = 0;
     for (uint32_t spins = 1;; ++spins) {
-        if (SLEEP ? mbar_try_sleep(b, parity) : mbar_try(b, parity)) return true;
+        if (SLEEP ? mbar_try_sleep(b, parity) : (TC_POLL8 ? mbar_try8(b, parity) : mbar_try(b, parity))) return true;
         if ((spins & 255u) == 0) {
             if (*(volatile int*)abort) return false;
             const uint64_t t = gtime();
@@ -203,6 +227,20 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16
         "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
         : "memory");
 }
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
+                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+// one decoded 16-byte unit (16 columns of one lane quadrant)
+__device__ __forceinline__ void tmem_st_unit(uint32_t taddr, const uint32_t (&v)[16]) {
+    if (TC_STW == 8) {
+        tmem_st8(taddr, v);
+        tmem_st8(taddr + 8, v + 8);
+    } else {
+        tmem_st16(taddr, v);
+    }
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
@@ -226,13 +264,25 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
     return d;
 }
 
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+// 16 tile codes -> 16 e4m3 bytes.  prmt takes 4 selector nibbles from the low half of its
+// selector: 3 bits pick a byte of {b, a}, and a set top bit replicates that byte's sign bit.
+//   even codes: w & 0x33..  nibble = code        -> a[0] = 2.0, a[1] = 1.0, a[2] = 0
+//   odd codes:  w & 0xCC..  nibble = code << 2   -> 0: a[0] = 2.0, 4: b[0] = 1.0,
+//                                                   8: sign of a[0] (0) replicated = 0
+// 8 integer instructions per 16 genotypes.  Output order: r0 = genotypes 0,2,4,6,
+// r1 = 8..14 even, r2 = 1,3,5,7, r3 = 9..15 odd (the K permutation kpos inverts).
 __device__ __forceinline__ void decode_word(uint32_t w, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
     const uint32_t e = w & 0x33333333u;
-    const uint32_t o = (w >> 2) & 0x33333333u;
-    r0 = __byte_perm(LUT_G, 0u, e);
-    r1 = __byte_perm(LUT_G, 0u, e >> 16);
-    r2 = __byte_perm(LUT_G, 0u, o);
-    r3 = __byte_perm(LUT_G, 0u, o >> 16);
+    const uint32_t o = w & 0xCCCCCCCCu;
+    r0 = prmt(LUT_A, LUT_B, e);
+    r1 = prmt(LUT_A, LUT_B, e >> 16);
+    r2 = prmt(LUT_A, LUT_B, o);
+    r3 = prmt(LUT_A, LUT_B, o >> 16);
 }
 
 // A operand: tile-blocked packed genotypes, block (tile t, chunk c) = 128 rows x 32 B contiguous at
@@ -324,18 +374,24 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
         if (lane == 0 && nloc > 0) {
             const uint32_t idesc = (1u << 4) | ((uint32_t)(NMMA >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
             const uint32_t dcol = tmem + (uint32_t)(m * NMMA);
+            // B descriptors differ only in their start address (bits 0-13, address / 16): slot sb
+            // and K step kk add sb * NMMA * BK / 16 + 2 kk, which stays inside the field
+            const uint64_t dbase = desc_sw128(saddr(S.bt[0]));
+            int sb = 0, ds = 0;
+            uint32_t pb = 0, pd = 0;
             for (int it = 0; it < nloc; ++it) {
-                const int sb = it % BSTAGES, ds = it % DSTAGES;
-                if (!mbar_wait(&S.bfull[sb], (it / BSTAGES) & 1, abort, err, 4u)) break;
-                if (!mbar_wait(&S.adfull[m][ds], (it / DSTAGES) & 1, abort, err, 8u)) break;
+                if (!mbar_wait(&S.bfull[sb], pb, abort, err, 4u)) break;
+                if (!mbar_wait(&S.adfull[m][ds], pd, abort, err, 8u)) break;
                 tc_after();
-                const uint32_t b0 = saddr(S.bt[sb]);
                 const uint32_t acol = tmem + (uint32_t)(ACOL0 + (ds * MT + m) * 32);
+                const uint64_t bd = dbase + (uint64_t)(sb * ((NMMA * BK) >> 4));
 #pragma unroll
                 for (int kk = 0; kk < BK / 32; ++kk)
-                    mma_f8_ta(dcol, acol + (uint32_t)(kk * 8), desc_sw128(b0 + kk * 32), idesc, (it | kk) != 0);
+                    mma_f8_ta(dcol, acol + (uint32_t)(kk * 8), bd + (uint64_t)(2 * kk), idesc, (it | kk) != 0);
                 mma_commit(&S.bempty[sb]);
                 mma_commit(&S.adempty[m][ds]);
+                if (++sb == BSTAGES) { sb = 0; pb ^= 1u; }
+                if (++ds == DSTAGES) { ds = 0; pd ^= 1u; }
             }
             mma_commit(&S.accfull[m]);  // tracks every MMA this thread issued
         }
@@ -349,17 +405,20 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
         const int swz = (r >> 2) & 1;
         bool ok = true;
         for (int it = set; it < nloc && ok; it += G::NSET) {
+            // (slots and phases from it: running counters here cost registers and ~15% of the pass)
             const int sa = it % ASTAGES, ds = it % DSTAGES;
-            if (!mbar_wait<TC_SLEEP_DEC != 0>(&S.afull[sa], (it / ASTAGES) & 1, abort, err, 16u)) { ok = false; break; }
+            const uint32_t pa = (it / ASTAGES) & 1, pdd = (it / DSTAGES) & 1;
+            if (!mbar_wait<TC_SLEEP_DEC != 0>(&S.afull[sa], pa, abort, err, 16u)) { ok = false; break; }
             uint4 v[G::UPW];
 #pragma unroll
             for (int i = 0; i < G::UPW; ++i) {
                 const int u = j * MT + i, m = u >> 1, h = u & 1;
                 v[i] = *reinterpret_cast<const uint4*>(S.pk[sa] + m * (BM * PKB) + (r * 2 + (h ^ swz)) * 16);
             }
+            constexpr int PRE = TC_DEC_PRE < G::UPW ? TC_DEC_PRE : G::UPW;
             uint32_t o[G::UPW][16];
 #pragma unroll
-            for (int i = 0; i < G::UPW; ++i) {
+            for (int i = 0; i < PRE; ++i) {
                 decode_word(v[i].x, o[i][0], o[i][1], o[i][2], o[i][3]);
                 decode_word(v[i].y, o[i][4], o[i][5], o[i][6], o[i][7]);
                 decode_word(v[i].z, o[i][8], o[i][9], o[i][10], o[i][11]);
@@ -372,7 +431,7 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
             if (it >= DSTAGES) {
 #pragma unroll
                 for (int q = 0; q < G::TPW; ++q)
-                    if (ok && !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[t0 + q][ds], ((it / DSTAGES) - 1) & 1, abort,
+                    if (ok && !mbar_wait<TC_SLEEP_DEC != 0>(&S.adempty[t0 + q][ds], pdd ^ 1u, abort,
                                                             err, 32u))
                         ok = false;
                 if (!ok) break;
@@ -381,7 +440,13 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
 #pragma unroll
             for (int i = 0; i < G::UPW; ++i) {
                 const int u = j * MT + i, m = u >> 1, h = u & 1;
-                tmem_st16(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[i]);
+                if (i >= PRE) {   // the rest of the units, decoded after the wait
+                    decode_word(v[i].x, o[i][0], o[i][1], o[i][2], o[i][3]);
+                    decode_word(v[i].y, o[i][4], o[i][5], o[i][6], o[i][7]);
+                    decode_word(v[i].z, o[i][8], o[i][9], o[i][10], o[i][11]);
+                    decode_word(v[i].w, o[i][12], o[i][13], o[i][14], o[i][15]);
+                }
+                tmem_st_unit(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[i]);
             }
             tmem_wait_st();
             tc_before();
@@ -620,8 +685,8 @@ __global__ void k_fill_pad(uint8_t* __restrict__ Gt, int32_t N, int64_t strideT,
     }
 }
 
-// row-major packed rows (stride bytes) -> tile-blocked layout, 16 bytes per thread;
-// rows >= nrows and bytes >= stride become 0xFF (genotype 0)
+// row-major packed rows (stride bytes) -> tile-blocked layout of tile codes, 16 bytes per
+// thread; rows >= nrows and bytes >= stride become PLINK 0xFF (genotype 0)
 __global__ void k_blockify(const uint8_t* __restrict__ src, int64_t nrows, int64_t stride, int64_t ntiles,
                            int64_t nch, uint8_t* __restrict__ dst) {
     const int64_t total = ntiles * nch * (BM * PKB / 16);
@@ -641,6 +706,7 @@ __global__ void k_blockify(const uint8_t* __restrict__ src, int64_t nrows, int64
                 v = *reinterpret_cast<const uint4*>(tmp);
             }
         }
+        v = make_uint4(recode_tile(v.x), recode_tile(v.y), recode_tile(v.z), recode_tile(v.w));
         const int64_t phys = (blkid * BM + r) * 2 + (h ^ ((r >> 2) & 1));   // halves swapped when bit 2 of r is set
         *reinterpret_cast<uint4*>(dst + phys * 16) = v;
     }

@@ -24,6 +24,17 @@ constexpr int NDIG = 9;           // digits per right-hand-side column (45 bits)
 constexpr int NDIG_HI = (NDIG + 1) / 2;
 constexpr int MAX_RHS_GROUP = 28; // 28 * 9 = 252 <= 256 MMA columns
 
+// The tile-blocked genotype copies hold "tile codes", 2 bits per genotype like the PLINK
+// codes they are made from (re-encoded once, by recode_tile):
+//   00 = genotype 2, 01 = genotype 1, 10 = genotype 0 or missing (11 is not produced).
+// With them the decode needs no shift for the odd codes of a word (see decode_word).
+__host__ __device__ __forceinline__ uint32_t recode_tile(uint32_t w) {
+    const uint32_t lo = w & 0x55555555u, hi = (w >> 1) & 0x55555555u;   // PLINK bit 0 / bit 1 of each code
+    return (hi & ~lo) | (lo << 1);                                      // 00->00, 10->01, 01->10, 11->10
+}
+// the PLINK code each tile code stands for (missing and genotype 0 share tile code 10)
+__host__ __device__ constexpr int tile_to_plink(int t) { return t == 0 ? 0 : (t == 1 ? 2 : 3); }
+
 __device__ __forceinline__ int kpos(int64_t i) {
     // K position of element i after the decode permutation within groups of 16
     const int q = (int)(i & 15);

@@ -1,5 +1,6 @@
 """CPU emulation of the tensor-core genotype product's data layout
-(globe_gb300/csrc/k_tc_geno.cu): the 2-bit -> e4m3 byte-permute decode, the
+(globe_gb300/csrc/k_tc_geno.cu): the PLINK -> tile-code recoding, the 2-bit ->
+e4m3 byte-permute decode (prmt with its sign-replicate mode), the
 K permutation it induces, base-16 digit slicing of the right-hand sides, the
 exact integer accumulation and the FP64 recombination -- checked against the
 oracle's FP64 GRM product.  Runs without a GPU."""
@@ -7,27 +8,37 @@ import numpy as np
 
 from helpers import cohort, rel
 
-LUT_G = 0x00380040
+LUT_A, LUT_B = 0x00003840, 0x00000038
 E4M3 = {0x00: 0.0, 0x38: 1.0, 0x40: 2.0}
 NDIG = 9      # balanced base-32 digits
 DBITS = 5
 
 
-def byte_perm(x, s):
-    """__byte_perm(x, 0, s) for selector nibbles 0..3 (bytes of x)."""
+def prmt(a, b, s):
+    """PTX prmt.b32 (default mode): selector nibble i of s[15:0] picks byte s&7 of {b, a};
+    with its top bit set, the picked byte's sign bit is replicated."""
+    src = a | (b << 32)
     out = 0
     for i in range(4):
-        sel = (s >> (4 * i)) & 0x7
-        b = (x >> (8 * sel)) & 0xFF if sel < 4 else 0
-        out |= b << (8 * i)
+        nib = (s >> (4 * i)) & 0xF
+        byte = (src >> (8 * (nib & 7))) & 0xFF
+        if nib & 8:
+            byte = 0xFF if byte & 0x80 else 0x00
+        out |= byte << (8 * i)
     return out
+
+
+def recode_tile(w):
+    """PLINK codes -> tile codes (00 = genotype 2, 01 = 1, 10 = 0 or missing)."""
+    lo, hi = w & 0x55555555, (w >> 1) & 0x55555555
+    return ((hi & ~lo) | (lo << 1)) & 0xFFFFFFFF
 
 
 def decode_word(w):
     e = w & 0x33333333
-    o = (w >> 2) & 0x33333333
-    return [byte_perm(LUT_G, e & 0xFFFF), byte_perm(LUT_G, (e >> 16) & 0xFFFF),
-            byte_perm(LUT_G, o & 0xFFFF), byte_perm(LUT_G, (o >> 16) & 0xFFFF)]
+    o = w & 0xCCCCCCCC
+    return [prmt(LUT_A, LUT_B, e), prmt(LUT_A, LUT_B, e >> 16),
+            prmt(LUT_A, LUT_B, o), prmt(LUT_A, LUT_B, o >> 16)]
 
 
 def kpos(i):
@@ -43,7 +54,7 @@ def decode_row(packed_row):
     words = b.view("<u4")
     out = []
     for w in words:
-        for r in decode_word(int(w)):
+        for r in decode_word(recode_tile(int(w))):
             out += [E4M3[(r >> (8 * i)) & 0xFF] for i in range(4)]
     return np.array(out)
 
@@ -113,3 +124,16 @@ def test_product_emulation_matches_oracle(orc):
         out[:, c] = np.ldexp(P2 @ (32.0 ** -np.arange(NDIG)), e) - 2 * (f * U[:, c]).sum()
     out *= 0.4 / Mk
     assert rel(out, s.grm_apply(Z)) < 1e-12
+
+
+def test_tile_code_decode_all_words():
+    """Every PLINK code in every position of a word decodes to its genotype (missing -> 0)."""
+    g_of = {0: 2.0, 1: 0.0, 2: 1.0, 3: 0.0}
+    rng = np.random.default_rng(0)
+    for w in [0, 0xFFFFFFFF, 0x55555555, 0xAAAAAAAA] + [int(x) for x in rng.integers(0, 2 ** 32, 2000)]:
+        out = decode_word(recode_tile(w))
+        vals = [E4M3[(r >> (8 * i)) & 0xFF] for r in out for i in range(4)]
+        # output order: r0 = genotypes 0,2,4,6; r1 = 8,10,12,14; r2 = 1,3,5,7; r3 = 9,11,13,15
+        order = [0, 2, 4, 6, 8, 10, 12, 14, 1, 3, 5, 7, 9, 11, 13, 15]
+        want = [g_of[(w >> (2 * q)) & 3] for q in order]
+        assert vals == want
