@@ -16,7 +16,8 @@
 // (|u 2^-e| < 16) and split into 9 balanced base-32 digits, so the digit
 // operand of column j is a table lookup on individual j's codes.  The MMAs
 // sum g * digit exactly in FP32, the digits are recombined in int64, and the
-// centring term sum_s 2 f_s u(s,j) is summed in FP64 from the same rounded u.
+// centring term sum_s 2 f_s u(s,j) is summed from the same rounded u (double-float per
+// thread, FP64 across threads).
 // Groups of 21 columns (189 digit rows, MMA N = 192) are the z dimension of
 // one k_tc_gemm launch; row tiles wholly above a group's first column are
 // skipped, so only the lower triangle is computed.
@@ -39,10 +40,11 @@ __global__ void k_grm_u4(const double* __restrict__ zs, const double* __restrict
 }
 
 // Per SNP s < kpad and tile code c: the 9 e4m3 digits of I = round(u 2^(40-e)) (bytes 0..8 of
-// dig[4s+c], most significant first) and 2 f_s u~ with u~ = I 2^(e-40) the rounded value.
+// dig[4s+c], most significant first) and 2 f_s u~ with u~ = I 2^(e-40) the rounded value, as a
+// float pair hi + lo (hi = the float nearest, lo = the float nearest the rest: ~48 bits).
 // SNPs >= Mk (padding of the K range) get zero digits and zero.
 __global__ void k_grm_table(const double* __restrict__ U4, const double* __restrict__ f, int64_t Mk, int64_t kpad,
-                            const double* __restrict__ info, uint4* __restrict__ dig, double* __restrict__ c2v) {
+                            const double* __restrict__ info, uint4* __restrict__ dig, float2* __restrict__ c2v) {
     const int e = (int)info[0];
     const double sc = ldexp(1.0, DBITS * (NDIG - 1) - e), back = ldexp(1.0, e - DBITS * (NDIG - 1));
     for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < 4 * kpad;
@@ -66,7 +68,8 @@ __global__ void k_grm_table(const double* __restrict__ U4, const double* __restr
             out.z = b[8];
         }
         dig[x] = out;
-        c2v[x] = cv;
+        const float hi = __double2float_rn(cv);
+        c2v[x] = make_float2(hi, __double2float_rn(cv - (double)hi));
     }
 }
 
@@ -80,8 +83,18 @@ __device__ __forceinline__ uint32_t dig_byte(const uint4& v, int j) {
 // decode order of the A operand (position P of a group of 16 holds SNP 2P for P < 8,
 // 2(P-8)+1 otherwise).  The codes come from the individual-major tile-blocked copy
 // (blk2, tile codes): 16 SNPs of individual i are one 32-bit word.  C2[jj] = sum_s 2 f_s u~(s, j).
+// (sh, sl) += (h, l) in double-float: Knuth's two-sum of the high parts, the rounding error and
+// the low parts into sl (GB300's FP32 pipe is many times its FP64 pipe)
+__device__ __forceinline__ void df_add(float& sh, float& sl, float h, float l) {
+    const float s = __fadd_rn(sh, h);
+    const float bp = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(h, bp));
+    sl = __fadd_rn(sl, __fadd_rn(err, l));
+    sh = s;
+}
+
 __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ blk2, int nch2, int32_t N, int jb,
-                                                    const uint4* __restrict__ dig, const double* __restrict__ c2v,
+                                                    const uint4* __restrict__ dig, const float2* __restrict__ c2v,
                                                     int64_t kpad, uint8_t* __restrict__ D, double* __restrict__ C2) {
     __shared__ double red[8];
     const int jj = blockIdx.x;
@@ -89,7 +102,7 @@ __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ 
     const int z = jj / GRM_KG, c = jj % GRM_KG;
     uint8_t* Dc = D + ((int64_t)z * GRM_NMMA + c * NDIG) * kpad;
     const int64_t nq = kpad >> 4;
-    double acc = 0.0;
+    float ah = 0.0f, al = 0.0f;
     if (j < N) {
         const int r = (int)(j & (BM - 1));
         const int64_t t = j / BM;
@@ -107,7 +120,8 @@ __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ 
                 const int m = P < 8 ? 2 * P : 2 * (P - 8) + 1;
                 const int64_t x = ((q << 4) + m) * 4 + ((w >> (2 * m)) & 3u);
                 const uint4 v = __ldg(dig + x);
-                acc += __ldg(c2v + x);
+                const float2 cv = __ldg(c2v + x);
+                df_add(ah, al, cv.x, cv.y);
 #pragma unroll
                 for (int d = 0; d < NDIG; ++d) o[d][P >> 2] |= dig_byte(v, d) << (8 * (P & 3));
             }
@@ -120,6 +134,7 @@ __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ 
 #pragma unroll
             for (int d = 0; d < NDIG; ++d) *reinterpret_cast<uint4*>(Dc + d * kpad + (q << 4)) = make_uint4(0, 0, 0, 0);
     }
+    double acc = (double)ah + (double)al;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
@@ -130,13 +145,13 @@ __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ 
     }
 }
 
-// A_ij = (2^e sum_d 32^-d P_d(i, j) - C2_j) / M rounded to float32, for the rows
+// A_ij = (2^e sum_d 32^-d P_d(i, j) - C2_j) (1/M) rounded to float32, for the rows
 // i = j0 + 32 blockIdx.x .. + 31 of group z = blockIdx.y (j0 = jb + z GRM_KG) and its
 // columns j <= i; written to lt[i(i+1)/2 + j].  Values pass through shared memory so the
 // row-contiguous writes of the packed triangle are coalesced.
 __global__ void __launch_bounds__(256) k_grm_combine(const float* __restrict__ part, int nsplit, int64_t ldp,
                                                      int64_t pz, int32_t N, int jb, const double* __restrict__ C2,
-                                                     const double* __restrict__ info, double M,
+                                                     const double* __restrict__ info, double inv_m,
                                                      float* __restrict__ lt) {
     __shared__ float sv[32][GRM_KG + 1];
     const int z = blockIdx.y;
@@ -151,7 +166,7 @@ __global__ void __launch_bounds__(256) k_grm_combine(const float* __restrict__ p
     for (int c = warp; c < GRM_KG; c += 8) {
         float v = 0.0f;
         if (i < N && j0 + c < N)
-            v = __double2float_rn((recombine(pzp, nsplit, GRM_NMMA, ldp, c, i, s_hi, s_lo) - C2[z * GRM_KG + c]) / M);
+            v = __double2float_rn((recombine(pzp, nsplit, GRM_NMMA, ldp, c, i, s_hi, s_lo) - C2[z * GRM_KG + c]) * inv_m);
         sv[lane][c] = v;
     }
     __syncthreads();
@@ -266,7 +281,8 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     const int G = (int)std::max<size_t>(1, gfit);
     const int nbr = 304;
     BuildBufs B(ctx);
-    double *U4, *c2v, *C2, *info, *pm, *ps;
+    double *U4, *C2, *info, *pm, *ps;
+    float2* c2v;
     uint4* dig;
     uint8_t* D;
     float* P;
@@ -312,7 +328,7 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
             GLOBE_RET(gemm_dispatch(ctx, GRM_NMMA, g.blk2, mB, N, nch, splits, P, ldp, err, zg));
         }
         k_grm_combine<<<dim3((unsigned)div_up(N - jb, 32), (unsigned)gb), 256, 0, ctx->stream>>>(
-            P, spe, ldp, pz, N, jb, C2, info, (double)g.Mk, lt);
+            P, spe, ldp, pz, N, jb, C2, info, 1.0 / (double)g.Mk, lt);
         GLOBE_LAUNCHED(ctx, "k_grm_combine");
     }
     return tc_check_error(ctx);
