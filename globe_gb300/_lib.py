@@ -39,7 +39,7 @@ class AiremlOpts(C.Structure):
     _fields_ = [("maxiter", C.c_int), ("tol", C.c_double), ("numMC", C.c_int), ("theta0", C.c_double * 5),
                 ("pcg_tol", C.c_double), ("pcg_maxit", C.c_int), ("precision", C.c_int), ("mask", C.c_int),
                 ("seed", C.c_uint64), ("probes", C.POINTER(C.c_double)), ("probes_len", C.c_int64),
-                ("fuse", C.c_int)]
+                ("fuse", C.c_int), ("digits", C.c_int)]
 
 
 class AiremlResult(C.Structure):
@@ -74,6 +74,8 @@ SIGNATURES = {
                                       _u8p, C.POINTER(BedInfo)]),
     "globe_load_grm": (C.c_int, [_vp, _fp, C.c_int32]),
     "globe_set_individuals": (C.c_int, [_vp, C.c_int32]),
+    "globe_set_digits": (C.c_int, [_vp, C.c_int]),
+    "globe_get_digits": (C.c_int, [_vp]),
     "globe_grm_build": (C.c_int, [_vp, _fp]),
     "globe_grm_build_dev": (C.c_int, [_vp, _vp]),
     "globe_write_grm": (C.c_int, [C.c_char_p, _fp, C.c_int32, C.c_char_p, C.c_int]),

@@ -172,6 +172,13 @@ class Context:
         no_time = self._L.globe_get_model(self.h) == L.MODEL_NO_TIME
         return (1 if no_time else 3) * self.N + self.Nrec
 
+    def set_digits(self, nd):
+        """Base-32 digits per column of the tensor-core product, 2..9 (default 9)."""
+        self._ck(self._L.globe_set_digits(self.h, nd))
+
+    def get_digits(self):
+        return int(self._L.globe_get_digits(self.h))
+
     def set_model(self, model):
         """MODEL_FULL (default) or MODEL_NO_TIME (components sig2e, sig2g only)."""
         self._ck(self._L.globe_set_model(self.h, model))
@@ -283,13 +290,15 @@ class Context:
 
     def aireml_run(self, theta0=(0.5, 0.3, 0.2, 0.1, 0.1), maxiter=50, tol=1e-3, numMC=15, pcg_tol=1e-5,
                    pcg_maxit=1000, precision=L.PREC_FP64, mask=False, seed=12345, probes=None, log_path=None,
-                   fuse=True):
+                   fuse=True, digits=0):
+        """digits: GLOBE_PREC_MIXED digits per column for this run (0: the context's, see set_digits)."""
         o = L.AiremlOpts()
         o.maxiter, o.tol, o.numMC = maxiter, tol, numMC
         for k in range(5):
             o.theta0[k] = theta0[k]
         o.pcg_tol, o.pcg_maxit, o.precision, o.mask, o.seed = pcg_tol, pcg_maxit, precision, int(mask), seed
         o.fuse = int(bool(fuse))
+        o.digits = int(digits)
         pr = None
         if probes is not None:
             pr = np.ascontiguousarray(probes, dtype=np.float64)

@@ -469,9 +469,8 @@ struct Driver {
 
 }  // namespace
 
-extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, const char* log_path,
-                                globe_aireml_result* res) {
-    if (!ctx || !o || !res) return GLOBE_ERR_ARG;
+static int aireml_run_impl(globe_ctx* ctx, const globe_aireml_opts* o, const char* log_path,
+                           globe_aireml_result* res) {
     if (o->numMC < 1 || o->maxiter < 0) return GLOBE_ERR_ARG;
     Driver d;
     d.ctx = ctx;
@@ -686,5 +685,18 @@ out:
     if (d.log.f) std::fclose(d.log.f);
     // restore the context's components to the final estimate
     if (rc == GLOBE_OK) globe_set_vc(ctx, theta);
+    return rc;
+}
+
+extern "C" int globe_aireml_run(globe_ctx* ctx, const globe_aireml_opts* o, const char* log_path,
+                                globe_aireml_result* res) {
+    if (!ctx || !o || !res) return GLOBE_ERR_ARG;
+    if (o->digits == 0) return aireml_run_impl(ctx, o, log_path, res);
+    // digits for this run only
+    const int keep = globe_get_digits(ctx);
+    int rc = globe_set_digits(ctx, o->digits);
+    if (rc != GLOBE_OK) return rc;
+    rc = aireml_run_impl(ctx, o, log_path, res);
+    globe_set_digits(ctx, keep);
     return rc;
 }

@@ -497,6 +497,15 @@ int globe_set_model(globe_ctx* ctx, int model) {
 
 int globe_get_model(const globe_ctx* ctx) { return ctx ? ctx->model : GLOBE_MODEL_FULL; }
 
+int globe_set_digits(globe_ctx* ctx, int nd) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (nd < 2 || nd > 9) return set_err(ctx, GLOBE_ERR_ARG, "digits per column must be in [2, 9], got %d", nd);
+    ctx->digits = nd;
+    return GLOBE_OK;
+}
+
+int globe_get_digits(const globe_ctx* ctx) { return ctx ? ctx->digits : 9; }
+
 int globe_set_precision(globe_ctx* ctx, int precision) {
     if (!ctx) return GLOBE_ERR_ARG;
     if (precision != GLOBE_PREC_FP64 && precision != GLOBE_PREC_MIXED)

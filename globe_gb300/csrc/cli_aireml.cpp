@@ -17,7 +17,8 @@
 // runAIREML reads only a dense GRM.
 // Each gradient evaluation solves the MME right-hand sides and the probes as
 // one block PCG (globe_aireml_eval); --separateSolves solves them one after
-// the other, as the reference does.
+// the other, as the reference does.  --digits <n> (with --precision mixed):
+// base-32 digits per column of the tensor-core product (globe_set_digits).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -55,7 +56,7 @@ int main(int argc, char** argv) {
     }
     std::string input = argv[1], grm = argv[2], outp = argv[3], probes_file, geno;
     float min_maf = 0.01f, max_miss = 0.2f;   // runPCGsolver's defaults (PCGsolver.cpp:34-35)
-    int fuse = 1;
+    int fuse = 1, digits = 0;
     int maxiter = 50, numMC = 15, precision = GLOBE_PREC_FP64, device = 0;
     float tol = 1e-3f;
 #ifdef GLOBE_NO_TIME
@@ -85,6 +86,7 @@ int main(int argc, char** argv) {
         else if (a == "--probes" && has) probes_file = argv[++i];
         else if (a == "--geno" && has) geno = argv[++i];
         else if (a == "--separateSolves") fuse = 0;
+        else if (a == "--digits" && has) digits = std::atoi(argv[++i]);
         else if (a == "--minMAF" && has) min_maf = std::strtof(argv[++i], nullptr);
         else if (a == "--maxMissingRate" && has) max_miss = std::strtof(argv[++i], nullptr);
         else {
@@ -165,6 +167,7 @@ int main(int argc, char** argv) {
     o.mask = 0;
     o.seed = seed;
     o.fuse = fuse;
+    o.digits = digits;
     o.probes = probes.empty() ? nullptr : probes.data();
     o.probes_len = (int64_t)probes.size();
     globe_aireml_result r{};

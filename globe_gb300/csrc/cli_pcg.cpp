@@ -4,7 +4,8 @@
 //
 // Extra flags (absent from the reference): --precision fp64|mixed,
 // --pcgTol <v> (default 1e-5, PCGsolver.cpp:54), --pcgMaxIter <n> (1000),
-// --device <id>, --save64 (also write <out>_*.f64.bin with float64 payloads).
+// --device <id>, --save64 (also write <out>_*.f64.bin with float64 payloads),
+// --digits <n> (with --precision mixed: base-32 digits per column, globe_set_digits).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -18,7 +19,7 @@ static void usage(const char* prog) {
                  "Usage:\n%s --input <file> --output <prefix>  --sig2e <val> --sig2g <val> --sig2b0 <val> "
                  "--sigb01 <val> --sig2b1 <val>\n  EITHER:  --geno <plinkPrefix>\n      OR:  --grm <grmPrefix>\n"
                  " Optional:\n   [--debug] [--minMAF val] [--maxMissingRate val]\n"
-                 "   [--precision fp64|mixed] [--pcgTol val] [--pcgMaxIter n] [--device id] [--save64]\n",
+                 "   [--precision fp64|mixed] [--pcgTol val] [--pcgMaxIter n] [--device id] [--save64] [--digits n]\n",
                  prog);
 }
 
@@ -46,7 +47,7 @@ int main(int argc, char** argv) {
     float vc_f[5] = {0.1f, 0.1f, 0.1f, 0.1f, 0.1f};
     bool have[5] = {false, false, false, false, false};
     const char* vcflag[5] = {"--sig2e", "--sig2g", "--sig2b0", "--sigb01", "--sig2b1"};
-    int precision = GLOBE_PREC_FP64, device = 0, maxit = 1000;
+    int precision = GLOBE_PREC_FP64, device = 0, maxit = 1000, digits = 0;
     double tol = 1e-5;
     bool have_in = false, have_out = false;
     for (int i = 1; i < argc; ++i) {
@@ -93,6 +94,9 @@ int main(int argc, char** argv) {
         } else if (a == "--device") {
             if (!next(&v)) return EXIT_FAILURE;
             device = std::atoi(v.c_str());
+        } else if (a == "--digits") {
+            if (!next(&v)) return EXIT_FAILURE;
+            digits = std::atoi(v.c_str());
         } else {
             int k = -1;
             for (int q = 0; q < 5; ++q)
@@ -131,6 +135,7 @@ int main(int argc, char** argv) {
         globe_destroy(ctx);
         return EXIT_FAILURE;
     };
+    if (digits && globe_set_digits(ctx, digits)) return die("digits");
     if (globe_load_records(ctx, Nrec, N, p, indiv.data(), X.data(), y.data())) return die("records");
     if (!geno.empty()) {
         // streamed from disk in chunks (globe_load_bed_file): the file never sits whole in host memory

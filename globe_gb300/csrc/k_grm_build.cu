@@ -159,14 +159,14 @@ __global__ void __launch_bounds__(256) k_grm_combine(const float* __restrict__ p
     const int64_t i0 = j0 + (int64_t)blockIdx.x * 32;
     if (j0 >= N || i0 >= N) return;
     double s_hi, s_lo;
-    recombine_scales((int)info[0], s_hi, s_lo);
+    recombine_scales<NDIG>((int)info[0], s_hi, s_lo);
     const float* pzp = part + z * pz;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t i = i0 + lane;
     for (int c = warp; c < GRM_KG; c += 8) {
         float v = 0.0f;
         if (i < N && j0 + c < N)
-            v = __double2float_rn((recombine(pzp, nsplit, GRM_NMMA, ldp, c, i, s_hi, s_lo) - C2[z * GRM_KG + c]) * inv_m);
+            v = __double2float_rn((recombine<NDIG>(pzp, nsplit, GRM_NMMA, ldp, c, i, s_hi, s_lo) - C2[z * GRM_KG + c]) * inv_m);
         sv[lane][c] = v;
     }
     __syncthreads();

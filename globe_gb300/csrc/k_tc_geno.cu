@@ -550,19 +550,19 @@ __global__ void k_col_finish(const double* __restrict__ pmax, const double* __re
 }
 
 
-// digits of X (n x k, FP64) into D[(c*NDIG + j) * kpad + kpos(r)]  (e4m3); every position
+// ND digits of X (n x k, FP64) into D[(c*ND + j) * kpad + kpos(r)]  (e4m3); every position
 // in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
 // fills 4 consecutive positions P..P+3 (a 32-bit word): within a group of 16, position
 // P < 8 holds row 2P and P >= 8 holds row 2(P-8)+1 (the inverse of kpos).
-// x 2^-e is rounded once to the integer I = round(x 2^-e 32^(NDIG-1)), |I| < 2^44; its
+// x 2^-e is rounded once to the integer I = round(x 2^-e 32^(ND-1)), |I| <= 2^(5 ND - 1); its
 // balanced base-32 digits are peeled off from the least significant end in integer
 // arithmetic (d = ((I + 16) mod 32) - 16, in [-16, 15]); the leading digit is what
-// remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (NDIG-1) fraction bits.
-
+// remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (ND-1) fraction bits.
+template <int ND>
 __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
                          uint8_t* __restrict__ D, int64_t kpad) {
     const int c = blockIdx.y;
-    const double sc = ldexp(1.0, DBITS * (NDIG - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
+    const double sc = ldexp(1.0, DBITS * (ND - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
     const int64_t nw = kpad >> 2;
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t P = w << 2, base = P & ~(int64_t)15;
@@ -574,13 +574,13 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
             const int64_t src = base + (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1);
             I[q] = src < n ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
         }
-        uint32_t word[NDIG];
+        uint32_t word[ND];
 #pragma unroll
-        for (int j = 0; j < NDIG; ++j) word[j] = 0;
+        for (int j = 0; j < ND; ++j) word[j] = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
 #pragma unroll
-            for (int j = NDIG - 1; j > 0; --j) {
+            for (int j = ND - 1; j > 0; --j) {
                 const int d = (int)((I[q] + DHALF) & (2 * DHALF - 1)) - DHALF;
                 I[q] = (I[q] - d) >> DBITS;   // exact: I - d is a multiple of 32
                 word[j] |= e4m3_int(d) << (8 * q);
@@ -588,11 +588,12 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
             word[0] |= e4m3_int((int)I[q]) << (8 * q);
         }
 #pragma unroll
-        for (int j = 0; j < NDIG; ++j) *reinterpret_cast<uint32_t*>(D + ((int64_t)c * NDIG + j) * kpad + P) = word[j];
+        for (int j = 0; j < ND; ++j) *reinterpret_cast<uint32_t*>(D + ((int64_t)c * ND + j) * kpad + P) = word[j];
     }
 }
 
 // pass-1 epilogue in FP64: u[s,c] = inv_s^2 (2^e_c sum_j 32^-j P1 - 2 f_s S_c); partial max|u|, sum 2 f u
+template <int ND>
 __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int64_t rows, int k,
                            const double* __restrict__ colinfo, const double* __restrict__ f,
                            const double* __restrict__ inv, double* __restrict__ U, double* __restrict__ pmax,
@@ -600,11 +601,11 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
     __shared__ double smx[32], ssm[32];
     const int c = blockIdx.y;
     double s_hi, s_lo;
-    recombine_scales((int)colinfo[2 * c], s_hi, s_lo);
+    recombine_scales<ND>((int)colinfo[2 * c], s_hi, s_lo);
     const double Sc = colinfo[2 * c + 1];
     double mx = 0, sm = 0;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < rows; s += (int64_t)gridDim.x * blockDim.x) {
-        const double gv = recombine(part, nsplit, nmma, ldp, c, s, s_hi, s_lo);
+        const double gv = recombine<ND>(part, nsplit, nmma, ldp, c, s, s_hi, s_lo);
         const double iv = inv[s], fs = f[s];
         const double u = iv * iv * (gv - 2.0 * fs * Sc);
         U[s + c * rows] = u;
@@ -632,14 +633,15 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
 }
 
 // pass-2 epilogue: out[i,c] = scale (2^e_c sum_j 32^-j P2 - C2_c)
+template <int ND>
 __global__ void k_combine2(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int64_t rows, int k,
                            const double* __restrict__ colinfo, double scale, double* __restrict__ out, int64_t ldo) {
     const int c = blockIdx.y;
     double s_hi, s_lo;
-    recombine_scales((int)colinfo[2 * c], s_hi, s_lo);
+    recombine_scales<ND>((int)colinfo[2 * c], s_hi, s_lo);
     const double C2 = colinfo[2 * c + 1];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-        out[i + c * ldo] = scale * (recombine(part, nsplit, nmma, ldp, c, i, s_hi, s_lo) - C2);
+        out[i + c * ldo] = scale * (recombine<ND>(part, nsplit, nmma, ldp, c, i, s_hi, s_lo) - C2);
     }
 }
 
@@ -868,11 +870,12 @@ static int pick_splits(globe_ctx* ctx, int tiles, int nchunks) {
     return best;
 }
 
-// out (N x k) = scale * Zs'(Zs Z) for one group of <= MAX_RHS_GROUP columns
+// out (N x k) = scale * Zs'(Zs Z) for one group of <= 256 / ND columns, ND digits per column
+template <int ND>
 static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, double* out) {
     auto& g = ctx->gen;
     const int32_t N = ctx->coh.N;
-    const int nmma = ((kg * NDIG + 15) / 16) * 16;
+    const int nmma = ((kg * ND + 15) / 16) * 16;
     // ---- pass 1 operands
     const int nch1 = g.nch1;
     const int64_t kpad1 = (int64_t)nch1 * BK;
@@ -908,10 +911,10 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col1);
     GLOBE_LAUNCHED(ctx, "k_col_finish");
     // digit rows past the kg columns stay zero
-    if (nmma > kg * NDIG)
-        GLOBE_CK(ctx, cudaMemsetAsync(D1 + (size_t)kg * NDIG * kpad1, 0, (size_t)(nmma - kg * NDIG) * kpad1,
+    if (nmma > kg * ND)
+        GLOBE_CK(ctx, cudaMemsetAsync(D1 + (size_t)kg * ND * kpad1, 0, (size_t)(nmma - kg * ND) * kpad1,
                                       ctx->stream));
-    k_digits<<<dim3((unsigned)std::min<int64_t>(div_up(kpad1 / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
+    k_digits<ND><<<dim3((unsigned)std::min<int64_t>(div_up(kpad1 / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
         Z, N, N, kg, col1, D1, kpad1);
     GLOBE_LAUNCHED(ctx, "k_digits");
     // ---- pass 1
@@ -920,15 +923,15 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
         GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, ZGrid()));
     }
     const int sp1e = eff_splits(nch1, sp1);
-    k_combine1<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
+    k_combine1<ND><<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
     GLOBE_LAUNCHED(ctx, "k_combine1");
     k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col2);
     GLOBE_LAUNCHED(ctx, "k_col_finish");
     // ---- digits of u, pass 2
-    if (nmma > kg * NDIG)
-        GLOBE_CK(ctx, cudaMemsetAsync(D2 + (size_t)kg * NDIG * kpad2, 0, (size_t)(nmma - kg * NDIG) * kpad2,
+    if (nmma > kg * ND)
+        GLOBE_CK(ctx, cudaMemsetAsync(D2 + (size_t)kg * ND * kpad2, 0, (size_t)(nmma - kg * ND) * kpad2,
                                       ctx->stream));
-    k_digits<<<dim3((unsigned)std::min<int64_t>(div_up(kpad2 / 4, 256), 2048), kg), 256, 0, ctx->stream>>>(
+    k_digits<ND><<<dim3((unsigned)std::min<int64_t>(div_up(kpad2 / 4, 256), 2048), kg), 256, 0, ctx->stream>>>(
         U, g.Mk, g.Mk, kg, col2, D2, kpad2);
     GLOBE_LAUNCHED(ctx, "k_digits");
     {
@@ -936,10 +939,24 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
         GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, mB2, N, nch2, sp2, P2, ldp2, err, ZGrid()));
     }
     const int sp2e = eff_splits(nch2, sp2);
-    k_combine2<<<dim3(div_up(N, 256) < 1024 ? div_up(N, 256) : 1024, kg), 256, 0, ctx->stream>>>(
+    k_combine2<ND><<<dim3(div_up(N, 256) < 1024 ? div_up(N, 256) : 1024, kg), 256, 0, ctx->stream>>>(
         P2, sp2e, nmma, ldp2, N, kg, col2, scale, out, N);
     GLOBE_LAUNCHED(ctx, "k_combine2");
     return GLOBE_OK;
+}
+
+static int tc_group_nd(globe_ctx* ctx, int nd, const double* Z, int kg, double scale, double* out) {
+    switch (nd) {
+        case 2: return tc_group<2>(ctx, Z, kg, scale, out);
+        case 3: return tc_group<3>(ctx, Z, kg, scale, out);
+        case 4: return tc_group<4>(ctx, Z, kg, scale, out);
+        case 5: return tc_group<5>(ctx, Z, kg, scale, out);
+        case 6: return tc_group<6>(ctx, Z, kg, scale, out);
+        case 7: return tc_group<7>(ctx, Z, kg, scale, out);
+        case 8: return tc_group<8>(ctx, Z, kg, scale, out);
+        case 9: return tc_group<9>(ctx, Z, kg, scale, out);
+    }
+    return set_err(ctx, GLOBE_ERR_ARG, "unsupported digit count %d", nd);
 }
 
 int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out) {
@@ -950,14 +967,17 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
         return GLOBE_OK;
     }
     GLOBE_RET(ensure_gt(ctx));
-    // near-equal groups of <= MAX_RHS_GROUP columns.  Groups wider than 21 (NMMA > 192)
-    // run one row tile per CTA, which costs more per column than two groups of two
-    // tiles once k > MAX_RHS_GROUP: then groups of <= 21 (e.g. 65 -> 17 + 16 + 16 + 16).
-    int ng = (k + MAX_RHS_GROUP - 1) / MAX_RHS_GROUP;
-    if (ng > 1) ng = (k + 20) / 21;
+    const int nd = ctx->digits;
+    // near-equal groups of <= 256 / nd columns (MMA width <= 256).  Groups wider than
+    // 192 / nd (MMA width > 192) run one row tile per CTA, which costs more per column than
+    // two groups of two tiles once k > 256 / nd: then groups of <= 192 / nd columns
+    // (at 9 digits: 28 and 21; 65 -> 17 + 16 + 16 + 16).
+    const int gmax = 256 / nd, gtwo = 192 / nd;
+    int ng = (k + gmax - 1) / gmax;
+    if (ng > 1) ng = (k + gtwo - 1) / gtwo;
     for (int gi = 0, c0 = 0; gi < ng; ++gi) {
         const int kg = k / ng + (gi < k % ng ? 1 : 0);
-        GLOBE_RET(tc_group(ctx, Z + (size_t)c0 * N, kg, scale, out + (size_t)c0 * N));
+        GLOBE_RET(tc_group_nd(ctx, nd, Z + (size_t)c0 * N, kg, scale, out + (size_t)c0 * N));
         c0 += kg;
     }
     return GLOBE_OK;

@@ -20,9 +20,8 @@ constexpr int BK = 128;           // K elements per stage (one 128-byte swizzle 
 constexpr int PKB = BK / 4;       // packed bytes per row per stage
 constexpr int DBITS = 5;          // digit base 32
 constexpr int DHALF = 1 << (DBITS - 1);   // 16: digits in [-16, 16]
-constexpr int NDIG = 9;           // digits per right-hand-side column (45 bits)
-constexpr int NDIG_HI = (NDIG + 1) / 2;
-constexpr int MAX_RHS_GROUP = 28; // 28 * 9 = 252 <= 256 MMA columns
+constexpr int NDIG = 9;           // digits per right-hand-side column by default (45 bits)
+constexpr int MIN_DIG = 2;        // fewest digits a context may ask for (globe_set_digits)
 
 // The tile-blocked genotype copies hold "tile codes", 2 bits per genotype like the PLINK
 // codes they are made from (re-encoded once, by recode_tile):
@@ -45,31 +44,35 @@ __device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], exact
     return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
 }
 
-// 2^e sum_j 32^-j P_j of one row.  Every FP32 partial is an exact integer (|P| < 2^24), so
-// the split partials are summed in int64 and the digits combined in two exact int64 halves
-// (hi = digits 0..4, lo = digits 5..8); the only rounding is the final FP64 addition.
+// 2^e sum_j 32^-j P_j of one row, ND digits per column (rows c*ND + j of the partials).
+// Every FP32 partial is an exact integer (|P| < 2^24), so the split partials are summed in
+// int64 and the digits combined in two exact int64 halves (hi = digits 0..ND_HI-1, lo = the
+// rest); the only rounding is the final FP64 addition.
+template <int ND>
 __device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
                                            int64_t row, double s_hi, double s_lo) {
-    long long pj[NDIG];
+    constexpr int NH = (ND + 1) / 2;
+    long long pj[ND];
 #pragma unroll
-    for (int j = 0; j < NDIG; ++j) pj[j] = (long long)__float2int_rn(part[((int64_t)c * NDIG + j) * ldp + row]);
+    for (int j = 0; j < ND; ++j) pj[j] = (long long)__float2int_rn(part[((int64_t)c * ND + j) * ldp + row]);
     for (int y = 1; y < nsplit; ++y) {
 #pragma unroll
-        for (int j = 0; j < NDIG; ++j)
-            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * NDIG + j) * ldp + row]);
+        for (int j = 0; j < ND; ++j)
+            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * ND + j) * ldp + row]);
     }
     long long hi = 0, lo = 0;
 #pragma unroll
-    for (int j = 0; j < NDIG_HI; ++j) hi = hi * (1 << DBITS) + pj[j];
+    for (int j = 0; j < NH; ++j) hi = hi * (1 << DBITS) + pj[j];
 #pragma unroll
-    for (int j = NDIG_HI; j < NDIG; ++j) lo = lo * (1 << DBITS) + pj[j];
+    for (int j = NH; j < ND; ++j) lo = lo * (1 << DBITS) + pj[j];
     return (double)hi * s_hi + (double)lo * s_lo;
 }
 
-// scale factors of recombine for exponent e: 2^(e - 5 (NDIG_HI - 1)) and 2^(e - 5 (NDIG - 1))
+// scale factors of recombine<ND> for exponent e: 2^(e - 5 (ND_HI - 1)) and 2^(e - 5 (ND - 1))
+template <int ND>
 __device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_lo) {
-    s_hi = ldexp(1.0, e - DBITS * (NDIG_HI - 1));
-    s_lo = ldexp(1.0, e - DBITS * (NDIG - 1));
+    s_hi = ldexp(1.0, e - DBITS * ((ND + 1) / 2 - 1));
+    s_lo = ldexp(1.0, e - DBITS * (ND - 1));
 }
 
 // per-column max |x| and sum over n rows (partials per CTA); colinfo[c] = {exponent e with

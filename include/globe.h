@@ -193,6 +193,17 @@ int globe_get_model(const globe_ctx* ctx);
  * PCG / MME / AIREML calls take the precision from their options. */
 int globe_set_precision(globe_ctx* ctx, int precision);
 
+/* GLOBE_PREC_MIXED rounds each right-hand-side column once to nd balanced
+ * base-32 digits (2 <= nd <= 9, default 9) and multiplies every digit exactly:
+ * a column x becomes x rounded to a multiple of 2^-(5(nd-1)+4) max|x| (both
+ * passes round their input this way), so each product column is within a few
+ * times that unit of the exact product (nd = 9: ~1e-13, nd = 6: ~5e-9,
+ * nd = 5: ~1.5e-7, the reference's own FP32 level).  Fewer digits
+ * mean fewer tensor-core columns: 20 columns take MMA width 192 at nd = 9 and
+ * 128 at nd = 6.  No reference counterpart (the reference works in FP32). */
+int globe_set_digits(globe_ctx* ctx, int nd);
+int globe_get_digits(const globe_ctx* ctx);
+
 /* ---- operators -------------------------------------------------------- */
 
 /* out (N x k) = sig2g * A * Z for Z (N x k): the GRM product of
@@ -303,6 +314,8 @@ typedef struct {
     int64_t probes_len;
     int fuse;          /* 1: one block solve of MME + probes per gradient evaluation
                           (globe_aireml_eval); 0: two solves, as the reference */
+    int digits;        /* GLOBE_PREC_MIXED: base-32 digits per column for this run
+                          (globe_set_digits); 0 keeps the context's setting */
 } globe_aireml_opts;
 
 typedef struct {

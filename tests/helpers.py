@@ -77,3 +77,40 @@ def f32_ulps(a, b):
         i = np.ascontiguousarray(x, np.float32).view(np.int32).astype(np.int64)
         return np.where(i < 0, -(i & 0x7FFFFFFF), i)
     return np.abs(key(a) - key(b))
+
+
+def tc_digits(col, nd):
+    """nd balanced base-32 digits of a column as k_digits forms them (rows: digit j), and the
+    column's exponent e: I = round(x 2^-e 32^(nd-1)) with |x 2^-e| < 16."""
+    col = np.asarray(col, np.float64)
+    mx = np.abs(col).max()
+    e = (np.frexp(mx)[1] - 4) if mx > 0 else -4
+    I = np.rint(np.ldexp(col, 5 * (nd - 1) - e)).astype(np.int64)
+    D = np.zeros((nd, len(col)))
+    for j in range(nd - 1, 0, -1):
+        d = ((I + 16) & 31) - 16
+        D[j] = d
+        I = (I - d) >> 5
+    assert np.all(np.abs(I) <= 16)
+    D[0] = I
+    return D, e
+
+
+def tc_product_emulation(G, f, inv, Z, scale, nd):
+    """The tensor-core GRM product with nd digits per column, in exact arithmetic:
+    G = kept genotypes (Mk x N, missing as 0), f / inv_std per SNP.  Pass 1 forms
+    u = inv^2 (G d(Z) - 2 f sum Z), pass 2 out = scale (G' d(u) - sum 2 f u), where d()
+    is the column rounded to nd base-32 digits."""
+    G = np.asarray(G, np.float64)
+    w = 32.0 ** -np.arange(nd)
+    U = np.zeros((G.shape[0], Z.shape[1]))
+    for c in range(Z.shape[1]):
+        D, e = tc_digits(Z[:, c], nd)
+        P = G @ D.T                                   # exact integers
+        U[:, c] = inv ** 2 * (np.ldexp(P @ w, e) - 2 * f * Z[:, c].sum())
+    out = np.zeros_like(Z, dtype=np.float64)
+    for c in range(Z.shape[1]):
+        D, e = tc_digits(U[:, c], nd)
+        P = G.T @ D.T
+        out[:, c] = scale * (np.ldexp(P @ w, e) - (2 * f * U[:, c]).sum())
+    return out

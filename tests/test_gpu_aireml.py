@@ -87,3 +87,22 @@ def test_loop_fused_and_separate_agree(gctx, case):
     b = gctx.aireml_run(fuse=False, **kw)
     assert a["iterations"] == b["iterations"]
     assert rel(a["theta"], b["theta"]) < 1e-6
+
+
+def test_loop_with_fewer_digits(orc):
+    """AIREML on genotypes with 6 base-32 digits per column (GLOBE_PREC_MIXED) follows the
+    9-digit and the FP64 runs to well inside the estimate's Monte-Carlo accuracy, and
+    leaves the context's own digit setting alone."""
+    from helpers import cohort
+    coh = cohort(41, 400, 1500, recs=("uniform", 2, 8), miss=0.02)
+    th0 = (0.5, 0.3, 0.2, 0.1, 0.1)
+    out = {}
+    with G.Context(0) as ctx:
+        ctx.load_records(coh["indiv"].astype(np.int32), coh["X"], coh["y"], coh["N"])
+        ctx.load_bed(coh["packed"])
+        for name, prec, nd in (("fp64", G.PREC_FP64, 0), ("d9", G.PREC_MIXED, 0), ("d6", G.PREC_MIXED, 6)):
+            out[name] = ctx.aireml_run(theta0=th0, maxiter=8, numMC=5, precision=prec, seed=7, digits=nd)
+            assert ctx.get_digits() == 9
+    for name in ("d9", "d6"):
+        assert out[name]["iterations"] == out["fp64"]["iterations"]
+        assert rel(out[name]["theta"], out["fp64"]["theta"]) < 1e-5, name

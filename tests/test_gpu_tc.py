@@ -108,3 +108,39 @@ def test_dense_mixed_matches_fp64(gctx, orc, N):
             assert max(rel(got[:, c], ref[:, c]) for c in range(k)) < 1e-11, k
     finally:
         gctx.set_precision(G.PREC_FP64)
+
+
+@pytest.mark.parametrize("nd", [2, 3, 4, 5, 6, 7, 8, 9])
+def test_digit_count_matches_exact_emulation(gctx, orc, nd):
+    """With nd digits per column the product is the exact product of the nd-digit-rounded
+    columns: equal to its CPU emulation up to FP64 rounding, for one group of 20 columns
+    (MMA width round16(20 nd)) and for a width that splits into groups."""
+    from helpers import tc_product_emulation
+    indiv, X, y, N, packed = _case("odd", (9, 131, 257, ("uniform", 1, 6), 0.03))
+    s = _load(gctx, orc, indiv, X, y, N, packed)
+    alt, miss, maf, _, keep = orc.bed_stats(packed, N)
+    Gk = synth.unpack_genotypes(packed[keep], N)
+    Gk = np.where(Gk < 0, 0, Gk)
+    rng = np.random.default_rng(nd)
+    assert gctx.get_digits() == 9
+    try:
+        gctx.set_precision(G.PREC_MIXED)
+        gctx.set_digits(nd)
+        for k in (20, 256 // nd + 3):
+            Z = rng.standard_normal((N, k)) * np.logspace(-2, 2, k)
+            got = gctx.grm_apply(Z)
+            emu = tc_product_emulation(Gk, s.f, s.inv_std, Z, VC_F[1] / keep.sum(), nd)
+            assert max(rel(got[:, c], emu[:, c]) for c in range(k)) < 1e-11, k
+            # and the error against the exact product is the digit rounding's
+            ref = s.grm_apply(Z)
+            assert max(rel(got[:, c], ref[:, c]) for c in range(k)) < 16 * 2.0 ** -(5 * (nd - 1) + 4) + 1e-12
+    finally:
+        gctx.set_digits(9)
+        gctx.set_precision(G.PREC_FP64)
+
+
+def test_digit_count_arguments(gctx):
+    for bad in (0, 1, 10):
+        with pytest.raises(G.GlobeError):
+            gctx.set_digits(bad)
+    assert gctx.get_digits() == 9

@@ -137,3 +137,21 @@ def test_tile_code_decode_all_words():
         order = [0, 2, 4, 6, 8, 10, 12, 14, 1, 3, 5, 7, 9, 11, 13, 15]
         want = [g_of[(w >> (2 * q)) & 3] for q in order]
         assert vals == want
+
+
+def test_digit_count_error_bound(orc):
+    """The product with nd digits per column (CPU emulation) is within a few times the
+    rounding unit 2^-(5(nd-1)+4) of the exact product, column by column."""
+    from globe_gb300 import synth
+    from helpers import tc_product_emulation
+    coh = cohort(31, 77, 150, recs=("uniform", 1, 3), miss=0.05, edge=True)
+    N = coh["N"]
+    s = orc.Solver(coh["indiv"], coh["X"], coh["y"], N, (0.6, 0.4, 0.4, 0.2, 0.2), packed=coh["packed"])
+    alt, miss, maf, _, keep = orc.bed_stats(coh["packed"], N)
+    Gk = synth.unpack_genotypes(coh["packed"][keep], N)
+    Gk = np.where(Gk < 0, 0, Gk)
+    Z = np.random.default_rng(5).standard_normal((N, 3)) * np.array([1.0, 1e-3, 40.0])
+    ref = s.grm_apply(Z)
+    for nd in range(2, 10):
+        out = tc_product_emulation(Gk, s.f, s.inv_std, Z, 0.4 / keep.sum(), nd)
+        assert max(rel(out[:, c], ref[:, c]) for c in range(3)) < 8 * 2.0 ** -(5 * (nd - 1) + 4), nd
