@@ -797,10 +797,12 @@ static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB
     const int cps = (nchunks + splits - 1) / splits;
     splits = (nchunks + cps - 1) / cps;
     const size_t smem = sizeof(Smem<NMMA, G::MT>) + 1024;
-    static bool attr = false;
-    if (!attr) {
+    // the shared-memory opt-in is a per-device attribute of the kernel
+    static std::atomic<uint64_t> attr_set{0};
+    const uint64_t bit = 1ull << (ctx->device & 63);
+    if (!(attr_set.load() & bit)) {
         GLOBE_CK(ctx, cudaFuncSetAttribute(k_tc_gemm<NMMA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
+        attr_set.fetch_or(bit);
     }
     dim3 grid((unsigned)((rows + G::MT * BM - 1) / (G::MT * BM)), (unsigned)splits, (unsigned)zg.nz);
     k_tc_gemm<NMMA><<<grid, G::NTHREADS, smem, ctx->stream>>>(blk, mB, rows, nchunks, cps, part, ldp, zg.pz,

@@ -8,6 +8,7 @@
 #include <cuda_fp8.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "internal.cuh"
