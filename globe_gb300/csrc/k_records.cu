@@ -911,9 +911,8 @@ int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double
     double* part;
     GLOBE_RET(ws(ctx, WS_GPART, (size_t)nb * numMC * 5, &part));
     size_t sm = sizeof(double) * RB_WARPS * numMC * 5;
-    if (sm > 48 * 1024) {
-        cudaFuncSetAttribute(k_trace_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    }
+    if (sm > 48 * 1024)
+        GLOBE_CK(ctx, cudaFuncSetAttribute(k_trace_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_trace_terms<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(),
                                                        1.0 / ctx->vc[1], VR, UH, TY, numMC, part);
     GLOBE_LAUNCHED(ctx, "k_trace_terms");
