@@ -16,7 +16,7 @@ GRM on the packed genotypes + the PCG vector updates).  ``value`` is the
 device-resident throughput; ``e2e`` is the same through globe_pcg with pinned
 host buffers (B copied in, X copied out inside the timed region).
 
-The same run also reports AIREML time to converge (numMC=15, tol 1e-3, same
+The same run also reports AIREML time to converge (numMC=15, 32 for c5; tol 1e-3, same
 probes for both precisions): ``aireml`` on this workload with the selected
 precision, and ``aireml_mixed_vs_fp64`` on a smaller cohort (N=20k, M=20k)
 where the plain FP64 path also finishes in seconds.  The phenotype's genetic
@@ -61,7 +61,7 @@ CONFIGS = {
                label="N=200k indiv, M=300k 2-bit SNPs (15 GB), 1.2M records, k=65 RHS"),
     # biobank shape: 60 GB of packed genotypes, geometric record counts 1-200
     "c5": dict(N=400_000, M=600_000, recs=("geometric", 0.1, 1, 200), T=15.0, maf_lo=0.01, maf_hi=0.5, miss=0.02,
-               label="N=400k indiv, M=600k 2-bit SNPs (60 GB), ~4M records (geometric 1-200), k=5 RHS"),
+               numMC=32, label="N=400k indiv, M=600k 2-bit SNPs (60 GB), ~4M records (geometric 1-200), k=5 RHS"),
     "c1": dict(N=2_000, M=10_000, recs=("uniform", 3, 10), T=5.0, maf_lo=0.05, maf_hi=0.5, miss=0.01,
                label="N=2000 indiv, M=10k SNPs, ~13k records, k=5"),
 }
@@ -468,14 +468,15 @@ def run_ours(args, cfg):
         fp64 = {"value": u64 / (t64 / 1000.0), "unit": "RHS*iters/s", "ms_per_iteration": t64 / 2,
                 "speedup_of_mixed": value / (u64 / (t64 / 1000.0))}
 
-    # AIREML time to converge on this workload (genotype GRM, numMC=15, tol 1e-3) -- replicas skip it
+    # AIREML time to converge on this workload (genotype GRM, numMC from the config, tol 1e-3) -- replicas skip it
     aireml = None
     if not args.no_aireml and world == 1:
+        numMC = int(cfg.get("numMC", 15))
         runs = {}
         for nd in ((AIREML_DIGITS, 9) if prec == G.PREC_MIXED and not dense else (0,)):
             barrier()
             t0 = time.perf_counter()
-            r = ctx.aireml_run(theta0=AIREML_THETA0, maxiter=50, tol=1e-3, numMC=15, precision=prec, seed=SEED,
+            r = ctx.aireml_run(theta0=AIREML_THETA0, maxiter=50, tol=1e-3, numMC=numMC, precision=prec, seed=SEED,
                                digits=nd)
             runs[nd] = (time.perf_counter() - t0, r)
         nd0 = next(iter(runs))
@@ -484,7 +485,7 @@ def run_ours(args, cfg):
                   "precision": args.precision, "digits": nd0 or None,
                   "seconds_to_converge": t_air, "converged": bool(r["converged"]), "iterations": r["iterations"],
                   "grad_evals": r["grad_evals"], "pcg_rhs_iters": r["pcg_rhs_iters"],
-                  "theta": [float(v) for v in r["theta"]], "numMC": 15, "tol": 1e-3}
+                  "theta": [float(v) for v in r["theta"]], "numMC": numMC, "tol": 1e-3}
         if 9 in runs and nd0 != 9:
             t9, r9 = runs[9]
             aireml["nine_digits"] = {"seconds_to_converge": t9, "iterations": r9["iterations"],
