@@ -144,3 +144,61 @@ def test_digit_count_arguments(gctx):
         with pytest.raises(G.GlobeError):
             gctx.set_digits(bad)
     assert gctx.get_digits() == 9
+
+
+def _synth_cohort(gctx, N, M, seed):
+    """Genotypes from the device generator (copied back for the oracle) and a one-record-
+    per-individual table; returns (indiv, X, y, packed)."""
+    torch = pytest.importorskip("torch")
+    bps = (N + 3) // 4
+    stride = (bps + 15) // 16 * 16
+    raw = torch.empty((M, stride), dtype=torch.uint8, device="cuda")
+    gctx.synth_bed_dev(raw.data_ptr(), M, N, stride, seed, 0.01, 0.5, 0.02)
+    packed = raw[:, :bps].cpu().numpy()
+    del raw
+    rng = np.random.default_rng(seed)
+    indiv = np.arange(N, dtype=np.int32)
+    X = np.asfortranarray(np.column_stack([np.ones(N), rng.standard_normal(N), rng.uniform(0, 5, N)]))
+    return indiv, X, rng.standard_normal(N), packed
+
+
+def test_k_range_split_beyond_one_cta(gctx, orc):
+    """M = 600k SNPs: pass 2 sums over 600k SNPs, more than the 2^19 products one CTA may
+    accumulate exactly in FP32, so its K range is split across CTAs; the product stays exact."""
+    N, M = 1000, 600_000
+    indiv, X, y, packed = _synth_cohort(gctx, N, M, 123)
+    s = _load(gctx, orc, indiv, X, y, N, packed)
+    Z = np.random.default_rng(1).standard_normal((N, 3)) * np.array([1.0, 1e-2, 1e2])
+    try:
+        gctx.set_precision(G.PREC_MIXED)
+        got = gctx.grm_apply(Z)
+    finally:
+        gctx.set_precision(G.PREC_FP64)
+    ref = s.grm_apply(Z)
+    assert max(rel(got[:, c], ref[:, c]) for c in range(3)) < 1e-11
+
+
+def test_mid_size_properties(gctx):
+    """N = 20k, M = 40k (12 K-stages per CTA, hundreds of CTAs): the mixed product is symmetric
+    and linear to FP64 rounding and matches the FP64 GPU product."""
+    N, M = 20_000, 40_000
+    indiv, X, y, packed = _synth_cohort(gctx, N, M, 321)
+    gctx.load_records(indiv, X, y, N)
+    gctx.load_bed(packed)
+    gctx.set_vc(VC_F)
+    rng = np.random.default_rng(2)
+    Z = rng.standard_normal((N, 5))
+    try:
+        gctx.set_precision(G.PREC_MIXED)
+        AZ = gctx.grm_apply(Z)
+        # symmetry: x'(A y) = (A x)'y for every pair of columns
+        S = Z.T @ AZ
+        assert np.abs(S - S.T).max() < 1e-11 * np.abs(S).max()
+        # linearity: A(2 z0 - z1) = 2 A z0 - A z1
+        comb = gctx.grm_apply(np.column_stack([2 * Z[:, 0] - Z[:, 1]]))[:, 0]
+        assert rel(comb, 2 * AZ[:, 0] - AZ[:, 1]) < 1e-11
+        gctx.set_precision(G.PREC_FP64)
+        ref = gctx.grm_apply(Z)
+    finally:
+        gctx.set_precision(G.PREC_FP64)
+    assert max(rel(AZ[:, c], ref[:, c]) for c in range(5)) < 1e-11
