@@ -43,8 +43,9 @@ extern "C" {
 /* precision of the GRM product inside the solver */
 #define GLOBE_PREC_FP64 0   /* plain FP64 everywhere (the drop-in path) */
 #define GLOBE_PREC_MIXED 1  /* genotype GRM product on the FP8 tensor cores with exact
-                               base-32 digit slicing of the right-hand sides (45 bits,
-                               matches FP64 to ~1e-13); dense GRM in double-float FP32
+                               base-32 digit slicing of the right-hand sides (9 digits =
+                               45 bits by default, matches FP64 to ~1e-13; see
+                               globe_set_digits); dense GRM in double-float FP32
                                arithmetic (~48 bits) */
 
 /* models (globe_set_model) */
