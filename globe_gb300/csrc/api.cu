@@ -322,9 +322,14 @@ int globe_set_individuals(globe_ctx* ctx, int32_t N) {
     return GLOBE_OK;
 }
 
-int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf,
-                       float max_miss, int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep,
-                       globe_bed_info* info) {
+}  // extern "C"
+
+namespace globe {
+
+// statistics, filter and compaction of the kept SNP rows; the tile-blocked layout follows
+// separately (ensure_gt), after the callers have released their staging copies
+int load_bed_rows(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf, float max_miss,
+                  int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep, globe_bed_info* info) {
     if (!ctx) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     const int32_t N = ctx->coh.N;
@@ -402,6 +407,19 @@ int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t 
     return GLOBE_OK;
 }
 
+}  // namespace globe
+
+extern "C" {
+
+int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf,
+                       float max_miss, int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep,
+                       globe_bed_info* info) {
+    int rc = load_bed_rows(ctx, d_bed, M, stride, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
+    // the tile-blocked copies every genotype kernel reads; the compacted rows are freed
+    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_gt(ctx);
+    return rc;
+}
+
 int globe_load_bed(globe_ctx* ctx, const uint8_t* bed, int64_t M, float min_maf, float max_miss,
                    int64_t* alt_count, int64_t* miss_count, float* maf, float* miss_rate, uint8_t* keep,
                    globe_bed_info* info) {
@@ -426,7 +444,7 @@ int globe_load_bed(globe_ctx* ctx, const uint8_t* bed, int64_t M, float min_maf,
         cudaError_t e = cudaMemcpyAsync(d_bed, bed, (size_t)M * bps, cudaMemcpyHostToDevice, ctx->stream);
         if (e != cudaSuccess) { rc = cuda_err(ctx, e, "copy .bed payload"); goto done; }
     }
-    rc = globe_load_bed_dev(ctx, d_bed, M, bps, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
+    rc = load_bed_rows(ctx, d_bed, M, bps, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
     if (rc == GLOBE_OK && M > 0) {
         cudaError_t e = cudaSuccess;
         if (alt_count && e == cudaSuccess) e = cudaMemcpyAsync(alt_count, d_alt, 8 * M, cudaMemcpyDeviceToHost, ctx->stream);
@@ -440,6 +458,8 @@ int globe_load_bed(globe_ctx* ctx, const uint8_t* bed, int64_t M, float min_maf,
 done:
     cudaStreamSynchronize(ctx->stream);
     for (void* p : {(void*)d_bed, (void*)d_alt, (void*)d_miss, (void*)d_maf, (void*)d_mr, (void*)d_keep}) dfree(ctx, p);
+    // tile-blocked layout once the staging copy of the payload is gone
+    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_gt(ctx);
     return rc;
 }
 

@@ -7,7 +7,8 @@
 // the host-to-device copy overlap and host memory stays at two chunks.  The
 // rows then go through the same statistics, filter and compaction as
 // globe_load_bed_dev (prepGenotypeInput, PCGsolver.cpp:615-763, which reads
-// the whole file serially).
+// the whole file serially).  The tile-blocked layout is built after the file's
+// device copy is released.
 #include <cstdio>
 #include <string>
 
@@ -87,7 +88,7 @@ extern "C" int globe_load_bed_file(globe_ctx* ctx, const char* prefix, float min
         }
         used[b] = true;
     }
-    rc = globe_load_bed_dev(ctx, d_bed, M, stride, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
+    rc = load_bed_rows(ctx, d_bed, M, stride, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
     if (rc == GLOBE_OK && M > 0) {
         cudaError_t e = cudaSuccess;
         if (alt_count && e == cudaSuccess) e = cudaMemcpyAsync(alt_count, d_alt, 8 * M, cudaMemcpyDeviceToHost, ctx->stream);
@@ -106,5 +107,7 @@ done:
         if (host[b]) cudaFreeHost(host[b]);
     }
     for (void* p : {(void*)d_bed, (void*)d_alt, (void*)d_miss, (void*)d_maf, (void*)d_mr, (void*)d_keep}) dfree(ctx, p);
+    // tile-blocked layout once the file's device copy is gone
+    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_gt(ctx);
     return rc;
 }

@@ -233,6 +233,8 @@ int dense_diag(globe_ctx* ctx, double* d);
 
 // k_tc_geno.cu
 int ensure_gt(globe_ctx* ctx);
+int load_bed_rows(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf, float max_miss,
+                  int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep, globe_bed_info* info);
 int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 int tc_check_error(globe_ctx* ctx);
 

@@ -179,8 +179,9 @@ __global__ void __launch_bounds__(256) k_grm_combine(const float* __restrict__ p
 
 // FP64: one CTA per 64 x 64 tile (ti, tj), tj <= ti, of the lower triangle; 256 threads,
 // thread (ty, tx) holds rows ti*64 + ty + 16a and columns tj*64 + tx + 16b.  K runs over
-// the SNP-major kept rows in chunks of 32 SNPs staged as zs values in shared memory.
-__global__ void __launch_bounds__(256) k_grm_f64(const uint8_t* __restrict__ geno, int64_t Mk, int64_t stride,
+// the SNP-major tile-blocked rows (blk1, tile codes) in chunks of 32 SNPs staged as zs
+// values in shared memory.
+__global__ void __launch_bounds__(256) k_grm_f64(const uint8_t* __restrict__ blk, int64_t Mk, int nch,
                                                  const double* __restrict__ zs, int32_t N, double M,
                                                  float* __restrict__ lt) {
     __shared__ double As[32][64], Bs[32][64];
@@ -209,8 +210,8 @@ __global__ void __launch_bounds__(256) k_grm_f64(const uint8_t* __restrict__ gen
                 const int64_t ind = base + l8 + q;
                 double v = 0.0;
                 if (s < Mk && ind < N) {
-                    const unsigned code = (geno[s * stride + (ind >> 2)] >> (2 * (ind & 3))) & 3u;
-                    v = zs[s * 4 + code];
+                    const unsigned code = (blk[blk_offset(s, ind >> 2, nch)] >> (2 * (ind & 3))) & 3u;
+                    v = zs[s * 4 + tile_to_plink((int)code)];
                 }
                 dst[ls][l8 + q] = v;
             }
@@ -340,8 +341,9 @@ static int grm_build_f64(globe_ctx* ctx, float* lt) {
     const int64_t nt = (N + 63) / 64;
     const int64_t ntiles = nt * (nt + 1) / 2;
     if (ntiles > 0x7FFFFFFFll) return set_err(ctx, GLOBE_ERR_ARG, "N too large for the FP64 GRM build");
+    GLOBE_RET(ensure_gt(ctx));
     ProfScope p(ctx, GLOBE_PROF_GRM_BUILD_GEMM);
-    k_grm_f64<<<(unsigned)ntiles, 256, 0, ctx->stream>>>(g.geno, g.Mk, g.stride, g.zs, N, (double)g.Mk, lt);
+    k_grm_f64<<<(unsigned)ntiles, 256, 0, ctx->stream>>>(g.blk1, g.Mk, g.nch1, g.zs, N, (double)g.Mk, lt);
     GLOBE_LAUNCHED(ctx, "k_grm_f64");
     return GLOBE_OK;
 }

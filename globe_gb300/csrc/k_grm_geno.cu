@@ -3,23 +3,25 @@
 //   out (N x k) = scale * Zs' (Zs Z),  zs(s,i) = (g - 2 f_s) inv_std_s,
 //   missing -> g = 0, scale = sig2g / M            (PCGsolver.cpp:1130-1201)
 //
-// Pass 1 (w = Zs Z): one warp per SNP row; lanes stream 16-byte chunks of
-// the packed row (64 samples each).  Pass 2 (Zs' w): a CTA owns 128
-// consecutive samples (32 bytes of every SNP row), stages SNP tiles in
-// shared memory and splits the SNP range across CTAs (partials reduced in a
-// fixed order).  zs per SNP is a 4-entry table indexed by the 2-bit code, so
-// the decode is a select, not arithmetic.  FP64 throughput bounds both passes.
-#include "internal.cuh"
+// The genotypes are read from the SNP-major tile-blocked copy of the
+// tensor-core path (blk1, tile codes; the only SNP-major copy kept).
+// Pass 1 (w = Zs Z): one warp per SNP row; lanes stream 16-byte pieces of
+// the row (64 samples each).  Pass 2 (Zs' w): a CTA owns 128 consecutive
+// samples (one 32-byte chunk of every SNP row), stages SNP tiles in shared
+// memory and splits the SNP range across CTAs (partials reduced in a fixed
+// order).  zs per SNP is a table indexed by the 2-bit code, so the decode is a
+// select, not arithmetic.  FP64 throughput bounds both passes.
+#include "tc_common.cuh"
 
 namespace globe {
 
 __device__ __forceinline__ double zsel(unsigned code, double t0, double t1, double t2) {
-    // code 00 -> t0 (g=2), 10 -> t2 (g=1), 01 / 11 -> t1 (g=0)
-    return (code & 1u) ? t1 : (code ? t2 : t0);
+    // tile code 00 -> t0 (g=2), 01 -> t2 (g=1), 10 / 11 -> t1 (g=0 or missing)
+    return code == 0u ? t0 : (code == 1u ? t2 : t1);
 }
 
 template <int KC>
-__global__ void __launch_bounds__(256) k_geno_p1(const uint8_t* __restrict__ geno, int64_t stride, int64_t Mk,
+__global__ void __launch_bounds__(256) k_geno_p1(const uint8_t* __restrict__ blk, int nch, int64_t Mk,
                                                  int32_t N, const double* __restrict__ zs,
                                                  const double* __restrict__ Z, int64_t ldz, int kc,
                                                  double* __restrict__ W, int64_t ldw) {
@@ -27,13 +29,12 @@ __global__ void __launch_bounds__(256) k_geno_p1(const uint8_t* __restrict__ gen
     const int64_t s = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (s >= Mk) return;
     const double t0 = zs[4 * s], t1 = zs[4 * s + 1], t2 = zs[4 * s + 2];
-    const uint4* row = reinterpret_cast<const uint4*>(geno + s * stride);
     const int nchunks = (N + 63) >> 6;
     double acc[KC];
 #pragma unroll
     for (int c = 0; c < KC; ++c) acc[c] = 0.0;
     for (int q = lane; q < nchunks; q += 32) {
-        const uint4 v = __ldg(row + q);
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(blk + tc::blk_offset(s, (int64_t)q << 4, nch)));
         const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
         const int i0 = q << 6;
 #pragma unroll
@@ -65,7 +66,7 @@ constexpr int P2_TS = 64;        // SNPs per shared-memory tile
 
 // SQUARE: accumulate zs^2 (genetic diagonal) instead of zs * W.
 template <int KC, bool SQUARE>
-__global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restrict__ geno, int64_t stride,
+__global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restrict__ blk, int nch,
                                                         int64_t Mk, int32_t N, const double* __restrict__ zs,
                                                         const double* __restrict__ W, int64_t ldw, int kc,
                                                         int64_t s_per, double* __restrict__ part) {
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restric
     __shared__ double wt[P2_TS][KC > 0 ? KC : 1];
     const int tid = threadIdx.x;
     const int64_t i = (int64_t)blockIdx.x * P2_THREADS + tid;
-    const int64_t byte0 = (int64_t)blockIdx.x * 32;
+    const int64_t byte0 = (int64_t)blockIdx.x * 32;   // this CTA's 32-byte chunk of every row
     const int64_t s_beg = (int64_t)blockIdx.y * s_per;
     int64_t s_end = s_beg + s_per;
     if (s_end > Mk) s_end = Mk;
@@ -88,9 +89,8 @@ __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restric
         {   // 64 rows x 32 bytes, 16 bytes per thread
             const int rs = tid >> 1, half = tid & 1;
             uint4 v = make_uint4(0, 0, 0, 0);
-            const int64_t off = byte0 + half * 16;
-            if (rs < ns && off < stride)
-                v = __ldg(reinterpret_cast<const uint4*>(geno + (s0 + rs) * stride + off));
+            if (rs < ns)
+                v = __ldg(reinterpret_cast<const uint4*>(blk + tc::blk_offset(s0 + rs, byte0 + half * 16, nch)));
             *reinterpret_cast<uint4*>(&gb[rs][half * 16]) = v;
         }
         for (int e = tid; e < P2_TS * 4; e += P2_THREADS) {
@@ -151,13 +151,13 @@ static int geno_chunk(globe_ctx* ctx, const double* Z, int kc, double scale, dou
     const int32_t N = ctx->coh.N;
     {
         ProfScope ps(ctx, GLOBE_PROF_GRM_PASS1);
-        k_geno_p1<KC><<<div_up(g.Mk, 8), 256, 0, ctx->stream>>>(g.geno, g.stride, g.Mk, N, g.zs, Z, N, kc, W, g.Mk);
+        k_geno_p1<KC><<<div_up(g.Mk, 8), 256, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, Z, N, kc, W, g.Mk);
         GLOBE_LAUNCHED(ctx, "k_geno_p1");
     }
     dim3 grid(div_up(N, P2_THREADS), nsplit);
     {
         ProfScope ps(ctx, GLOBE_PROF_GRM_PASS2);
-        k_geno_p2<KC, false><<<grid, P2_THREADS, 0, ctx->stream>>>(g.geno, g.stride, g.Mk, N, g.zs, W, g.Mk, kc,
+        k_geno_p2<KC, false><<<grid, P2_THREADS, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, W, g.Mk, kc,
                                                                     s_per, part);
         GLOBE_LAUNCHED(ctx, "k_geno_p2");
     }
@@ -176,6 +176,7 @@ int geno_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double*
         GLOBE_CK(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)N * k, ctx->stream));
         return GLOBE_OK;
     }
+    GLOBE_RET(ensure_gt(ctx));
     const int kcmax = 8;
     int kc0 = k < kcmax ? k : kcmax;
     double* W;
@@ -207,6 +208,7 @@ int geno_diag(globe_ctx* ctx, double* d) {
         GLOBE_CK(ctx, cudaMemsetAsync(d, 0, sizeof(double) * N, ctx->stream));
         return GLOBE_OK;
     }
+    GLOBE_RET(ensure_gt(ctx));
     int64_t ctas_x = div_up(N, P2_THREADS);
     int nsplit = pick_splits(ctas_x, g.Mk);
     int64_t s_per = ((g.Mk + nsplit - 1) / nsplit + P2_TS - 1) / P2_TS * P2_TS;
@@ -214,7 +216,7 @@ int geno_diag(globe_ctx* ctx, double* d) {
     double* part;
     GLOBE_RET(ws(ctx, WS_GPART, (size_t)nsplit * N, &part));
     dim3 grid((unsigned)ctas_x, nsplit);
-    k_geno_p2<1, true><<<grid, P2_THREADS, 0, ctx->stream>>>(g.geno, g.stride, g.Mk, N, g.zs, nullptr, 0, 1,
+    k_geno_p2<1, true><<<grid, P2_THREADS, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, nullptr, 0, 1,
                                                               s_per, part);
     GLOBE_LAUNCHED(ctx, "k_geno_diag");
     // A_ii = (1/M) sum_s zs^2   (PCGsolver.cpp:986-988)

@@ -762,12 +762,19 @@ static int blockify(globe_ctx* ctx, const uint8_t* src, int64_t nrows, int64_t s
     return GLOBE_OK;
 }
 
+// The two tile-blocked copies (blk1 SNP-major, blk2 individual-major) from the compacted
+// SNP-major rows, which are freed afterwards: every genotype kernel reads the tile-blocked
+// copies.  Order: blk1, then the individual-major staging copy, then the rows are freed
+// before blk2 is laid out, so at most three copies are resident at once.
 int ensure_gt(globe_ctx* ctx) {
     auto& g = ctx->gen;
     if (g.blk2) return GLOBE_OK;
+    if (!g.geno) return set_err(ctx, GLOBE_ERR_STATE, "no genotype rows to lay out");
     const int32_t N = ctx->coh.N;
+    if (!g.blk1) GLOBE_RET(blockify(ctx, g.geno, g.Mk, g.stride, &g.blk1, &g.nch1, &g.ntiles1));
     g.strideT = ((g.Mk + 3) / 4 + PKB - 1) / PKB * PKB;
     if (g.strideT < PKB) g.strideT = PKB;
+    if (g.gt) dfree(ctx, g.gt);   // a staging copy left by an earlier failed attempt
     GLOBE_RET(dalloc(ctx, &g.gt, (size_t)N * g.strideT));
     const int64_t snp_bytes = (g.Mk + 3) / 4;
     if (g.Mk > 0) {
@@ -782,7 +789,9 @@ int ensure_gt(globe_ctx* ctx) {
         k_fill_pad<<<1024, 256, 0, ctx->stream>>>(g.gt, N, g.strideT, from);
         GLOBE_LAUNCHED(ctx, "k_fill_pad");
     }
-    GLOBE_RET(blockify(ctx, g.geno, g.Mk, g.stride, &g.blk1, &g.nch1, &g.ntiles1));
+    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    dfree(ctx, g.geno);   // the compacted rows live on as blk1
+    g.geno = nullptr;
     GLOBE_RET(blockify(ctx, g.gt, N, g.strideT, &g.blk2, &g.nch2, &g.ntiles2));
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
     dfree(ctx, g.gt);   // the row-major individual-major copy is only a staging step

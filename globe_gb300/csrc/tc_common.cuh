@@ -35,6 +35,17 @@ __host__ __device__ __forceinline__ uint32_t recode_tile(uint32_t w) {
 // the PLINK code each tile code stands for (missing and genotype 0 share tile code 10)
 __host__ __device__ constexpr int tile_to_plink(int t) { return t == 0 ? 0 : (t == 1 ? 2 : 3); }
 
+// Byte b of row `row` in a tile-blocked copy with nch 32-byte chunks per row: block (row / 128,
+// b / 32) of 128 rows x 32 bytes, the two 16-byte halves of a row swapped when bit 2 of the row
+// (within its tile) is set.
+__host__ __device__ __forceinline__ int64_t blk_offset(int64_t row, int64_t b, int nch) {
+    const int64_t t = row >> 7;
+    const int r = (int)(row & 127);
+    const int w = (int)(b & 31);
+    const int h = (w >> 4) ^ ((r >> 2) & 1);
+    return (((t * nch + (b >> 5)) * 128 + r) * 32) + h * 16 + (w & 15);
+}
+
 __device__ __forceinline__ int kpos(int64_t i) {
     // K position of element i after the decode permutation within groups of 16
     const int q = (int)(i & 15);

@@ -76,3 +76,22 @@ def test_streamed_file_errors(gctx, tmp_path):
     with pytest.raises(G.GlobeError) as e:
         gctx.load_bed_file(str(tmp_path / "missing"))
     assert e.value.code == -4
+
+
+def test_resident_genotype_copies():
+    """After loading, the genotypes are held as the two tile-blocked copies only (SNP-major
+    and individual-major); the compacted row-major copy and the staging buffers are gone."""
+    c = cohort(17, 2000, 10000, recs=("uniform", 3, 10), miss=0.01)
+    N = c["N"]
+    with Context(0) as ctx:
+        ctx.load_records(c["indiv"].astype(np.int32), c["X"], c["y"], N)
+        before = ctx.device_bytes()
+        st = ctx.load_bed(c["packed"])
+        grew = ctx.device_bytes() - before
+        Mk = int(st["kept"])
+        # tiles of 128 rows x 32 bytes, row counts rounded to 512 (a CTA's four tiles)
+        blk1 = -(-Mk // 512) * 512 * (-(-((N + 3) // 4) // 32) * 32)
+        blk2 = -(-N // 512) * 512 * (-(-((Mk + 3) // 4) // 32) * 32)
+        tables = Mk * 8 * 6 + N * 8          # zs (4), f, inv per SNP; genetic diagonal
+        assert grew <= blk1 + blk2 + tables + (1 << 20)
+        assert grew >= blk1 + blk2
