@@ -91,3 +91,19 @@ def test_runaireml_geno_matches_grm_input(tmp_path):
         th[name] = _final_theta(out + ".log")
     assert rel(th["geno"], th["dense"]) < 1e-4          # float32 rounding of the .grm.bin
     assert rel(th["geno_mixed"], th["geno"]) < 1e-6
+
+
+def test_runpcgsolver_digits_flag(tmp_path):
+    """--precision mixed --digits 6: the solve matches the FP64 reference to the product's
+    ~5e-9 rounding (amplified by the solve), well inside the FP32 program's accuracy."""
+    c = golden_case("geno_small")
+    out = os.path.join(str(tmp_path), "d")
+    exe = os.path.join(BIN, "runPCGsolver")
+    base = [exe, "--input", c["prefix"] + ".txt", "--output", out, "--geno", c["prefix"], "--save64",
+            "--pcgTol", "1e-13", "--precision", "mixed"] + VCARGS
+    r = _run(base + ["--digits", "6"])
+    assert r.returncode == 0, r.stderr
+    for v in ("beta", "uhat", "bhat"):
+        assert rel(G.read_vector("%s_%s.f64.bin" % (out, v)), c["ref"]["geno64_" + v]) < 1e-6, v
+    r = _run(base + ["--digits", "12"])
+    assert r.returncode != 0 and "digits" in r.stderr
