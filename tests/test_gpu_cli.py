@@ -107,3 +107,22 @@ def test_runpcgsolver_digits_flag(tmp_path):
         assert rel(G.read_vector("%s_%s.f64.bin" % (out, v)), c["ref"]["geno64_" + v]) < 1e-6, v
     r = _run(base + ["--digits", "12"])
     assert r.returncode != 0 and "digits" in r.stderr
+
+
+@pytest.mark.parametrize("prog", ["runAIREML", "runAIREML_reducedModel"])
+def test_aireml_on_built_grm_matches_geno(tmp_path, prog):
+    """The .grm.bin that buildGRM writes is the matrix --geno applies: AIREML on it follows
+    AIREML on the genotypes to the float32 rounding of the file, for both models."""
+    c = golden_case("geno_small")
+    g = os.path.join(str(tmp_path), "g")
+    r = _run([os.path.join(BIN, "buildGRM"), c["prefix"], g])
+    assert r.returncode == 0, r.stderr
+    common = ["--numMC", "5", "--maxiter", "6", "--seed", "5", "--pcgTol", "1e-10"]
+    th = {}
+    for name, grm_arg, extra in (("built", g, []), ("geno", "-", ["--geno", c["prefix"]])):
+        out = os.path.join(str(tmp_path), name)
+        r = _run([os.path.join(BIN, prog), c["prefix"] + ".txt", grm_arg, out] + common + extra)
+        assert r.returncode == 0, r.stderr
+        th[name] = _final_theta(out + ".log")
+    assert len(th["geno"]) == (5 if prog == "runAIREML" else 2)
+    assert rel(th["built"], th["geno"]) < 1e-5
