@@ -857,12 +857,8 @@ int eff_splits(int nchunks, int splits) {
 // 3907 stages gives 10 splits (1960 CTAs, 12.9 waves on 152 SMs) where aiming at ~8 waves
 // gave 7 (1372 CTAs, 9.03 waves: a tenth wave of 4 CTAs).
 static int pick_splits(globe_ctx* ctx, int tiles, int nchunks) {
-    static int sms = 0;
-    if (sms == 0) {
-        int v = 0;
-        sms = (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, ctx->device) == cudaSuccess && v > 0) ? v
-                                                                                                             : 152;
-    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || sms < 1) sms = 152;
     constexpr int CTA_COST = 8;                       // fixed cost of a CTA, in stages
     const int lo = std::max(1, (nchunks + 4095) / 4096);
     const int hi = std::max(lo, std::min(64, nchunks / 8));
