@@ -415,8 +415,11 @@ static int mme_rhs(globe_ctx* ctx, double* B) {
     return GLOBE_OK;
 }
 
-// From ctx->vinv_X = V^-1 [X y]: beta, V^-1 r, u-hat, b-hat (fitMME, varCompEst.cpp:587-685)
-static int mme_finish(globe_ctx* ctx, double* beta, double* uhat, double* bhat, double* vinv_r) {
+// From ctx->vinv_X = V^-1 [X y]: beta, V^-1 r, u-hat, b-hat (fitMME, varCompEst.cpp:587-685).
+// with_uhat = false leaves u-hat to the caller (the fused AIREML evaluation forms it in one
+// GRM product with the probes' u-hat); the MME is then not marked complete.
+static int mme_finish(globe_ctx* ctx, double* beta, double* uhat, double* bhat, double* vinv_r,
+                      bool with_uhat = true) {
     auto& c = ctx->coh;
     const int64_t n = c.Nrec;
     const int32_t N = c.N;
@@ -442,8 +445,10 @@ static int mme_finish(globe_ctx* ctx, double* beta, double* uhat, double* bhat, 
     double *Zi, *S1, *dbhat;
     GLOBE_RET(ws(ctx, WS_ZI, (size_t)N, &Zi));
     GLOBE_RET(ws(ctx, WS_S1, (size_t)N, &S1));
-    GLOBE_RET(seg_sums(ctx, ctx->vinv_r, nullptr, nullptr, nullptr, nullptr, 1, Zi, S1));
-    GLOBE_RET(grm_apply_dev(ctx, Zi, 1, ctx->uhat));
+    if (with_uhat) {
+        GLOBE_RET(seg_sums(ctx, ctx->vinv_r, nullptr, nullptr, nullptr, nullptr, 1, Zi, S1));
+        GLOBE_RET(grm_apply_dev(ctx, Zi, 1, ctx->uhat));
+    }
     GLOBE_RET(ws(ctx, WS_BHAT, (size_t)2 * N, &dbhat));
     GLOBE_RET(bhat_kernel(ctx, ctx->vinv_r, dbhat));
     if (beta) std::memcpy(beta, b.data(), sizeof(double) * p1);
@@ -451,7 +456,7 @@ static int mme_finish(globe_ctx* ctx, double* beta, double* uhat, double* bhat, 
     if (bhat) GLOBE_CK(ctx, cudaMemcpyAsync(bhat, dbhat, sizeof(double) * 2 * N, cudaMemcpyDeviceToHost, ctx->stream));
     if (vinv_r) GLOBE_CK(ctx, cudaMemcpyAsync(vinv_r, ctx->vinv_r, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    ctx->mme_ok = true;
+    ctx->mme_ok = with_uhat;
     return GLOBE_OK;
 }
 
@@ -480,8 +485,10 @@ static int grad_check(globe_ctx* ctx, int numMC) {
 
 // Probes Y_v ~ N(0, V*) and TY = V*^-1 Y (the PCG start), sample_Yvs and
 // estimateTrace_PdV (varCompEst.cpp:775-862)
+// VR and UH have one leading column more than the probes (VR0 / UH0): the fused evaluation
+// puts V^-1 r there and gets u-hat from the same GRM product as the probes' u-hat.
 struct ProbeBufs {
-    double *Y, *TY, *VR, *UH, *Hs;
+    double *Y, *TY, *VR, *UH, *Hs, *VR0, *UH0;
 };
 
 static int grad_probes(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, ProbeBufs& pb) {
@@ -489,8 +496,10 @@ static int grad_probes(globe_ctx* ctx, const double* probes, int numMC, uint64_t
     const int32_t N = ctx->coh.N;
     GLOBE_RET(ws(ctx, WS_TMP1, (size_t)n * numMC, &pb.Y));
     GLOBE_RET(ws(ctx, WS_TMP2, (size_t)n * numMC, &pb.TY));
-    GLOBE_RET(ws(ctx, WS_TMP4, (size_t)n * numMC, &pb.VR));
-    GLOBE_RET(ws(ctx, WS_UH, (size_t)N * numMC, &pb.UH));
+    GLOBE_RET(ws(ctx, WS_TMP4, (size_t)n * (numMC + 1), &pb.VR0));
+    GLOBE_RET(ws(ctx, WS_UH, (size_t)N * (numMC + 1), &pb.UH0));
+    pb.VR = pb.VR0 + n;
+    pb.UH = pb.UH0 + N;
     GLOBE_RET(ws(ctx, WS_HSTAR, (size_t)N * 4, &pb.Hs));
     if (probes) {
         double* dd;
@@ -508,26 +517,39 @@ static int grad_probes(globe_ctx* ctx, const double* probes, int numMC, uint64_t
 }
 
 // From the MME (V^-1 r, u-hat) and VY = V^-1 Y: f_theta, the first-order terms, the
-// Monte-Carlo trace and the score (computeDerivative_first, varCompEst.cpp:693-1012)
+// Monte-Carlo trace and the score (computeDerivative_first, varCompEst.cpp:693-1012).
+// with_uhat: u-hat is not formed yet; it comes out of the probes' GRM product (column 0 of
+// VR0 / UH0).  Every column of a GRM product is computed on its own, so the values are the
+// same as from two products.
 static int grad_finish(globe_ctx* ctx, int numMC, const double* VY, const ProbeBufs& pb, double* f_theta,
-                       double* first, double* trace, double* grad) {
+                       double* first, double* trace, double* grad, bool with_uhat = false) {
     auto& c = ctx->coh;
     const int64_t n = c.Nrec;
     const int32_t N = c.N;
     if (!ctx->f_theta) GLOBE_RET(dalloc(ctx, &ctx->f_theta, (size_t)n * 5));
     double* fth = ctx->f_theta;
+    GLOBE_RET(project_dev(ctx, VY, numMC, pb.VR));
+    double *Zi, *S1;
+    GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * (numMC + 1), &Zi));
+    GLOBE_RET(ws(ctx, WS_S1, (size_t)N * (numMC + 1), &S1));
+    if (with_uhat) {
+        GLOBE_CK(ctx, cudaMemcpyAsync(pb.VR0, ctx->vinv_r, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        GLOBE_RET(seg_sums(ctx, pb.VR0, nullptr, nullptr, nullptr, nullptr, numMC + 1, Zi, S1));
+        GLOBE_RET(grm_apply_dev(ctx, Zi, numMC + 1, pb.UH0));
+        GLOBE_CK(ctx, cudaMemcpyAsync(ctx->uhat, pb.UH0, sizeof(double) * N, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        ctx->mme_ok = true;
+    } else {
+        GLOBE_RET(seg_sums(ctx, pb.VR, nullptr, nullptr, nullptr, nullptr, numMC, Zi, S1));
+        GLOBE_RET(grm_apply_dev(ctx, Zi, numMC, pb.UH));
+    }
     GLOBE_RET(ftheta_kernel(ctx, ctx->vinv_r, ctx->uhat, fth));
     double* small;
     GLOBE_RET(ws(ctx, WS_SMALL, (size_t)numMC * 5 + 64, &small));
     GLOBE_RET(xt_mat(ctx, ctx->vinv_r, 1, fth, 5, small));
     double h_first[5];
     GLOBE_RET(d2h(ctx, h_first, small, 5));
-    GLOBE_RET(project_dev(ctx, VY, numMC, pb.VR));
-    double *Zi, *S1;
-    GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * numMC, &Zi));
-    GLOBE_RET(ws(ctx, WS_S1, (size_t)N * numMC, &S1));
-    GLOBE_RET(seg_sums(ctx, pb.VR, nullptr, nullptr, nullptr, nullptr, numMC, Zi, S1));
-    GLOBE_RET(grm_apply_dev(ctx, Zi, numMC, pb.UH));
     GLOBE_RET(ws(ctx, WS_SMALL, (size_t)numMC * 5 + 64, &small));
     GLOBE_RET(trace_terms(ctx, pb.VR, pb.UH, pb.TY, numMC, small));
     std::vector<double> tt((size_t)numMC * 5);
@@ -598,8 +620,8 @@ static int aireml_eval_impl(globe_ctx* ctx, const double* probes, int numMC, uin
     o.x0mode = GLOBE_X0_GIVEN;
     GLOBE_RET(pcg_dev(ctx, FB, FX, kt, &o, info));
     GLOBE_CK(ctx, cudaMemcpyAsync(ctx->vinv_X, FX, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
-    GLOBE_RET(mme_finish(ctx, nullptr, nullptr, nullptr, nullptr));
-    return grad_finish(ctx, numMC, FX + (size_t)n * k, pb, nullptr, first, trace, grad);
+    GLOBE_RET(mme_finish(ctx, nullptr, nullptr, nullptr, nullptr, false));
+    return grad_finish(ctx, numMC, FX + (size_t)n * k, pb, nullptr, first, trace, grad, true);
 }
 
 // The GRM products outside the PCG solves (u-hat, the probes' u-hat) run at the
