@@ -78,11 +78,6 @@ __device__ __forceinline__ uint32_t dig_byte(const uint4& v, int j) {
     return (w >> (8 * (j & 3))) & 0xFFu;
 }
 
-// Digit operand of the columns jb .. jb + gridDim.x - 1 (one CTA per column).  Column
-// jj = z * GRM_KG + c goes to digit rows z * GRM_NMMA + c * NDIG + j, K positions in the
-// decode order of the A operand (position P of a group of 16 holds SNP 2P for P < 8,
-// 2(P-8)+1 otherwise).  The codes come from the individual-major tile-blocked copy
-// (blk2, tile codes): 16 SNPs of individual i are one 32-bit word.  C2[jj] = sum_s 2 f_s u~(s, j).
 // (sh, sl) += (h, l) in double-float: Knuth's two-sum of the high parts, the rounding error and
 // the low parts into sl (GB300's FP32 pipe is many times its FP64 pipe)
 __device__ __forceinline__ void df_add(float& sh, float& sl, float h, float l) {
@@ -93,56 +88,106 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, float h, float l) {
     sh = s;
 }
 
+constexpr int GD_Q = 32;      // 16-SNP groups per CTA (one per lane): 512 SNPs
+constexpr int GD_COLS = 32;   // columns per CTA (four per warp)
+constexpr int GD_PAD = 65;    // table slots per 16-SNP group: 64 entries + 1 (spreads shared-memory banks)
+constexpr size_t GD_SMEM = (size_t)GD_Q * GD_PAD * (sizeof(uint4) + sizeof(float2));
+
+// bytes [a0.k, a1.k, a2.k, a3.k] (byte k of each word)
+__device__ __forceinline__ uint32_t gather_byte(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t k) {
+    const uint32_t sel = k | ((k + 4) << 4);
+    uint32_t lo, hi, r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(lo) : "r"(a0), "r"(a1), "r"(sel));
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(hi) : "r"(a2), "r"(a3), "r"(sel));
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(lo), "r"(hi), "r"(0x5410u));
+    return r;
+}
+
+// Digit operand of the batch's columns jb .. jb + ncols - 1.  Column jj = z * GRM_KG + c
+// goes to digit rows z * GRM_NMMA + c * NDIG + j, K positions in the decode order of the A
+// operand (position P of a group of 16 holds SNP 2P for P < 8, 2(P-8)+1 otherwise).
+// A CTA covers 512 SNPs (32 groups of 16, one per lane) for 32 columns (four per warp): the
+// table entries of its SNPs are staged once in shared memory, each lane reads the 16 codes
+// of its group for one column (one 32-bit word of blk2, tile codes), gathers the 16 table
+// entries and assembles the 9 digit rows 4 bytes at a time (3 prmt per word).  The centring
+// sums come out per (CTA SNP range, column) in part[blockIdx.y * ncols + jj].
 __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ blk2, int nch2, int32_t N, int jb,
-                                                    const uint4* __restrict__ dig, const float2* __restrict__ c2v,
-                                                    int64_t kpad, uint8_t* __restrict__ D, double* __restrict__ C2) {
-    __shared__ double red[8];
-    const int jj = blockIdx.x;
-    const int64_t j = (int64_t)jb + jj;
-    const int z = jj / GRM_KG, c = jj % GRM_KG;
-    uint8_t* Dc = D + ((int64_t)z * GRM_NMMA + c * NDIG) * kpad;
+                                                    int ncols, const uint4* __restrict__ dig,
+                                                    const float2* __restrict__ c2v, int64_t kpad,
+                                                    uint8_t* __restrict__ D, double* __restrict__ part) {
+    extern __shared__ __align__(16) uint8_t gd_sm[];
+    uint4* tdig = reinterpret_cast<uint4*>(gd_sm);
+    float2* tc2 = reinterpret_cast<float2*>(gd_sm + (size_t)GD_Q * GD_PAD * sizeof(uint4));
     const int64_t nq = kpad >> 4;
-    float ah = 0.0f, al = 0.0f;
-    if (j < N) {
-        const int r = (int)(j & (BM - 1));
-        const int64_t t = j / BM;
-        const int swz = (r >> 2) & 1;
-        for (int64_t q = threadIdx.x; q < nq; q += blockDim.x) {
-            const int64_t ch = q >> 3;
-            const int qb = (int)(q & 7), h = qb >> 2;
-            const uint32_t w = *reinterpret_cast<const uint32_t*>(
-                blk2 + (((t * nch2 + ch) * BM + r) * 2 + (h ^ swz)) * 16 + (qb & 3) * 4);
+    const int64_t q0 = (int64_t)blockIdx.y * GD_Q;
+    for (int e = threadIdx.x; e < GD_Q * 64; e += blockDim.x) {
+        const int ql = e >> 6, w = e & 63;          // w = 4 m + tile code
+        const int64_t x = (q0 + ql) * 64 + w;        // entry of SNP 16 (q0 + ql) + m
+        const bool in = q0 + ql < nq;
+        tdig[ql * GD_PAD + w] = in ? __ldg(dig + x) : make_uint4(0u, 0u, 0u, 0u);
+        tc2[ql * GD_PAD + w] = in ? __ldg(c2v + x) : make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t q = q0 + lane;
+    const bool qin = q < nq;
+    const uint4* te = tdig + lane * GD_PAD;
+    const float2* tc = tc2 + lane * GD_PAD;
+    for (int cc = warp; cc < GD_COLS; cc += 8) {
+        const int jj = blockIdx.x * GD_COLS + cc;
+        if (jj >= ncols) break;                      // uniform across the warp
+        const int64_t j = (int64_t)jb + jj;
+        const int z = jj / GRM_KG, c = jj % GRM_KG;
+        uint8_t* Dc = D + ((int64_t)z * GRM_NMMA + c * NDIG) * kpad;
+        float ah = 0.0f, al = 0.0f;
+        if (qin) {
             uint32_t o[NDIG][4];
 #pragma unroll
             for (int d = 0; d < NDIG; ++d) o[d][0] = o[d][1] = o[d][2] = o[d][3] = 0u;
+            if (j < N) {
+                const int r = (int)(j & (BM - 1));
+                const int64_t t = j / BM;
+                const int swz = (r >> 2) & 1;
+                const int64_t ch = q >> 3;
+                const int qb = (int)(q & 7), h = qb >> 2;
+                const uint32_t w = *reinterpret_cast<const uint32_t*>(
+                    blk2 + (((t * nch2 + ch) * BM + r) * 2 + (h ^ swz)) * 16 + (qb & 3) * 4);
 #pragma unroll
-            for (int P = 0; P < 16; ++P) {
-                const int m = P < 8 ? 2 * P : 2 * (P - 8) + 1;
-                const int64_t x = ((q << 4) + m) * 4 + ((w >> (2 * m)) & 3u);
-                const uint4 v = __ldg(dig + x);
-                const float2 cv = __ldg(c2v + x);
-                df_add(ah, al, cv.x, cv.y);
+                for (int wq = 0; wq < 4; ++wq) {   // output word wq: positions 4 wq .. 4 wq + 3
+                    uint4 e[4];
 #pragma unroll
-                for (int d = 0; d < NDIG; ++d) o[d][P >> 2] |= dig_byte(v, d) << (8 * (P & 3));
+                    for (int b = 0; b < 4; ++b) {
+                        const int P = 4 * wq + b;
+                        const int m = P < 8 ? 2 * P : 2 * (P - 8) + 1;
+                        const int code = (int)((w >> (2 * m)) & 3u);
+                        e[b] = te[m * 4 + code];
+                        const float2 cv = tc[m * 4 + code];
+                        df_add(ah, al, cv.x, cv.y);
+                    }
+#pragma unroll
+                    for (int d = 0; d < 4; ++d) o[d][wq] = gather_byte(e[0].x, e[1].x, e[2].x, e[3].x, d);
+#pragma unroll
+                    for (int d = 4; d < 8; ++d) o[d][wq] = gather_byte(e[0].y, e[1].y, e[2].y, e[3].y, d - 4);
+                    o[8][wq] = gather_byte(e[0].z, e[1].z, e[2].z, e[3].z, 0);
+                }
             }
 #pragma unroll
             for (int d = 0; d < NDIG; ++d)
                 *reinterpret_cast<uint4*>(Dc + d * kpad + (q << 4)) = make_uint4(o[d][0], o[d][1], o[d][2], o[d][3]);
         }
-    } else {
-        for (int64_t q = threadIdx.x; q < nq; q += blockDim.x)
-#pragma unroll
-            for (int d = 0; d < NDIG; ++d) *reinterpret_cast<uint4*>(Dc + d * kpad + (q << 4)) = make_uint4(0, 0, 0, 0);
+        double acc = (double)ah + (double)al;
+        for (int o2 = 16; o2 > 0; o2 >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o2);
+        if (lane == 0) part[(int64_t)blockIdx.y * ncols + jj] = acc;
     }
-    double acc = (double)ah + (double)al;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-        C2[jj] = s;
-    }
+}
+
+// C2[jj] = sum over the SNP ranges of the centring partials, in range order
+__global__ void k_grm_c2(const double* __restrict__ part, int nqb, int ncols, double* __restrict__ C2) {
+    const int jj = blockIdx.x * blockDim.x + threadIdx.x;
+    if (jj >= ncols) return;
+    double a = 0.0;
+    for (int y = 0; y < nqb; ++y) a += part[(int64_t)y * ncols + jj];
+    C2[jj] = a;
 }
 
 // A_ij = (2^e sum_d 32^-d P_d(i, j) - C2_j) (1/M) rounded to float32, for the rows
@@ -282,7 +327,7 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     const int G = (int)std::max<size_t>(1, gfit);
     const int nbr = 304;
     BuildBufs B(ctx);
-    double *U4, *C2, *info, *pm, *ps;
+    double *U4, *C2, *info, *pm, *ps, *c2part;
     float2* c2v;
     uint4* dig;
     uint8_t* D;
@@ -292,6 +337,8 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     GLOBE_RET(B.get(&dig, (size_t)4 * kpad));
     GLOBE_RET(B.get(&c2v, (size_t)4 * kpad));
     GLOBE_RET(B.get(&C2, (size_t)G * GRM_KG));
+    const int nqb = (int)((kpad / 16 + GD_Q - 1) / GD_Q);   // SNP ranges of k_grm_digits
+    GLOBE_RET(B.get(&c2part, (size_t)nqb * G * GRM_KG));
     GLOBE_RET(B.get(&info, (size_t)2));
     GLOBE_RET(B.get(&pm, (size_t)nbr));
     GLOBE_RET(B.get(&ps, (size_t)nbr));
@@ -303,6 +350,15 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     GLOBE_CK(ctx, cudaMemsetAsync(D, 0, (size_t)G * GRM_NMMA * kpad, ctx->stream));
     CUtensorMap mB;
     GLOBE_RET(make_map(ctx, &mB, D, (uint64_t)kpad, (uint64_t)G * GRM_NMMA, BK, (uint32_t)GRM_NMMA, true));
+    {   // the digit kernel's staged table is above the default 48 KB (a per-device opt-in)
+        static std::atomic<uint64_t> attr_set{0};
+        const uint64_t bit = 1ull << (ctx->device & 63);
+        if (!(attr_set.load() & bit)) {
+            GLOBE_CK(ctx, cudaFuncSetAttribute(k_grm_digits, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)GD_SMEM));
+            attr_set.fetch_or(bit);
+        }
+    }
     // digit table with one exponent for the whole matrix
     k_grm_u4<<<(unsigned)std::min<int64_t>(div_up(4 * g.Mk, 256), 4096), 256, 0, ctx->stream>>>(g.zs, g.inv, g.Mk,
                                                                                                  U4);
@@ -317,8 +373,12 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     const int64_t pz = (int64_t)spe * GRM_NMMA * ldp;
     for (int jb = 0; jb < N; jb += G * GRM_KG) {
         const int gb = std::min(G, (N - jb + GRM_KG - 1) / GRM_KG);
-        k_grm_digits<<<(unsigned)(gb * GRM_KG), 256, 0, ctx->stream>>>(g.blk2, nch, N, jb, dig, c2v, kpad, D, C2);
+        const int ncols = gb * GRM_KG;
+        k_grm_digits<<<dim3((unsigned)div_up(ncols, GD_COLS), (unsigned)nqb), 256, GD_SMEM, ctx->stream>>>(
+            g.blk2, nch, N, jb, ncols, dig, c2v, kpad, D, c2part);
         GLOBE_LAUNCHED(ctx, "k_grm_digits");
+        k_grm_c2<<<div_up(ncols, 128), 128, 0, ctx->stream>>>(c2part, nqb, ncols, C2);
+        GLOBE_LAUNCHED(ctx, "k_grm_c2");
         ZGrid zg;
         zg.nz = gb;
         zg.pz = pz;
