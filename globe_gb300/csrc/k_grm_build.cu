@@ -78,16 +78,6 @@ __device__ __forceinline__ uint32_t dig_byte(const uint4& v, int j) {
     return (w >> (8 * (j & 3))) & 0xFFu;
 }
 
-// (sh, sl) += (h, l) in double-float: Knuth's two-sum of the high parts, the rounding error and
-// the low parts into sl (GB300's FP32 pipe is many times its FP64 pipe)
-__device__ __forceinline__ void df_add(float& sh, float& sl, float h, float l) {
-    const float s = __fadd_rn(sh, h);
-    const float bp = __fsub_rn(s, sh);
-    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(h, bp));
-    sl = __fadd_rn(sl, __fadd_rn(err, l));
-    sh = s;
-}
-
 constexpr int GD_Q = 32;      // 16-SNP groups per CTA (one per lane): 512 SNPs
 constexpr int GD_COLS = 32;   // columns per CTA (four per warp)
 constexpr int GD_PAD = 65;    // table slots per 16-SNP group: 64 entries + 1 (spreads shared-memory banks)

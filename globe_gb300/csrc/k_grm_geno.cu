@@ -64,15 +64,19 @@ __global__ void __launch_bounds__(256) k_geno_p1(const uint8_t* __restrict__ blk
 constexpr int P2_THREADS = 128;  // samples per CTA (32 bytes per SNP row)
 constexpr int P2_TS = 64;        // SNPs per shared-memory tile
 
-// SQUARE: accumulate zs^2 (genetic diagonal) instead of zs * W.
+// SQUARE: accumulate zs^2 (genetic diagonal) instead of zs * W, as double-float sums of the
+// FP64 squares split into float pairs (GB300's FP64 pipe would bound the 5e10 additions of
+// the full workload at ~0.1 s; on the FP32 pipe they take a few ms).
 template <int KC, bool SQUARE>
 __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restrict__ blk, int nch,
                                                         int64_t Mk, int32_t N, const double* __restrict__ zs,
+                                                        const float2* __restrict__ zsq,
                                                         const double* __restrict__ W, int64_t ldw, int kc,
                                                         int64_t s_per, double* __restrict__ part) {
     __shared__ __align__(16) uint8_t gb[P2_TS][32];
     __shared__ double zt[P2_TS][4];
     __shared__ double wt[P2_TS][KC > 0 ? KC : 1];
+    __shared__ float2 zq[P2_TS][4];   // SQUARE: zs^2 by tile code as (hi, lo) floats
     const int tid = threadIdx.x;
     const int64_t i = (int64_t)blockIdx.x * P2_THREADS + tid;
     const int64_t byte0 = (int64_t)blockIdx.x * 32;   // this CTA's 32-byte chunk of every row
@@ -82,6 +86,7 @@ __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restric
     double acc[KC];
 #pragma unroll
     for (int c = 0; c < KC; ++c) acc[c] = 0.0;
+    float qh = 0.0f, ql = 0.0f;   // SQUARE: double-float sum
     const int sh = 2 * (tid & 3);
     const int bi = tid >> 2;
     for (int64_t s0 = s_beg; s0 < s_end; s0 += P2_TS) {
@@ -95,7 +100,8 @@ __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restric
         }
         for (int e = tid; e < P2_TS * 4; e += P2_THREADS) {
             const int rs = e >> 2;
-            zt[rs][e & 3] = rs < ns ? zs[(s0 + rs) * 4 + (e & 3)] : 0.0;
+            if (SQUARE) zq[rs][e & 3] = rs < ns ? zsq[(s0 + rs) * 4 + (e & 3)] : make_float2(0.0f, 0.0f);
+            else zt[rs][e & 3] = rs < ns ? zs[(s0 + rs) * 4 + (e & 3)] : 0.0;
         }
         if (!SQUARE) {
             for (int e = tid; e < P2_TS * KC; e += P2_THREADS) {
@@ -106,22 +112,34 @@ __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restric
         __syncthreads();
         for (int rs = 0; rs < ns; ++rs) {
             const unsigned code = (gb[rs][bi] >> sh) & 3u;
-            const double z = zsel(code, zt[rs][0], zt[rs][1], zt[rs][2]);
             if (SQUARE) {
-                acc[0] += z * z;
+                const float2 q = zq[rs][code];
+                tc::df_add(qh, ql, q.x, q.y);
             } else {
+                const double z = zsel(code, zt[rs][0], zt[rs][1], zt[rs][2]);
 #pragma unroll
                 for (int c = 0; c < KC; ++c) acc[c] += z * wt[rs][c];
             }
         }
         __syncthreads();
     }
+    if (SQUARE) acc[0] = (double)qh + (double)ql;
     if (i < N) {
         const size_t base = (size_t)blockIdx.y * (size_t)N * (SQUARE ? 1 : kc);
 #pragma unroll
         for (int c = 0; c < KC; ++c)
             if (c < (SQUARE ? 1 : kc)) part[base + i + (size_t)c * N] = acc[c];
     }
+}
+
+// zsq[4 s + t] = zs^2 of tile code t as a (hi, lo) float pair (t: 0 -> g=2, 1 -> g=1, 2/3 -> g=0)
+__global__ void k_zs_square(const double* __restrict__ zs, int64_t Mk, float2* __restrict__ zsq) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 4 * Mk) return;
+    const double z = zs[(e & ~3ll) + tc::tile_to_plink((int)(e & 3))];
+    const double q = z * z;
+    const float hi = __double2float_rn(q);
+    zsq[e] = make_float2(hi, __double2float_rn(q - (double)hi));
 }
 
 // out[e] = scale * sum_y part[y * n + e]  (fixed order)
@@ -157,7 +175,7 @@ static int geno_chunk(globe_ctx* ctx, const double* Z, int kc, double scale, dou
     dim3 grid(div_up(N, P2_THREADS), nsplit);
     {
         ProfScope ps(ctx, GLOBE_PROF_GRM_PASS2);
-        k_geno_p2<KC, false><<<grid, P2_THREADS, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, W, g.Mk, kc,
+        k_geno_p2<KC, false><<<grid, P2_THREADS, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, nullptr, W, g.Mk, kc,
                                                                     s_per, part);
         GLOBE_LAUNCHED(ctx, "k_geno_p2");
     }
@@ -215,8 +233,12 @@ int geno_diag(globe_ctx* ctx, double* d) {
     nsplit = (int)((g.Mk + s_per - 1) / s_per);
     double* part;
     GLOBE_RET(ws(ctx, WS_GPART, (size_t)nsplit * N, &part));
+    float2* zsq;
+    GLOBE_RET(ws(ctx, WS_W, (size_t)g.Mk * 4, &zsq));
+    k_zs_square<<<div_up(4 * g.Mk, 256), 256, 0, ctx->stream>>>(g.zs, g.Mk, zsq);
+    GLOBE_LAUNCHED(ctx, "k_zs_square");
     dim3 grid((unsigned)ctas_x, nsplit);
-    k_geno_p2<1, true><<<grid, P2_THREADS, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, nullptr, 0, 1,
+    k_geno_p2<1, true><<<grid, P2_THREADS, 0, ctx->stream>>>(g.blk1, g.nch1, g.Mk, N, g.zs, zsq, nullptr, 0, 1,
                                                               s_per, part);
     GLOBE_LAUNCHED(ctx, "k_geno_diag");
     // A_ii = (1/M) sum_s zs^2   (PCGsolver.cpp:986-988)

@@ -35,6 +35,16 @@ __host__ __device__ __forceinline__ uint32_t recode_tile(uint32_t w) {
 // the PLINK code each tile code stands for (missing and genotype 0 share tile code 10)
 __host__ __device__ constexpr int tile_to_plink(int t) { return t == 0 ? 0 : (t == 1 ? 2 : 3); }
 
+// (sh, sl) += (h, l) in double-float: Knuth's two-sum of the high parts, the rounding error and
+// the low parts into sl (GB300's FP32 pipe is many times its FP64 pipe)
+__device__ __forceinline__ void df_add(float& sh, float& sl, float h, float l) {
+    const float s = __fadd_rn(sh, h);
+    const float bp = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bp)), __fsub_rn(h, bp));
+    sl = __fadd_rn(sl, __fadd_rn(err, l));
+    sh = s;
+}
+
 // Byte b of row `row` in a tile-blocked copy with nch 32-byte chunks per row: block (row / 128,
 // b / 32) of 128 rows x 32 bytes, the two 16-byte halves of a row swapped when bit 2 of the row
 // (within its tile) is set.
