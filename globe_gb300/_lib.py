@@ -75,6 +75,7 @@ SIGNATURES = {
     "globe_load_grm": (C.c_int, [_vp, _fp, C.c_int32]),
     "globe_set_individuals": (C.c_int, [_vp, C.c_int32]),
     "globe_set_digits": (C.c_int, [_vp, C.c_int]),
+    "globe_debug_stall_next_gemm": (C.c_int, [_vp]),
     "globe_get_digits": (C.c_int, [_vp]),
     "globe_grm_build": (C.c_int, [_vp, _fp]),
     "globe_grm_build_dev": (C.c_int, [_vp, _vp]),

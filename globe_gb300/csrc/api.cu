@@ -526,6 +526,12 @@ int globe_set_digits(globe_ctx* ctx, int nd) {
 
 int globe_get_digits(const globe_ctx* ctx) { return ctx ? ctx->digits : 9; }
 
+int globe_debug_stall_next_gemm(globe_ctx* ctx) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    ctx->stall_next_gemm = 1;
+    return GLOBE_OK;
+}
+
 int globe_set_precision(globe_ctx* ctx, int precision) {
     if (!ctx) return GLOBE_ERR_ARG;
     if (precision != GLOBE_PREC_FP64 && precision != GLOBE_PREC_MIXED)

@@ -109,6 +109,7 @@ struct globe_ctx {
     int prec = GLOBE_PREC_FP64;   // precision of operator calls (globe_set_precision / PCG options)
     int model = GLOBE_MODEL_FULL; // GLOBE_MODEL_NO_TIME: components (sig2e, sig2g) only
     int digits = 9;               // base-32 digits per column of the tensor-core product (globe_set_digits)
+    int stall_next_gemm = 0;      // test hook of the bounded waits (globe_debug_stall_next_gemm)
     int nvc() const { return model == GLOBE_MODEL_NO_TIME ? 2 : 5; }
     bool precond_ok = false;      // H built for the current vc
     globe::Slot ws[globe::WS_COUNT];

@@ -292,7 +292,7 @@ template <int NMMA>
 __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
     k_tc_gemm(const uint8_t* __restrict__ blk, const __grid_constant__ CUtensorMap tmB, int rows, int nchunks,
               int cps, float* __restrict__ part, int64_t ldp, int64_t pz, int skip0, int skipz,
-              unsigned* __restrict__ err) {
+              unsigned* __restrict__ err, int stall) {
     using G = Geo<NMMA>;
     constexpr int MT = G::MT;
     static_assert(NMMA % 16 == 0 && NMMA >= 16 && NMMA <= 256, "NMMA");
@@ -361,6 +361,10 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
             for (int it = 0; it < nloc; ++it) {
                 const int s = it % BSTAGES, n = it / BSTAGES;
                 if (n > 0 && !mbar_wait(&S.bempty[s], (n - 1) & 1, abort, err, 2u)) break;
+                if (stall && it == 0) {   // test hook: the stage is never loaded, so its waits run out
+                    issued = 1;
+                    continue;
+                }
                 mbar_expect_tx(&S.bfull[s], NMMA * BK);
                 tma_load_2d(S.bt[s], &tmB, (c0 + it) * BK, z * NMMA, &S.bfull[s]);
                 issued = it + 1;
@@ -815,7 +819,7 @@ static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB
     }
     dim3 grid((unsigned)((rows + G::MT * BM - 1) / (G::MT * BM)), (unsigned)splits, (unsigned)zg.nz);
     k_tc_gemm<NMMA><<<grid, G::NTHREADS, smem, ctx->stream>>>(blk, mB, rows, nchunks, cps, part, ldp, zg.pz,
-                                                               zg.skip0, zg.skipz, err);
+                                                               zg.skip0, zg.skipz, err, zg.stall);
     GLOBE_LAUNCHED(ctx, "k_tc_gemm");
     return GLOBE_OK;
 }
@@ -927,7 +931,10 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     // ---- pass 1
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS1);
-        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, ZGrid()));
+        ZGrid zg;
+        zg.stall = ctx->stall_next_gemm;
+        ctx->stall_next_gemm = 0;
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, zg));
     }
     const int sp1e = eff_splits(nch1, sp1);
     k_combine1<ND><<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);

@@ -114,6 +114,7 @@ struct ZGrid {
     int nz = 1;
     int64_t pz = 0;
     int skip0 = 0, skipz = 0;
+    int stall = 0;   // test hook (globe_debug_stall_next_gemm): leave the first digit stage unloaded
 };
 
 int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t box_in,

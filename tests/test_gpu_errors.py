@@ -42,3 +42,28 @@ def test_record_table_errors():
         X[1, 0] = np.nan
         with pytest.raises(G.GlobeError, match="non-finite"):
             ctx.load_records(np.array([0, 0, 1, 1]), X, y, 2)
+
+
+def test_tensor_core_wait_timeout_is_reported_and_recovered(orc):
+    """A tensor-core launch whose first digit stage never arrives (test hook): its bounded
+    waits run out (~2 s), the kernel aborts cleanly and the call reports the timeout; the
+    same context then computes the product correctly."""
+    import time
+    from helpers import rel
+    c = cohort(23, 200, 300, recs=("uniform", 1, 3), miss=0.02)     # one CTA per pass
+    N = c["N"]
+    Z = np.random.default_rng(4).standard_normal((N, 3))
+    with G.Context(0) as ctx:
+        ctx.load_records(c["indiv"].astype(np.int32), c["X"], c["y"], N)
+        ctx.load_bed(c["packed"])
+        ctx.set_vc(VC_F)
+        ctx.set_precision(G.PREC_MIXED)
+        assert ctx._L.globe_debug_stall_next_gemm(ctx.h) == 0
+        t0 = time.perf_counter()
+        with pytest.raises(G.GlobeError) as e:
+            ctx.grm_apply(Z)
+        assert time.perf_counter() - t0 < 30
+        assert e.value.code == -2 and "timed out" in str(e.value)   # GLOBE_ERR_CUDA
+        got = ctx.grm_apply(Z)                  # the context is still usable
+        s = orc.Solver(c["indiv"].astype(np.int32), c["X"], c["y"], N, VC_F, packed=c["packed"])
+        assert rel(got, s.grm_apply(Z)) < 1e-11
