@@ -1,9 +1,10 @@
 """Host-side mirror of GLOBE's interface over the C ABI.
 
 ``Context`` wraps one ``globe_ctx`` (one GPU, one stream).  ``run_pcg_solver``
-and ``run_aireml`` mirror the reference's two programs (same arguments, same
-files); the C++ programs ``globe_gb300/bin/runPCGsolver`` and ``runAIREML``
-are the command-line drop-ins.
+and ``run_aireml`` mirror the reference's programs (same arguments, same
+files); the C++ programs ``globe_gb300/bin/runPCGsolver``, ``runAIREML`` and
+``runAIREML_reducedModel`` are the command-line drop-ins.  ``build_grm`` (and
+the ``buildGRM`` program) writes the ``.grm.bin`` input from genotypes.
 """
 import ctypes as C
 import os
