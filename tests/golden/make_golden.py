@@ -18,6 +18,13 @@ seeds; the reference programs' outputs are stored next to them:
 * ``reduced_small.{txt,grm.bin}`` + ``reduced_small_ref.json`` -- the same for
   runAIREML_reducedModel (no time effects, components sig2e and sig2g; one
   record per individual; record table INDIV PHENO COV0 COV1 COV2).
+* ``geno_small_grmf64_ref.npz`` -- beta / uhat / bhat of the float->double
+  runPCGsolver --grm on the GRM of geno_small built by the oracle's
+  orc_grm_build with the double allele frequency (the GPU builder's
+  convention), next to geno64_* of the same program with --geno.
+
+``python make_golden.py grm_build`` makes only the last fixture (from the
+committed geno_small inputs).
 """
 import json
 import os
@@ -172,17 +179,39 @@ def make_reduced_case(tmp):
     print(name, "N=%d iterations=%d" % (N, len(its)))
 
 
+def make_grm_build_case(tmp):
+    """The reference's FP64 runPCGsolver --grm on the oracle-built GRM (double allele
+    frequency) of the committed geno_small inputs."""
+    from oracle import oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import golden_case
+    c = golden_case("geno_small")
+    lt = oracle.grm_build(c["packed"], c["N"], freq="f64")
+    g = os.path.join(tmp, "geno_small_f64")
+    synth.write_grm_bin(g, lt)
+    o = os.path.join(tmp, "geno_small_grmf64")
+    subprocess.run([os.path.join(REF, "runPCGsolver64"), "--input", c["prefix"] + ".txt", "--output", o,
+                    "--grm", g] + _vcargs(VC), capture_output=True, text=True, check=True)
+    out = {v: _vec("%s_%s.bin" % (o, v)) for v in ("beta", "uhat", "bhat")}
+    np.savez_compressed(os.path.join(HERE, "geno_small_grmf64_ref.npz"), **out)
+    print("geno_small_grmf64: reference --grm on the oracle-built GRM")
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "runPCGsolver64")):
         sys.exit("build the reference first: python oracle/build_ref.py")
     tmp = "/tmp/globe_golden"
     os.makedirs(tmp, exist_ok=True)
+    if sys.argv[1:] == ["grm_build"]:
+        make_grm_build_case(tmp)
+        return
     for name, args in CASES.items():
         make_pcg_case(name, *args, tmp)
     if os.path.exists(os.path.join(REF, "runAIREML64")):
         make_aireml_case(tmp)
     if os.path.exists(os.path.join(REF, "runAIREML_reduced64")):
         make_reduced_case(tmp)
+    make_grm_build_case(tmp)
 
 
 if __name__ == "__main__":

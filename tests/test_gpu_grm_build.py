@@ -155,3 +155,18 @@ def test_buildgrm_program_errors(tmp_path):
     r = subprocess.run([exe, os.path.join(str(tmp_path), "missing"), os.path.join(str(tmp_path), "x")],
                        capture_output=True, text=True)
     assert r.returncode != 0 and ".fam" in r.stderr
+
+
+def test_built_grm_solve_matches_reference_run(gctx):
+    """The MME on the GPU-built GRM matches the reference's FP64 runPCGsolver --grm on the
+    oracle-built GRM (tests/golden/geno_small_grmf64_ref.npz): the two matrices are the
+    same to float32 rounding ties."""
+    c = golden_case("geno_small")
+    d = np.load(os.path.join(ROOT, "tests", "golden", "geno_small_grmf64_ref.npz"))
+    lt = _build(c["packed"], c["N"], G.PREC_MIXED)
+    gctx.load_records(c["indiv"], c["X"], c["y"], c["N"])
+    gctx.load_grm(lt, c["N"])
+    gctx.set_vc(VC_F)
+    r = gctx.mme(tol=1e-13, rule=G.RULE_PCGSOLVER)
+    for v in ("beta", "uhat", "bhat"):
+        assert rel(r[v], d[v]) < 2e-8, v

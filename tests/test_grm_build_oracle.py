@@ -3,10 +3,12 @@ Those are the matrices the reference programs were run on
 (tests/golden/make_golden.py), whose --grm solutions agree with the
 reference's own --geno solutions (test_oracle_golden.py), so this pins the
 builder's arithmetic and convention to the reference's standardisation."""
+import os
+
 import numpy as np
 import pytest
 
-from helpers import f32_ulps, golden_case
+from helpers import GOLDEN, VC_F, f32_ulps, golden_case, rel
 
 
 @pytest.mark.parametrize("name", ["geno_small", "tiny"])
@@ -38,3 +40,19 @@ def test_oracle_grm_definition(orc):
     A = Z.T @ Z / keep.sum()
     il = np.tril_indices(N)
     assert np.abs(lt - A[il]).max() <= 2 * np.abs(A).max() * 2.0 ** -24
+
+
+def test_reference_on_built_grm_reproduces_geno(orc):
+    """The reference's own FP64 runPCGsolver, run with --grm on the GRM this builder's
+    convention gives (oracle build; tests/golden/geno_small_grmf64_ref.npz), reproduces its
+    --geno solution to the float32 rounding of the file; the oracle's solve on that GRM
+    matches the reference run."""
+    c = golden_case("geno_small")
+    d = np.load(os.path.join(GOLDEN, "geno_small_grmf64_ref.npz"))
+    for v in ("beta", "uhat", "bhat"):
+        assert rel(d[v], c["ref"]["geno64_" + v]) < 5e-8, v
+    lt = orc.grm_build(c["packed"], c["N"])
+    s = orc.Solver(c["indiv"], c["X"], c["y"], c["N"], VC_F, grm_lt=lt)
+    res = s.mme(1e-13)
+    for v in ("beta", "uhat", "bhat"):
+        assert rel(res[v], d[v]) < 2e-8, v
