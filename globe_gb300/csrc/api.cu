@@ -133,7 +133,7 @@ static void free_cohort(globe_ctx* ctx) {
 
 static void free_genetic(globe_ctx* ctx) {
     auto& g = ctx->gen;
-    for (void* p : {(void*)g.geno, (void*)g.zs, (void*)g.f, (void*)g.inv, (void*)g.grm, (void*)g.gdiag, (void*)g.gt,
+    for (void* p : {(void*)g.geno, (void*)g.zs, (void*)g.f, (void*)g.inv, (void*)g.grm, (void*)g.gdiag,
                     (void*)g.blk1, (void*)g.blk2})
         dfree(ctx, p);
     g = Genetic();
@@ -327,7 +327,7 @@ int globe_set_individuals(globe_ctx* ctx, int32_t N) {
 namespace globe {
 
 // statistics, filter and compaction of the kept SNP rows; the tile-blocked layout follows
-// separately (ensure_gt), after the callers have released their staging copies
+// separately (ensure_blk1), after the callers have released their staging copies
 int load_bed_rows(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf, float max_miss,
                   int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep, globe_bed_info* info) {
     if (!ctx) return GLOBE_ERR_ARG;
@@ -415,8 +415,8 @@ int globe_load_bed_dev(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t 
                        float max_miss, int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep,
                        globe_bed_info* info) {
     int rc = load_bed_rows(ctx, d_bed, M, stride, min_maf, max_miss, d_alt, d_miss, d_maf, d_mr, d_keep, info);
-    // the tile-blocked copies every genotype kernel reads; the compacted rows are freed
-    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_gt(ctx);
+    // the tile-blocked copy the genotype kernels read; the compacted rows are freed
+    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_blk1(ctx);
     return rc;
 }
 
@@ -459,7 +459,7 @@ done:
     cudaStreamSynchronize(ctx->stream);
     for (void* p : {(void*)d_bed, (void*)d_alt, (void*)d_miss, (void*)d_maf, (void*)d_mr, (void*)d_keep}) dfree(ctx, p);
     // tile-blocked layout once the staging copy of the payload is gone
-    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_gt(ctx);
+    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_blk1(ctx);
     return rc;
 }
 

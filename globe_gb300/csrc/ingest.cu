@@ -108,6 +108,6 @@ done:
     }
     for (void* p : {(void*)d_bed, (void*)d_alt, (void*)d_miss, (void*)d_maf, (void*)d_mr, (void*)d_keep}) dfree(ctx, p);
     // tile-blocked layout once the file's device copy is gone
-    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_gt(ctx);
+    if (rc == GLOBE_OK && ctx->gen.Mk > 0) rc = ensure_blk1(ctx);
     return rc;
 }

@@ -51,17 +51,14 @@ struct Genetic {
     // genotype source
     int64_t Mk = 0;          // kept SNPs
     int64_t stride = 0;      // bytes per SNP row (multiple of 16)
-    uint8_t* geno = nullptr; // Mk x stride
+    uint8_t* geno = nullptr; // Mk x stride compacted rows (PLINK codes), freed once blk1 exists
     double* zs = nullptr;    // Mk x 4
     double* f = nullptr;     // Mk
     double* inv = nullptr;   // Mk
-    // individual-major copy for the tensor-core pass 2 (built on first use):
-    // N rows of strideT bytes, byte b = SNPs 4b..4b+3, padding codes 11
-    uint8_t* gt = nullptr;
-    int64_t strideT = 0;
-    // tile-blocked copies for the tensor-core passes: block (tile, chunk) = 128 rows x 32 B
-    uint8_t* blk1 = nullptr;   // SNP-major (pass 1)
-    uint8_t* blk2 = nullptr;   // individual-major (pass 2)
+    int64_t strideT = 0;     // bytes of an individual-major row of blk2 (whole 32-byte chunks)
+    // tile-blocked copies (tile codes): block (tile, chunk) = 128 rows x 32 B
+    uint8_t* blk1 = nullptr;   // SNP-major: every genotype kernel (built at load)
+    uint8_t* blk2 = nullptr;   // individual-major: tensor-core pass 2, GRM build (first use)
     int nch1 = 0, ntiles1 = 0, nch2 = 0, ntiles2 = 0;
     // dense source
     float* grm = nullptr;    // N(N+1)/2
@@ -233,7 +230,8 @@ int dense_apply_df(globe_ctx* ctx, const double* Z, int k, double scale, double*
 int dense_diag(globe_ctx* ctx, double* d);
 
 // k_tc_geno.cu
-int ensure_gt(globe_ctx* ctx);
+int ensure_blk1(globe_ctx* ctx);   // SNP-major tile-blocked copy; frees the compacted rows
+int ensure_blk2(globe_ctx* ctx);   // individual-major tile-blocked copy (first tensor-core use)
 int load_bed_rows(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf, float max_miss,
                   int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep, globe_bed_info* info);
 int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out);

@@ -301,7 +301,7 @@ struct BuildBufs {
 static int grm_build_tc(globe_ctx* ctx, float* lt) {
     auto& g = ctx->gen;
     const int32_t N = ctx->coh.N;
-    GLOBE_RET(ensure_gt(ctx));
+    GLOBE_RET(ensure_blk2(ctx));
     const int nch = g.nch2;
     const int64_t kpad = (int64_t)nch * BK;
     const int rpc = rows_per_cta(GRM_NMMA);
@@ -391,7 +391,7 @@ static int grm_build_f64(globe_ctx* ctx, float* lt) {
     const int64_t nt = (N + 63) / 64;
     const int64_t ntiles = nt * (nt + 1) / 2;
     if (ntiles > 0x7FFFFFFFll) return set_err(ctx, GLOBE_ERR_ARG, "N too large for the FP64 GRM build");
-    GLOBE_RET(ensure_gt(ctx));
+    GLOBE_RET(ensure_blk1(ctx));
     ProfScope p(ctx, GLOBE_PROF_GRM_BUILD_GEMM);
     k_grm_f64<<<(unsigned)ntiles, 256, 0, ctx->stream>>>(g.blk1, g.Mk, g.nch1, g.zs, N, (double)g.Mk, lt);
     GLOBE_LAUNCHED(ctx, "k_grm_f64");

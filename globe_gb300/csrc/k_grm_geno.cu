@@ -194,7 +194,7 @@ int geno_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double*
         GLOBE_CK(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)N * k, ctx->stream));
         return GLOBE_OK;
     }
-    GLOBE_RET(ensure_gt(ctx));
+    GLOBE_RET(ensure_blk1(ctx));
     const int kcmax = 8;
     int kc0 = k < kcmax ? k : kcmax;
     double* W;
@@ -226,7 +226,7 @@ int geno_diag(globe_ctx* ctx, double* d) {
         GLOBE_CK(ctx, cudaMemsetAsync(d, 0, sizeof(double) * N, ctx->stream));
         return GLOBE_OK;
     }
-    GLOBE_RET(ensure_gt(ctx));
+    GLOBE_RET(ensure_blk1(ctx));
     int64_t ctas_x = div_up(N, P2_THREADS);
     int nsplit = pick_splits(ctas_x, g.Mk);
     int64_t s_per = ((g.Mk + nsplit - 1) / nsplit + P2_TS - 1) / P2_TS * P2_TS;

@@ -649,45 +649,47 @@ __global__ void k_combine2(const float* __restrict__ part, int nsplit, int nmma,
     }
 }
 
-// individual-major copy: Gt[i][b] holds SNPs 4b..4b+3 of individual i; 64 SNPs x 256 individuals per tile
-__global__ void k_transpose_codes(const uint8_t* __restrict__ G, int64_t Mk, int64_t stride, int32_t N,
-                                  uint8_t* __restrict__ Gt, int64_t strideT) {
-    __shared__ uint8_t t[64][64 + 4];
-    const int64_t s0 = (int64_t)blockIdx.x * 64;
-    for (int64_t i0 = (int64_t)blockIdx.y * 256; i0 < N; i0 += (int64_t)gridDim.y * 256) {
-        // load 64 rows x 64 bytes (256 individuals); beyond Mk -> 0xFF (genotype 0)
-        for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
-            const int rs = e >> 6, b = e & 63;
-            const int64_t s = s0 + rs, byte = i0 / 4 + b;
-            t[rs][b] = (s < Mk && byte < stride) ? G[s * stride + byte] : (uint8_t)0xFF;
-        }
-        __syncthreads();
-        // write 256 rows x 16 bytes (64 SNPs)
-        for (int e = threadIdx.x; e < 256 * 16; e += blockDim.x) {
-            const int il = e >> 4, ob = e & 15;
-            const int64_t i = i0 + il;
-            if (i < N) {
-                unsigned v = 0;
+// blk2 from blk1 by 2-bit block transposes.  blk1 block (t1, c1) holds SNP rows 128 t1 .. + 127
+// and individuals 128 c1 .. + 127 (32 bytes per row); blk2 block (t2, c2) holds individual rows
+// 128 t2 .. and SNPs 128 c2 .. -- the transpose of blk1 block (c2, t2).  Blocks of blk2 past blk1's
+// individual chunks are padding (tile code 10 everywhere, 0xAA).  One 4 KB block at a time per
+// CTA: rows staged in shared memory, each thread assembles 16 bytes (64 SNPs) of one individual.
+__global__ void __launch_bounds__(256) k_blk_transpose(const uint8_t* __restrict__ blk1, int nch1, int ntiles1,
+                                                       uint8_t* __restrict__ blk2, int nch2, int ntiles2) {
+    __shared__ uint8_t in[BM][PKB + 1];   // SNP rows x 32 bytes (+1: spreads banks)
+    const int64_t nblk = (int64_t)ntiles2 * nch2;
+    const int tid = threadIdx.x;
+    for (int64_t b = blockIdx.x; b < nblk; b += gridDim.x) {
+        const int64_t t2 = b / nch2;
+        const int c2 = (int)(b % nch2);
+        const int64_t t1 = c2, c1 = t2;
+        const bool have = t1 < ntiles1 && c1 < nch1;
+        {   // row r, logical half h (physical halves swapped when bit 2 of r is set)
+            const int r = tid >> 1, h = tid & 1;
+            uint4 v = make_uint4(0xAAAAAAAAu, 0xAAAAAAAAu, 0xAAAAAAAAu, 0xAAAAAAAAu);
+            if (have)
+                v = *reinterpret_cast<const uint4*>(blk1 + (((t1 * nch1 + c1) * BM + r) * 2 + (h ^ ((r >> 2) & 1))) * 16);
+            const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int rs = ob * 4 + q;
-                    const unsigned code = (t[rs][il >> 2] >> (2 * (il & 3))) & 3u;
-                    v |= code << (2 * q);
-                }
-                Gt[i * strideT + s0 / 4 + ob] = (uint8_t)v;
-            }
+            for (int q = 0; q < 16; ++q) in[r][h * 16 + q] = (uint8_t)(w[q >> 2] >> (8 * (q & 3)));
         }
         __syncthreads();
-    }
-}
-
-// pad bytes of Gt beyond the last SNP byte: 0xFF
-__global__ void k_fill_pad(uint8_t* __restrict__ Gt, int32_t N, int64_t strideT, int64_t from) {
-    const int64_t w = strideT - from;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)N * w;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = e / w, b = from + e % w;
-        Gt[i * strideT + b] = 0xFF;
+        {   // individual i, logical half hh: SNPs 64 hh .. + 63 of the block
+            const int i = tid >> 1, hh = tid & 1;
+            const int ib = i >> 2, sh = 2 * (i & 3);
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint32_t word = 0;
+#pragma unroll
+                for (int e = 0; e < 16; ++e)
+                    word |= (uint32_t)((in[64 * hh + 16 * q + e][ib] >> sh) & 3u) << (2 * e);
+                w[q] = word;
+            }
+            *reinterpret_cast<uint4*>(blk2 + (((t2 * nch2 + c2) * BM + i) * 2 + (hh ^ ((i >> 2) & 1))) * 16) =
+                make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        __syncthreads();
     }
 }
 
@@ -766,40 +768,37 @@ static int blockify(globe_ctx* ctx, const uint8_t* src, int64_t nrows, int64_t s
     return GLOBE_OK;
 }
 
-// The two tile-blocked copies (blk1 SNP-major, blk2 individual-major) from the compacted
-// SNP-major rows, which are freed afterwards: every genotype kernel reads the tile-blocked
-// copies.  Order: blk1, then the individual-major staging copy, then the rows are freed
-// before blk2 is laid out, so at most three copies are resident at once.
-int ensure_gt(globe_ctx* ctx) {
+// The SNP-major tile-blocked copy (blk1) from the compacted rows, which are freed: every
+// genotype kernel reads the tile-blocked copies.  Called when genotypes are loaded.
+int ensure_blk1(globe_ctx* ctx) {
     auto& g = ctx->gen;
-    if (g.blk2) return GLOBE_OK;
+    if (g.blk1) return GLOBE_OK;
     if (!g.geno) return set_err(ctx, GLOBE_ERR_STATE, "no genotype rows to lay out");
-    const int32_t N = ctx->coh.N;
-    if (!g.blk1) GLOBE_RET(blockify(ctx, g.geno, g.Mk, g.stride, &g.blk1, &g.nch1, &g.ntiles1));
-    g.strideT = ((g.Mk + 3) / 4 + PKB - 1) / PKB * PKB;
-    if (g.strideT < PKB) g.strideT = PKB;
-    if (g.gt) dfree(ctx, g.gt);   // a staging copy left by an earlier failed attempt
-    GLOBE_RET(dalloc(ctx, &g.gt, (size_t)N * g.strideT));
-    const int64_t snp_bytes = (g.Mk + 3) / 4;
-    if (g.Mk > 0) {
-        dim3 grid((unsigned)((g.Mk + 63) / 64), (unsigned)std::min<int64_t>((N + 255) / 256, 64));
-        k_transpose_codes<<<grid, 256, 0, ctx->stream>>>(g.geno, g.Mk, g.stride, N, g.gt, g.strideT);
-        GLOBE_LAUNCHED(ctx, "k_transpose_codes");
-    }
-    // bytes past the last 64-SNP tile written above
-    const int64_t written = (g.Mk + 63) / 64 * 16;
-    const int64_t from = std::min<int64_t>(std::max<int64_t>(snp_bytes, written), g.strideT);
-    if (from < g.strideT) {
-        k_fill_pad<<<1024, 256, 0, ctx->stream>>>(g.gt, N, g.strideT, from);
-        GLOBE_LAUNCHED(ctx, "k_fill_pad");
-    }
+    GLOBE_RET(blockify(ctx, g.geno, g.Mk, g.stride, &g.blk1, &g.nch1, &g.ntiles1));
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
     dfree(ctx, g.geno);   // the compacted rows live on as blk1
     g.geno = nullptr;
-    GLOBE_RET(blockify(ctx, g.gt, N, g.strideT, &g.blk2, &g.nch2, &g.ntiles2));
+    return GLOBE_OK;
+}
+
+// The individual-major tile-blocked copy (blk2, the tensor-core pass-2 operand) by block
+// transposes of blk1; built on the first tensor-core use, so FP64-only work holds one copy.
+int ensure_blk2(globe_ctx* ctx) {
+    auto& g = ctx->gen;
+    if (g.blk2) return GLOBE_OK;
+    GLOBE_RET(ensure_blk1(ctx));
+    const int32_t N = ctx->coh.N;
+    g.strideT = ((g.Mk + 3) / 4 + PKB - 1) / PKB * PKB;   // individual-major row: SNP bytes, whole chunks
+    if (g.strideT < PKB) g.strideT = PKB;
+    g.nch2 = (int)(g.strideT / PKB);
+    g.ntiles2 = (int)((N + BM - 1) / BM);
+    g.ntiles2 = (g.ntiles2 + 3) / 4 * 4;   // whole CTAs of four tiles
+    GLOBE_RET(dalloc(ctx, &g.blk2, (size_t)g.ntiles2 * g.nch2 * BM * PKB));
+    const int64_t nblk = (int64_t)g.ntiles2 * g.nch2;
+    k_blk_transpose<<<(unsigned)std::min<int64_t>(nblk, 152 * 16), 256, 0, ctx->stream>>>(g.blk1, g.nch1, g.ntiles1,
+                                                                                         g.blk2, g.nch2, g.ntiles2);
+    GLOBE_LAUNCHED(ctx, "k_blk_transpose");
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    dfree(ctx, g.gt);   // the row-major individual-major copy is only a staging step
-    g.gt = nullptr;
     return GLOBE_OK;
 }
 
@@ -980,7 +979,7 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
         GLOBE_CK(ctx, cudaMemsetAsync(out, 0, sizeof(double) * (size_t)N * k, ctx->stream));
         return GLOBE_OK;
     }
-    GLOBE_RET(ensure_gt(ctx));
+    GLOBE_RET(ensure_blk2(ctx));
     const int nd = ctx->digits;
     // near-equal groups of <= 256 / nd columns (MMA width <= 256).  Groups wider than
     // 192 / nd (MMA width > 192) run one row tile per CTA, which costs more per column than

@@ -79,8 +79,9 @@ def test_streamed_file_errors(gctx, tmp_path):
 
 
 def test_resident_genotype_copies():
-    """After loading, the genotypes are held as the two tile-blocked copies only (SNP-major
-    and individual-major); the compacted row-major copy and the staging buffers are gone."""
+    """After loading, the genotypes are held as the SNP-major tile-blocked copy only (the
+    compacted rows and the staging buffers are gone); the first tensor-core product adds
+    the individual-major copy, and FP64 work never needs it."""
     c = cohort(17, 2000, 10000, recs=("uniform", 3, 10), miss=0.01)
     N = c["N"]
     with Context(0) as ctx:
@@ -93,5 +94,11 @@ def test_resident_genotype_copies():
         blk1 = -(-Mk // 512) * 512 * (-(-((N + 3) // 4) // 32) * 32)
         blk2 = -(-N // 512) * 512 * (-(-((Mk + 3) // 4) // 32) * 32)
         tables = Mk * 8 * 6 + N * 8          # zs (4), f, inv per SNP; genetic diagonal
-        assert grew <= blk1 + blk2 + tables + (1 << 20)
-        assert grew >= blk1 + blk2
+        assert blk1 <= grew <= blk1 + tables + (1 << 20)
+        ctx.set_vc((0.6, 0.4, 0.4, 0.2, 0.2))
+        ctx.grm_apply(np.ones((N, 1)))        # FP64: no second copy
+        assert ctx.device_bytes() - before - grew < blk2 // 2
+        from globe_gb300 import PREC_MIXED
+        ctx.set_precision(PREC_MIXED)
+        ctx.grm_apply(np.ones((N, 1)))        # tensor cores: the individual-major copy appears
+        assert ctx.device_bytes() - before >= blk1 + blk2
