@@ -134,7 +134,7 @@ static void free_cohort(globe_ctx* ctx) {
 static void free_genetic(globe_ctx* ctx) {
     auto& g = ctx->gen;
     for (void* p : {(void*)g.geno, (void*)g.zs, (void*)g.f, (void*)g.inv, (void*)g.grm, (void*)g.gdiag,
-                    (void*)g.blk1, (void*)g.blk2})
+                    (void*)g.blk1, (void*)g.blk2, (void*)g.adig})
         dfree(ctx, p);
     g = Genetic();
     ctx->precond_ok = false;

@@ -62,6 +62,12 @@ struct Genetic {
     int nch1 = 0, ntiles1 = 0, nch2 = 0, ntiles2 = 0;
     // dense source
     float* grm = nullptr;    // N(N+1)/2
+    // digit planes of the dense GRM for the tensor-core product (first GLOBE_PREC_MIXED use):
+    // adig_da planes of adig_rows / adig_da rows x adig_np bytes, A ~ 2^adig_e sum_d a_d 32^-d
+    uint8_t* adig = nullptr;
+    int adig_state = 0;      // 0 not built, 1 ready, -1 unusable (memory, non-finite A): double-float kernel
+    int adig_da = 0, adig_e = 0;
+    int64_t adig_np = 0, adig_rows = 0;
     // both
     double* gdiag = nullptr; // A_ii
     bool gdiag_ok = false;
@@ -228,6 +234,10 @@ int geno_diag(globe_ctx* ctx, double* d);
 int dense_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 int dense_apply_df(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 int dense_diag(globe_ctx* ctx, double* d);
+
+// k_tc_dense.cu
+int dense_digit_planes(globe_ctx* ctx);   // (re)builds the digit planes for the context's digit count
+int dense_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 
 // k_tc_geno.cu
 int ensure_blk1(globe_ctx* ctx);   // SNP-major tile-blocked copy; frees the compacted rows

@@ -32,7 +32,7 @@
 // tiles repeat (kpos()).
 // Every mbarrier wait is bounded (globaltimer); on timeout the CTA records
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
-#include "tc_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace globe {
 namespace tc {
@@ -46,17 +46,11 @@ namespace tc {
 #ifndef TC_DSTAGES
 #define TC_DSTAGES 2
 #endif
-#ifndef TC_SLEEP
-#define TC_SLEEP 1       // producers / MMA issuer suspend in their waits
-#endif
 #ifndef TC_DEC_PRE
 #define TC_DEC_PRE 8     // 16-byte units a decoder warp decodes before it waits for its TMEM slot
 #endif
 #ifndef TC_STW
 #define TC_STW 16        // columns per tcgen05.st of a decoded unit (16, or 8 in two stores)
-#endif
-#ifndef TC_POLL8
-#define TC_POLL8 0       // polling waits make 8 try_waits per loop iteration
 #endif
 #ifndef TC_SLEEP_DEC
 #define TC_SLEEP_DEC 1   // decoders suspend in their waits too
@@ -85,14 +79,10 @@ struct Geo {
     static constexpr int DPT = MT >= 2 ? 4 : 8;            // warps of one set per tile (adfull count)
     static constexpr int ES = MT >= 2 ? 2 : 4;             // warps sharing a (tile, quadrant) epilogue
 };
-constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
 // byte tables of the decode (prmt operands a, b): a = {2.0, 1.0, 0, 0}, b = {1.0, 0, 0, 0} in e4m3
 constexpr uint32_t LUT_A = 0x00003840u;
 constexpr uint32_t LUT_B = 0x00000038u;
 
-__host__ __device__ constexpr int ncols_alloc(int n) {
-    return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
-}
 
 // MT row tiles of 128 share every digit tile.  TMEM columns: accumulators
 // [0, MT*NMMA), then DSTAGES x MT decoded A tiles of 32 columns (K = 128 e4m3).
@@ -106,132 +96,7 @@ struct __align__(1024) Smem {
     int abort;
 };
 
-// ---- PTX wrappers ---------------------------------------------------------
 
-__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ uint64_t gtime() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(n) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(saddr(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// up to 8 try_waits in straight-line PTX, leaving at the first that succeeds: one call
-// costs a few integer instructions however many polls it makes
-__device__ __forceinline__ bool mbar_try8(uint64_t* b, uint32_t parity) {
-    uint32_t ok;
-#define GLOBE_TRY1 " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n @p bra.uni DONE;\n"
-    asm volatile("{\n .reg .pred p;\n" GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1
-                 GLOBE_TRY1 " mov.u32 %0, 0;\n bra.uni END;\n DONE:\n mov.u32 %0, 1;\n END:\n}\n"
-                 : "=r"(ok)
-                 : "r"(saddr(b)), "r"(parity)
-                 : "memory");
-#undef GLOBE_TRY1
-    return ok != 0;
-}
-// try_wait that may suspend the thread until the phase completes (hint in ns)
-__device__ __forceinline__ bool mbar_try_sleep(uint64_t* b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(saddr(b)), "r"(parity), "r"(200000u)
-        : "memory");
-    return ok != 0;
-}
-// bounded wait; false on timeout or when another role aborted.  The clock
-// and the abort flag are read only every 256 polls, off the fast path.
-template <bool SLEEP = (TC_SLEEP != 0)>
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* abort, unsigned* err, unsigned bit) {
-    if (mbar_try(b, parity)) return true;
-    uint64_t t0 = 0;
-    for (uint32_t spins = 1;; ++spins) {
-        if (SLEEP ? mbar_try_sleep(b, parity) : (TC_POLL8 ? mbar_try8(b, parity) : mbar_try(b, parity))) return true;
-        if ((spins & 255u) == 0) {
-            if (*(volatile int*)abort) return false;
-            const uint64_t t = gtime();
-            if (t0 == 0) t0 = t;
-            else if (t - t0 > WAIT_LIMIT_NS) {
-                *(volatile int*)abort = 1;
-                atomicOr(err, bit);
-                return false;
-            }
-        }
-    }
-}
-// bounded wait used on the way out (ignores the abort flag)
-__device__ __forceinline__ void mbar_drain(uint64_t* b, uint32_t parity) {
-    const uint64_t t0 = gtime();
-    while (!mbar_try(b, parity) && gtime() - t0 < WAIT_LIMIT_NS) {
-    }
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            saddr(dst)),
-        "l"((uint64_t)tm), "r"(x), "r"(y), "r"(saddr(bar))
-        : "memory");
-}
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     saddr(dst)),
-                 "l"(src), "r"(bytes), "r"(saddr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(dst)), "r"(ncols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void mma_f8(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void mma_f8_ta(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
-        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-            taddr),
-        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
-        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
-        : "memory");
-}
-__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* v) {
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
-                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
-                 : "memory");
-}
 // one decoded 16-byte unit (16 columns of one lane quadrant)
 __device__ __forceinline__ void tmem_st_unit(uint32_t taddr, const uint32_t (&v)[16]) {
     if (TC_STW == 8) {
@@ -241,29 +106,6 @@ __device__ __forceinline__ void tmem_st_unit(uint32_t taddr, const uint32_t (&v)
         tmem_st16(taddr, v);
     }
 }
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
-          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-// K-major operand, 128-byte swizzle: 8-row atoms of 1024 B (SBO), start advanced by 32 B per K=32 step
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
-    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;             // LBO (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;   // SBO
-    d |= (uint64_t)1 << 46;             // descriptor version
-    d |= (uint64_t)2 << 61;             // SWIZZLE_128B
-    return d;
-}
-
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
     uint32_t r;
     asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
@@ -553,48 +395,6 @@ __global__ void k_col_finish(const double* __restrict__ pmax, const double* __re
     }
 }
 
-
-// ND digits of X (n x k, FP64) into D[(c*ND + j) * kpad + kpos(r)]  (e4m3); every position
-// in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
-// fills 4 consecutive positions P..P+3 (a 32-bit word): within a group of 16, position
-// P < 8 holds row 2P and P >= 8 holds row 2(P-8)+1 (the inverse of kpos).
-// x 2^-e is rounded once to the integer I = round(x 2^-e 32^(ND-1)), |I| <= 2^(5 ND - 1); its
-// balanced base-32 digits are peeled off from the least significant end in integer
-// arithmetic (d = ((I + 16) mod 32) - 16, in [-16, 15]); the leading digit is what
-// remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (ND-1) fraction bits.
-template <int ND>
-__global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
-                         uint8_t* __restrict__ D, int64_t kpad) {
-    const int c = blockIdx.y;
-    const double sc = ldexp(1.0, DBITS * (ND - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
-    const int64_t nw = kpad >> 2;
-    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t P = w << 2, base = P & ~(int64_t)15;
-        const int pl = (int)(P & 15);
-        long long I[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int pq = pl + q;
-            const int64_t src = base + (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1);
-            I[q] = src < n ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
-        }
-        uint32_t word[ND];
-#pragma unroll
-        for (int j = 0; j < ND; ++j) word[j] = 0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-#pragma unroll
-            for (int j = ND - 1; j > 0; --j) {
-                const int d = (int)((I[q] + DHALF) & (2 * DHALF - 1)) - DHALF;
-                I[q] = (I[q] - d) >> DBITS;   // exact: I - d is a multiple of 32
-                word[j] |= e4m3_int(d) << (8 * q);
-            }
-            word[0] |= e4m3_int((int)I[q]) << (8 * q);
-        }
-#pragma unroll
-        for (int j = 0; j < ND; ++j) *reinterpret_cast<uint32_t*>(D + ((int64_t)c * ND + j) * kpad + P) = word[j];
-    }
-}
 
 // pass-1 epilogue in FP64: u[s,c] = inv_s^2 (2^e_c sum_j 32^-j P1 - 2 f_s S_c); partial max|u|, sum 2 f u
 template <int ND>

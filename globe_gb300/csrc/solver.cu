@@ -26,7 +26,7 @@ int grm_apply_dev(globe_ctx* ctx, const double* Z, int k, double* out) {
         return geno_apply_f64(ctx, Z, k, scale, out);
     }
     if (ctx->gen.src == GSRC_DENSE)
-        return ctx->prec == GLOBE_PREC_MIXED ? dense_apply_df(ctx, Z, k, ctx->vc[1], out)
+        return ctx->prec == GLOBE_PREC_MIXED ? dense_apply_tc(ctx, Z, k, ctx->vc[1], out)
                                              : dense_apply_f64(ctx, Z, k, ctx->vc[1], out);
     return set_err(ctx, GLOBE_ERR_STATE, "no genetic relationship source loaded");
 }

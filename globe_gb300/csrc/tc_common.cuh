@@ -104,6 +104,48 @@ __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld
 __global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
                              double* __restrict__ colinfo);
 
+// ND digits of X (n x k, FP64) into D[(c*ND + j) * kpad + kpos(r)]  (e4m3); every position
+// in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
+// fills 4 consecutive positions P..P+3 (a 32-bit word): within a group of 16, position
+// P < 8 holds row 2P and P >= 8 holds row 2(P-8)+1 (the inverse of kpos).
+// x 2^-e is rounded once to the integer I = round(x 2^-e 32^(ND-1)), |I| <= 2^(5 ND - 1); its
+// balanced base-32 digits are peeled off from the least significant end in integer
+// arithmetic (d = ((I + 16) mod 32) - 16, in [-16, 15]); the leading digit is what
+// remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (ND-1) fraction bits.
+template <int ND>
+__global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
+                         uint8_t* __restrict__ D, int64_t kpad) {
+    const int c = blockIdx.y;
+    const double sc = ldexp(1.0, DBITS * (ND - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
+    const int64_t nw = kpad >> 2;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t P = w << 2, base = P & ~(int64_t)15;
+        const int pl = (int)(P & 15);
+        long long I[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int pq = pl + q;
+            const int64_t src = base + (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1);
+            I[q] = src < n ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
+        }
+        uint32_t word[ND];
+#pragma unroll
+        for (int j = 0; j < ND; ++j) word[j] = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int j = ND - 1; j > 0; --j) {
+                const int d = (int)((I[q] + DHALF) & (2 * DHALF - 1)) - DHALF;
+                I[q] = (I[q] - d) >> DBITS;   // exact: I - d is a multiple of 32
+                word[j] |= e4m3_int(d) << (8 * q);
+            }
+            word[0] |= e4m3_int((int)I[q]) << (8 * q);
+        }
+#pragma unroll
+        for (int j = 0; j < ND; ++j) *reinterpret_cast<uint32_t*>(D + ((int64_t)c * ND + j) * kpad + P) = word[j];
+    }
+}
+
 }  // namespace tc
 
 // Extra launch dimension of k_tc_gemm: gridDim.z = nz independent digit

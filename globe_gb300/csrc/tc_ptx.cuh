@@ -1,0 +1,172 @@
+// tc_ptx.cuh -- inline-PTX wrappers of the tensor-core kernels: mbarriers with bounded
+// waits, TMA and bulk copies, tcgen05 (TMEM allocation, MMA, loads / stores, commit) and the
+// shared-memory matrix descriptor.  Every wait gives up after WAIT_LIMIT_NS, sets an abort
+// flag the other roles of the CTA poll, and records an error bit for the host.
+#pragma once
+#include "tc_common.cuh"
+
+namespace globe {
+namespace tc {
+
+#ifndef TC_SLEEP
+#define TC_SLEEP 1       // producers / MMA issuer suspend in their waits
+#endif
+#ifndef TC_POLL8
+#define TC_POLL8 0       // polling waits make 8 try_waits per loop iteration
+#endif
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s per wait
+
+__host__ __device__ constexpr int ncols_alloc(int n) {
+    return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : n <= 256 ? 256 : 512;
+}
+
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint64_t gtime() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t n) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(n) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// up to 8 try_waits in straight-line PTX, leaving at the first that succeeds: one call
+// costs a few integer instructions however many polls it makes
+__device__ __forceinline__ bool mbar_try8(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+#define GLOBE_TRY1 " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n @p bra.uni DONE;\n"
+    asm volatile("{\n .reg .pred p;\n" GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1 GLOBE_TRY1
+                 GLOBE_TRY1 " mov.u32 %0, 0;\n bra.uni END;\n DONE:\n mov.u32 %0, 1;\n END:\n}\n"
+                 : "=r"(ok)
+                 : "r"(saddr(b)), "r"(parity)
+                 : "memory");
+#undef GLOBE_TRY1
+    return ok != 0;
+}
+// try_wait that may suspend the thread until the phase completes (hint in ns)
+__device__ __forceinline__ bool mbar_try_sleep(uint64_t* b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(b)), "r"(parity), "r"(200000u)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; false on timeout or when another role aborted.  The clock
+// and the abort flag are read only every 256 polls, off the fast path.
+template <bool SLEEP = (TC_SLEEP != 0)>
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* abort, unsigned* err, unsigned bit) {
+    if (mbar_try(b, parity)) return true;
+    uint64_t t0 = 0;
+    for (uint32_t spins = 1;; ++spins) {
+        if (SLEEP ? mbar_try_sleep(b, parity) : (TC_POLL8 ? mbar_try8(b, parity) : mbar_try(b, parity))) return true;
+        if ((spins & 255u) == 0) {
+            if (*(volatile int*)abort) return false;
+            const uint64_t t = gtime();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > WAIT_LIMIT_NS) {
+                *(volatile int*)abort = 1;
+                atomicOr(err, bit);
+                return false;
+            }
+        }
+    }
+}
+// bounded wait used on the way out (ignores the abort flag)
+__device__ __forceinline__ void mbar_drain(uint64_t* b, uint32_t parity) {
+    const uint64_t t0 = gtime();
+    while (!mbar_try(b, parity) && gtime() - t0 < WAIT_LIMIT_NS) {
+    }
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            saddr(dst)),
+        "l"((uint64_t)tm), "r"(x), "r"(y), "r"(saddr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_f8(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void mma_f8_ta(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]),
+        "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
+                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// K-major operand, 128-byte swizzle: 8-row atoms of 1024 B (SBO), start advanced by 32 B per K=32 step
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // LBO (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // SBO
+    d |= (uint64_t)1 << 46;             // descriptor version
+    d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+    return d;
+}
+
+}  // namespace tc
+}  // namespace globe

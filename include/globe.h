@@ -45,8 +45,12 @@ extern "C" {
 #define GLOBE_PREC_MIXED 1  /* genotype GRM product on the FP8 tensor cores with exact
                                base-32 digit slicing of the right-hand sides (9 digits =
                                45 bits by default, matches FP64 to ~1e-13; see
-                               globe_set_digits); dense GRM in double-float FP32
-                               arithmetic (~48 bits) */
+                               globe_set_digits); dense GRM on the same tensor
+                               cores, A held as min(7, digits) e4m3 digit planes of
+                               one fixed-point grid (7 N^2 bytes; A within 2^-34
+                               max|A|), or in double-float FP32 arithmetic (~48 bits)
+                               when the planes do not fit in free device memory or
+                               A has a non-finite entry */
 
 /* models (globe_set_model) */
 #define GLOBE_MODEL_FULL 0     /* random intercept and slope per individual (runAIREML) */
@@ -201,7 +205,11 @@ int globe_set_precision(globe_ctx* ctx, int precision);
  * times that unit of the exact product (nd = 9: ~1e-13, nd = 6: ~5e-9,
  * nd = 5: ~1.5e-7, the reference's own FP32 level).  Fewer digits
  * mean fewer tensor-core columns: 20 columns take MMA width 192 at nd = 9 and
- * 128 at nd = 6.  No reference counterpart (the reference works in FP32). */
+ * 128 at nd = 6.  A dense GRM is rounded the same way, to min(7, nd) digits
+ * on one grid for the whole matrix (a multiple of 2^-(5(min(7,nd)-1)+3) max|A|;
+ * nd >= 7: ~1e-10 relative product error, nd = 6: ~2e-8); its digit planes are
+ * rebuilt on the first mixed product after the count changes.
+ * No reference counterpart (the reference works in FP32). */
 int globe_set_digits(globe_ctx* ctx, int nd);
 int globe_get_digits(const globe_ctx* ctx);
 

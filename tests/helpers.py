@@ -114,3 +114,27 @@ def tc_product_emulation(G, f, inv, Z, scale, nd):
         P = G.T @ D.T
         out[:, c] = scale * (np.ldexp(P @ w, e) - (2 * f * U[:, c]).sum())
     return out
+
+
+def lt_to_full(lt, N):
+    """The symmetric N x N matrix of a packed lower triangle (row-major, i >= j)."""
+    A = np.zeros((N, N))
+    A[np.tril_indices(N)] = np.asarray(lt, np.float64)
+    return A + np.tril(A, -1).T
+
+
+def dense_tc_emulation(A, Z, scale, nd, da=None):
+    """The tensor-core dense GRM product in exact arithmetic: A rounded to the grid of its
+    da = min(7, nd) digit planes (k_dense_digits: I = round(A 2^-e 32^(da-1)), max|A| 2^-e in
+    [8, 16)), each column of Z to nd base-32 digits (k_digits); then one FP64 product."""
+    A = np.asarray(A, np.float64)
+    da = min(7, nd) if da is None else da
+    mx = np.abs(A).max()
+    e = (np.frexp(mx)[1] - 4) if mx > 0 else -4
+    Ar = np.ldexp(np.rint(np.ldexp(A, 5 * (da - 1) - e)), e - 5 * (da - 1))
+    w = 32.0 ** -np.arange(nd)
+    Zr = np.zeros_like(np.asarray(Z, np.float64))
+    for c in range(Zr.shape[1]):
+        D, ez = tc_digits(Z[:, c], nd)
+        Zr[:, c] = np.ldexp(D.T @ w, ez)
+    return scale * (Ar @ Zr)

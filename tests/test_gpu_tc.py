@@ -88,26 +88,80 @@ def test_mixed_precision_covers_every_grm_product(gctx, orc):
     assert rel(res[G.PREC_MIXED]["theta"], res[G.PREC_FP64]["theta"]) < 1e-6
 
 
-@pytest.mark.parametrize("N", [203, 2000])
-def test_dense_mixed_matches_fp64(gctx, orc, N):
-    """Dense GRM under GLOBE_PREC_MIXED (double-float FP32 arithmetic) vs the FP64 oracle,
-    per column; N=2000 exercises the split J range, k=20 two column chunks."""
-    coh = cohort(31 + N, N, 600, recs=("uniform", 1, 3), miss=0.02)
+def _dense(gctx, orc, N, seed):
+    coh = cohort(seed, N, 600, recs=("uniform", 1, 3), miss=0.02)
     grm = synth.grm_from_packed(coh["packed"], N)
     indiv = coh["indiv"].astype(np.int32)
     gctx.load_records(indiv, coh["X"], coh["y"], N)
     gctx.load_grm(grm, N)
     gctx.set_vc(VC_F)
-    s = orc.Solver(indiv, coh["X"], coh["y"], N, VC_F, grm_lt=grm)
+    return grm, orc.Solver(indiv, coh["X"], coh["y"], N, VC_F, grm_lt=grm)
+
+
+@pytest.mark.parametrize("N", [129, 203, 2000])
+def test_dense_mixed_matches_emulation(gctx, orc, N):
+    """Dense GRM under GLOBE_PREC_MIXED (tensor cores): the product of A rounded to its 7
+    digit planes (within 2^-34 max|A|) and each column of Z rounded to 9 base-32 digits,
+    equal to that product evaluated in FP64 (the MMA sums are exact integers); and within
+    ~1e-10 of the FP64 oracle (the rounding of A).  N = 129, 203 pad the last row tile
+    and K chunk; k = 40 runs two column groups (MMA widths 16 .. 192)."""
+    from helpers import dense_tc_emulation, lt_to_full
+    grm, s = _dense(gctx, orc, N, 31 + N)
+    A = lt_to_full(grm, N)
     rng = np.random.default_rng(N)
     try:
         gctx.set_precision(G.PREC_MIXED)
-        for k in (1, 5, 16, 20):
+        for k in (1, 5, 16, 21, 40):
             Z = rng.standard_normal((N, k)) * np.logspace(-3, 3, k)
             got, ref = gctx.grm_apply(Z), s.grm_apply(Z)
-            assert max(rel(got[:, c], ref[:, c]) for c in range(k)) < 1e-11, k
+            emu = dense_tc_emulation(A, Z, VC_F[1], 9)
+            assert max(rel(got[:, c], emu[:, c]) for c in range(k)) < 1e-13, k
+            assert max(rel(got[:, c], ref[:, c]) for c in range(k)) < 1e-9, k
     finally:
         gctx.set_precision(G.PREC_FP64)
+
+
+def test_dense_mixed_digit_count(gctx, orc):
+    """The digit count sets the planes of A too (min(7, digits)); changing it rebuilds them."""
+    from helpers import dense_tc_emulation, lt_to_full
+    N = 300
+    grm, s = _dense(gctx, orc, N, 5)
+    A = lt_to_full(grm, N)
+    Z = np.random.default_rng(2).standard_normal((N, 6))
+    try:
+        gctx.set_precision(G.PREC_MIXED)
+        for nd in (4, 9, 2, 6):
+            gctx.set_digits(nd)
+            got = gctx.grm_apply(Z)
+            emu = dense_tc_emulation(A, Z, VC_F[1], nd)
+            assert max(rel(got[:, c], emu[:, c]) for c in range(6)) < 1e-13, nd
+    finally:
+        gctx.set_digits(9)
+        gctx.set_precision(G.PREC_FP64)
+
+
+def test_dense_mixed_nonfinite_entry(gctx, orc):
+    """A non-finite GRM entry has no digit planes: the product propagates it (double-float
+    kernel), into the rows of both of its indices, as the FP64 product does."""
+    N = 150
+    grm, _ = _dense(gctx, orc, N, 8)
+    grm = grm.copy()
+    i0, j0 = 40, 7
+    grm[i0 * (i0 + 1) // 2 + j0] = np.nan
+    gctx.load_grm(grm, N)
+    Z = np.random.default_rng(1).standard_normal((N, 3))
+    out = {}
+    try:
+        for prec in (G.PREC_MIXED, G.PREC_FP64):
+            gctx.set_precision(prec)
+            out[prec] = gctx.grm_apply(Z)
+    finally:
+        gctx.set_precision(G.PREC_FP64)
+    for o in out.values():
+        bad = ~np.isfinite(o).all(axis=1)
+        assert set(np.flatnonzero(bad)) == {i0, j0}
+    ok = np.isfinite(out[G.PREC_FP64])
+    assert rel(out[G.PREC_MIXED][ok], out[G.PREC_FP64][ok]) < 1e-11
 
 
 @pytest.mark.parametrize("nd", [2, 3, 4, 5, 6, 7, 8, 9])

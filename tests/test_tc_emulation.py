@@ -155,3 +155,44 @@ def test_digit_count_error_bound(orc):
     for nd in range(2, 10):
         out = tc_product_emulation(Gk, s.f, s.inv_std, Z, 0.4 / keep.sum(), nd)
         assert max(rel(out[:, c], ref[:, c]) for c in range(3)) < 8 * 2.0 ** -(5 * (nd - 1) + 4), nd
+
+
+def _dense_plane_digits(A, da):
+    """k_dense_digits on the CPU: the da balanced base-32 digit planes of A (plane 0 most
+    significant) and the exponent e, max|A| 2^-e in [8, 16)."""
+    mx = np.abs(A).max()
+    e = (np.frexp(mx)[1] - 4) if mx > 0 else -4
+    I = np.rint(np.ldexp(A, 5 * (da - 1) - e)).astype(np.int64)
+    P = np.zeros((da,) + A.shape, np.int64)
+    for d in range(da - 1, 0, -1):
+        dg = ((I + 16) & 31) - 16
+        P[d] = dg
+        I = (I - dg) >> 5
+    P[0] = I
+    return P, e
+
+
+def test_dense_digit_planes_and_bound(orc):
+    """The dense tensor-core product (globe_gb300/csrc/k_tc_dense.cu) on the CPU: A's digit
+    planes are integers in [-16, 16], they rebuild A to within 2^-34 max|A| (7 planes), every
+    plane-by-digit partial sum is an exact FP32 integer (|sum| <= 256 K), and the
+    recombination sum_d 32^-d R_d matches the FP64 oracle product to ~1e-10."""
+    from globe_gb300 import synth
+    from helpers import lt_to_full, tc_digits
+    N = 333
+    c = cohort(3, N, 500, recs=("uniform", 1, 2), miss=0.02)
+    lt = synth.grm_from_packed(c["packed"], N)
+    A = lt_to_full(lt, N)
+    P, e = _dense_plane_digits(A, 7)
+    assert np.abs(P).max() <= 16
+    Ar = np.ldexp(np.tensordot(32.0 ** -np.arange(7), P.astype(np.float64), 1), e)
+    assert np.abs(Ar - A).max() <= 2.0 ** -34 * np.abs(A).max()
+    z = np.random.default_rng(1).standard_normal(N)
+    D, ez = tc_digits(z, NDIG)
+    R = np.einsum("dij,kj->dik", P.astype(np.float64), D)      # plane x row x z digit
+    assert np.abs(R).max() <= 256 * N and np.array_equal(R, np.rint(R))
+    assert np.array_equal(R.astype(np.float32).astype(np.float64), R)
+    y = np.ldexp(np.einsum("dik,d,k->i", R, 32.0 ** -np.arange(7), 32.0 ** -np.arange(NDIG)), e + ez)
+    indiv = c["indiv"].astype(np.int32)
+    s = orc.Solver(indiv, c["X"], c["y"], N, (0.6, 1.0, 0.4, 0.2, 0.2), grm_lt=lt)
+    assert rel(y, s.grm_apply(z[:, None])[:, 0]) < 1e-9
