@@ -239,20 +239,46 @@ __global__ void __launch_bounds__(256) k_dense_digits(const float* __restrict__ 
     }
 }
 
-// out[i,c] = sA sum_d 32^-d R_d(i,c), R_d = 2^e_c sum_j 32^-j P[plane d rows] (recombine<ND>);
-// sA = scale 2^eA.  Horner from the least significant plane: every step is one FP64 rounding.
+// out[i,c] = sA 2^e_c sum_{d,j} 32^-(d+j) P[plane d, digit j](i,c), sA = scale 2^eA.  Each
+// split partial is an exact integer in FP32; they are summed in int64 by total weight
+// s = d + j (T_s, |T_s| <= 7 * 256 N), and the weights folded in three exact int64 chunks of
+// five (C_q = sum_{s=5q}^{5q+4} 32^(5q+4-s) T_s, |C_q| < 2^31 N): three conversions and two
+// FP64 additions per value instead of a recombination per plane.
 template <int ND>
 __global__ void k_dense_combine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int32_t N,
                                 int64_t np, int da, const double* __restrict__ colinfo, double sA,
                                 double* __restrict__ out, int64_t ldo) {
+    constexpr int NT = DA_MAX + ND - 1;
+    static_assert(NT <= 15, "three chunks of five weights");
     const int c = blockIdx.y;
-    double s_hi, s_lo;
-    recombine_scales<ND>((int)colinfo[2 * c], s_hi, s_lo);
+    const double s0 = sA * ldexp(1.0, (int)colinfo[2 * c] - 20);   // 2^(e_c - 5*4) for chunk 0
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        double v = 0.0;
-        for (int d = da - 1; d >= 0; --d)
-            v = v * (1.0 / 32.0) + recombine<ND>(part, nsplit, nmma, ldp, c, (int64_t)d * np + i, s_hi, s_lo);
-        out[i + c * ldo] = sA * v;
+        long long T[NT];
+#pragma unroll
+        for (int q = 0; q < NT; ++q) T[q] = 0;
+        // per plane: the ND digit loads of split 0 issued together, further splits after
+#pragma unroll
+        for (int d = 0; d < DA_MAX; ++d) {
+            if (d < da) {
+                const float* src = part + (int64_t)c * ND * ldp + (int64_t)d * np + i;
+                long long pj[ND];
+#pragma unroll
+                for (int j = 0; j < ND; ++j) pj[j] = (long long)__float2int_rn(src[(int64_t)j * ldp]);
+                for (int y = 1; y < nsplit; ++y) {
+#pragma unroll
+                    for (int j = 0; j < ND; ++j)
+                        pj[j] += (long long)__float2int_rn(src[((int64_t)y * nmma + j) * ldp]);
+                }
+#pragma unroll
+                for (int j = 0; j < ND; ++j) T[d + j] += pj[j];
+            }
+        }
+        long long C[3] = {0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+#pragma unroll
+            for (int m = 0; m < 5; ++m) C[q] = C[q] * 32 + (5 * q + m < NT ? T[5 * q + m] : 0);
+        out[i + c * ldo] = s0 * ((double)C[0] + ldexp((double)C[1], -25) + ldexp((double)C[2], -50));
     }
 }
 
@@ -400,9 +426,10 @@ static int dense_group(globe_ctx* ctx, const double* Z, int kg, double scale, do
     CUtensorMap mA, mB;
     GLOBE_RET(make_map(ctx, &mA, g.adig, (uint64_t)np, (uint64_t)rows, BK, BM, true));
     GLOBE_RET(make_map(ctx, &mB, D, (uint64_t)np, (uint64_t)nmma, BK, (uint32_t)nmma, true));
-    k_col_maxsum<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
+    const int nz = col_parts(N);
+    k_col_maxsum<<<dim3(nz, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
     GLOBE_LAUNCHED(ctx, "k_col_maxsum");
-    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col);
+    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nz, kg, col);
     GLOBE_LAUNCHED(ctx, "k_col_finish");
     if (nmma > kg * ND)   // digit rows past the kg columns stay zero
         GLOBE_CK(ctx, cudaMemsetAsync(D + (size_t)kg * ND * np, 0, (size_t)(nmma - kg * ND) * np, ctx->stream));

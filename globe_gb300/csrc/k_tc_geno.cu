@@ -716,9 +716,10 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     GLOBE_RET(make_map(ctx, &mB1, D1, (uint64_t)kpad1, (uint64_t)nmma, BK, (uint32_t)nmma, true));
     GLOBE_RET(make_map(ctx, &mB2, D2, (uint64_t)kpad2, (uint64_t)nmma, BK, (uint32_t)nmma, true));
     // ---- digits of Z
-    k_col_maxsum<<<dim3(nbr, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
+    const int nz = col_parts(N);
+    k_col_maxsum<<<dim3(nz, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
     GLOBE_LAUNCHED(ctx, "k_col_maxsum");
-    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col1);
+    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nz, kg, col1);
     GLOBE_LAUNCHED(ctx, "k_col_finish");
     // digit rows past the kg columns stay zero
     if (nmma > kg * ND)

@@ -97,6 +97,13 @@ __device__ __forceinline__ void recombine_scales(int e, double& s_hi, double& s_
     s_lo = ldexp(1.0, e - DBITS * (ND - 1));
 }
 
+// CTAs per column of k_col_maxsum for n rows: ~8 values per thread (its FP64 reduction runs
+// on GB300's small FP64 pipe, so surplus CTAs cost more than they hide), at most 304
+__host__ __forceinline__ int col_parts(int64_t n) {
+    const int64_t p = (n + 2047) / 2048;
+    return (int)(p < 1 ? 1 : (p > 304 ? 304 : p));
+}
+
 // per-column max |x| and sum over n rows (partials per CTA); colinfo[c] = {exponent e with
 // max |x 2^-e| < 16, column sum} from those partials (k_tc_geno.cu)
 __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld, double* __restrict__ pmax,
