@@ -1,5 +1,6 @@
-// k_grm_dense.cu -- dense GRM product from the packed lower triangle (FP64, or
-// double-float FP32 arithmetic under GLOBE_PREC_MIXED).
+// k_grm_dense.cu -- dense GRM product from the packed lower triangle: FP64
+// (GLOBE_PREC_FP64), and double-float FP32 arithmetic for GLOBE_PREC_MIXED when the
+// tensor-core digit planes of k_tc_dense.cu cannot be held (device memory, non-finite A).
 //
 //   out (N x k) = scale * A Z,  A(i,j) = lt[max(i,j)(max(i,j)+1)/2 + min(i,j)]
 //   (PCGsolver.cpp:1202-1213, varCompEst.cpp:531-558)
