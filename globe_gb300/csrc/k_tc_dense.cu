@@ -63,7 +63,7 @@ struct __align__(1024) DSmem {
 template <int NMMA>
 __global__ void __launch_bounds__(256, 1)
     k_tc_dense(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int rows,
-               int nchunks, int cps, float* __restrict__ part, int64_t ldp, unsigned* __restrict__ err) {
+               int nchunks, int cps, float* __restrict__ part, int64_t ldp, unsigned* __restrict__ err, int stall) {
     constexpr int ST = DGeo<NMMA>::STAGES;
     static_assert(NMMA % 16 == 0 && NMMA >= 16 && NMMA <= 256, "NMMA");
     constexpr uint32_t NCOLS = ncols_alloc(DMT * NMMA);
@@ -96,6 +96,10 @@ __global__ void __launch_bounds__(256, 1)
             for (int it = 0; it < nloc; ++it) {
                 const int s = it % ST, n = it / ST;
                 if (n > 0 && !mbar_wait(&S.empty[s], (n - 1) & 1, abort, err, 1u)) break;
+                if (stall && it == 0) {   // test hook: the stage is never loaded, so its waits run out
+                    issued = 1;
+                    continue;
+                }
                 mbar_expect_tx(&S.full[s], DGeo<NMMA>::ABYTES + DGeo<NMMA>::BBYTES);
                 const int x = (c0 + it) * BK;
                 tma_load_2d(S.a[s][0], &tmA, x, row0, &S.full[s]);
@@ -306,7 +310,7 @@ int dense_digit_planes(globe_ctx* ctx) {
         g.adig_da = da;
         return GLOBE_OK;
     }
-    unsigned* mx;
+    unsigned* mx;   // words 1-2 of the error-flag slot (word 0 is the kernels' flag): max |A| bits, non-finite
     GLOBE_RET(ws(ctx, WS_TC_ERR, 4, &mx));
     GLOBE_CK(ctx, cudaMemsetAsync(mx + 1, 0, 2 * sizeof(unsigned), ctx->stream));
     const int64_t nelt = (int64_t)N * (N + 1) / 2;
@@ -345,7 +349,7 @@ int dense_digit_planes(globe_ctx* ctx) {
 
 template <int NMMA>
 static int launch_dense(globe_ctx* ctx, const CUtensorMap& mA, const CUtensorMap& mB, int rows, int nchunks,
-                        int cps, float* part, int64_t ldp, unsigned* err) {
+                        int cps, float* part, int64_t ldp, unsigned* err, int stall) {
     const size_t smem = sizeof(DSmem<NMMA>) + 1024;
     static std::atomic<uint64_t> attr_set{0};   // the shared-memory opt-in is per device
     const uint64_t bit = 1ull << (ctx->device & 63);
@@ -355,16 +359,16 @@ static int launch_dense(globe_ctx* ctx, const CUtensorMap& mA, const CUtensorMap
     }
     const int splits = (nchunks + cps - 1) / cps;
     const dim3 grid((unsigned)(rows / DROWS), (unsigned)splits);
-    k_tc_dense<NMMA><<<grid, 256, smem, ctx->stream>>>(mA, mB, rows, nchunks, cps, part, ldp, err);
+    k_tc_dense<NMMA><<<grid, 256, smem, ctx->stream>>>(mA, mB, rows, nchunks, cps, part, ldp, err, stall);
     GLOBE_LAUNCHED(ctx, "k_tc_dense");
     return GLOBE_OK;
 }
 
 static int dense_dispatch(globe_ctx* ctx, int nmma, const CUtensorMap& mA, const CUtensorMap& mB, int rows,
-                          int nchunks, int cps, float* part, int64_t ldp, unsigned* err) {
+                          int nchunks, int cps, float* part, int64_t ldp, unsigned* err, int stall) {
     switch (nmma) {
 #define GLOBE_DENSE_CASE(n) \
-    case n: return launch_dense<n>(ctx, mA, mB, rows, nchunks, cps, part, ldp, err);
+    case n: return launch_dense<n>(ctx, mA, mB, rows, nchunks, cps, part, ldp, err, stall);
         GLOBE_DENSE_CASE(16) GLOBE_DENSE_CASE(32) GLOBE_DENSE_CASE(48) GLOBE_DENSE_CASE(64)
         GLOBE_DENSE_CASE(80) GLOBE_DENSE_CASE(96) GLOBE_DENSE_CASE(112) GLOBE_DENSE_CASE(128)
         GLOBE_DENSE_CASE(144) GLOBE_DENSE_CASE(160) GLOBE_DENSE_CASE(176) GLOBE_DENSE_CASE(192)
@@ -438,7 +442,9 @@ static int dense_group(globe_ctx* ctx, const double* Z, int kg, double scale, do
     GLOBE_LAUNCHED(ctx, "k_digits");
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS1);
-        GLOBE_RET(dense_dispatch(ctx, nmma, mA, mB, rows, nch, cps, P, ldp, err));
+        const int stall = ctx->stall_next_gemm;   // test hook (globe_debug_stall_next_gemm)
+        ctx->stall_next_gemm = 0;
+        GLOBE_RET(dense_dispatch(ctx, nmma, mA, mB, rows, nch, cps, P, ldp, err, stall));
     }
     k_dense_combine<ND><<<dim3(std::min(div_up(N, 256), 1024), kg), 256, 0, ctx->stream>>>(
         P, splits, nmma, ldp, N, np, g.adig_da, col, std::ldexp(scale, g.adig_e), out, N);

@@ -213,11 +213,12 @@ int globe_set_precision(globe_ctx* ctx, int precision);
 int globe_set_digits(globe_ctx* ctx, int nd);
 int globe_get_digits(const globe_ctx* ctx);
 
-/* Test hook for the tensor-core kernel's bounded waits: the next genotype
- * product's first launch leaves its first digit stage unloaded.  The MMA
- * issuer's wait for it runs out after ~2 s, the CTA raises its abort flag,
- * drains its copies with bounded waits and frees TMEM, and the call returns
- * GLOBE_ERR_CUDA ("timed out ... code 0x4"); the context stays usable.  Nothing
+/* Test hook for the tensor-core kernels' bounded waits: the next tensor-core
+ * GRM product's first launch (genotype or dense) leaves its first stage
+ * unloaded.  The MMA issuer's wait for it runs out after ~2 s, the CTA raises
+ * its abort flag, drains its copies with bounded waits and frees TMEM, and the
+ * call returns GLOBE_ERR_CUDA ("timed out ... code 0x4" from the genotype
+ * kernel, "code 0x2" from the dense one); the context stays usable.  Nothing
  * faults and nothing waits without a limit.  Not for production use. */
 int globe_debug_stall_next_gemm(globe_ctx* ctx);
 

@@ -3,6 +3,7 @@ import numpy as np
 import pytest
 
 import globe_gb300 as G
+from globe_gb300 import synth
 from helpers import VC_F, cohort
 
 pytestmark = pytest.mark.gpu
@@ -67,3 +68,29 @@ def test_tensor_core_wait_timeout_is_reported_and_recovered(orc):
         got = ctx.grm_apply(Z)                  # the context is still usable
         s = orc.Solver(c["indiv"].astype(np.int32), c["X"], c["y"], N, VC_F, packed=c["packed"])
         assert rel(got, s.grm_apply(Z)) < 1e-11
+
+
+def test_dense_tensor_core_wait_timeout_is_reported_and_recovered(orc):
+    """The same for the dense GRM's tensor-core kernel: its first stage (digit planes and
+    digit tiles) never arrives, the MMA issuers' bounded waits run out, the call reports
+    the timeout, and the context then computes the dense product correctly."""
+    import time
+    from helpers import rel
+    c = cohort(29, 200, 300, recs=("uniform", 1, 3), miss=0.02)
+    N = c["N"]
+    grm = synth.grm_from_packed(c["packed"], N)
+    Z = np.random.default_rng(5).standard_normal((N, 3))
+    with G.Context(0) as ctx:
+        ctx.load_records(c["indiv"].astype(np.int32), c["X"], c["y"], N)
+        ctx.load_grm(grm, N)
+        ctx.set_vc(VC_F)
+        ctx.set_precision(G.PREC_MIXED)
+        assert ctx._L.globe_debug_stall_next_gemm(ctx.h) == 0
+        t0 = time.perf_counter()
+        with pytest.raises(G.GlobeError) as e:
+            ctx.grm_apply(Z)
+        assert time.perf_counter() - t0 < 30
+        assert e.value.code == -2 and "timed out" in str(e.value)   # GLOBE_ERR_CUDA
+        got = ctx.grm_apply(Z)
+        s = orc.Solver(c["indiv"].astype(np.int32), c["X"], c["y"], N, VC_F, grm_lt=grm)
+        assert rel(got, s.grm_apply(Z)) < 1e-9
