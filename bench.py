@@ -434,6 +434,22 @@ def run_ours(args, cfg):
         t_max, total_units = aggregate_replicas(torch, t_ms, rhs_iters, "cuda")
     value = total_units / (t_max / 1000.0)
 
+    # The timed region above records CUDA events around every pass (the roofline's kernel
+    # times), and profiling runs the PCG iterations as direct launches.  The same steps again
+    # with profiling off replay each iteration as a CUDA graph (the library's default).
+    barrier()
+    ev0.record(stream)
+    g_units = 0
+    for _ in range(args.steps):
+        g_units += step_dev()["rhs_iters"]
+    ev1.record(stream)
+    barrier()
+    t_g = ev0.elapsed_time(ev1)
+    if world > 1:
+        t_g, g_units = aggregate_replicas(torch, t_g, g_units, "cuda")
+    graphs_line = {"value": g_units / (t_g / 1000.0), "unit": "RHS*iters/s", "ms_per_step": t_g / args.steps,
+                   "cuda_graphs": bool(ctx.get_graphs())}
+
     # e2e through the public API with pinned host buffers
     hB = torch.empty((k, Nrec), dtype=torch.float64, pin_memory=True)
     hB.copy_(B.cpu())
@@ -544,8 +560,11 @@ def run_ours(args, cfg):
                        "iters_per_step": args.iters, "kept_snps": Mk, "records": Nrec,
                        "l2": ("inputs larger than L2 (%s %.1f GB)" % (
                            ("dense GRM", N * (N + 1) / 2 * 4 / 1e9) if dense else ("packed genotypes", Mk * stride / 1e9))),
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches)}
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "cuda_graphs": "off in the timed region (per-pass CUDA events); on in e2e and "
+                                      "device_unprofiled"},
+            "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches),
+            "device_unprofiled": graphs_line}
     if fp64 is not None:
         line["fp64_plain"] = fp64
     if aireml is not None:

@@ -77,6 +77,8 @@ SIGNATURES = {
     "globe_set_digits": (C.c_int, [_vp, C.c_int]),
     "globe_debug_stall_next_gemm": (C.c_int, [_vp]),
     "globe_get_digits": (C.c_int, [_vp]),
+    "globe_set_graphs": (C.c_int, [_vp, C.c_int]),
+    "globe_get_graphs": (C.c_int, [_vp]),
     "globe_grm_build": (C.c_int, [_vp, _fp]),
     "globe_grm_build_dev": (C.c_int, [_vp, _vp]),
     "globe_write_grm": (C.c_int, [C.c_char_p, _fp, C.c_int32, C.c_char_p, C.c_int]),

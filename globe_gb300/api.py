@@ -180,6 +180,13 @@ class Context:
     def get_digits(self):
         return int(self._L.globe_get_digits(self.h))
 
+    def set_graphs(self, on):
+        """Replay the block-PCG iteration as a CUDA graph (default on; off while profiling)."""
+        self._ck(self._L.globe_set_graphs(self.h, int(on)))
+
+    def get_graphs(self):
+        return bool(self._L.globe_get_graphs(self.h))
+
     def set_model(self, model):
         """MODEL_FULL (default) or MODEL_NO_TIME (components sig2e, sig2g only)."""
         self._ck(self._L.globe_set_model(self.h, model))

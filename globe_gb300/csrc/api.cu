@@ -28,6 +28,7 @@ int cuda_err(globe_ctx* ctx, cudaError_t e, const char* what) {
 
 int dalloc_bytes(globe_ctx* ctx, void** p, size_t bytes) {
     *p = nullptr;
+    if (ctx->capturing) return set_err(ctx, GLOBE_ERR_STATE, "device allocation during CUDA graph capture");
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
@@ -53,6 +54,9 @@ void dfree(globe_ctx* ctx, void* p) {
 int wslot(globe_ctx* ctx, int id, size_t bytes, void** out) {
     Slot& s = ctx->ws[id];
     if (s.bytes < bytes) {
+        // growth synchronises the stream: not while a capture is open (the caller then runs
+        // the same work directly)
+        if (ctx->capturing) return set_err(ctx, GLOBE_ERR_STATE, "workspace growth during CUDA graph capture");
         if (s.p) {
             cudaStreamSynchronize(ctx->stream);
             cudaFree(s.p);
@@ -184,6 +188,8 @@ void globe_destroy(globe_ctx* ctx) {
     for (auto& s : ctx->ws)
         if (s.p) cudaFree(s.p);
     if (ctx->hpin) cudaFreeHost(ctx->hpin);
+    for (auto& g : ctx->pcg_graph)
+        if (g) cudaGraphExecDestroy(g);
     for (auto& e : ctx->prof_pool) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
@@ -193,6 +199,15 @@ void globe_destroy(globe_ctx* ctx) {
 }
 
 const char* globe_last_error(const globe_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+int globe_set_graphs(globe_ctx* ctx, int on) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (on != 0 && on != 1) return set_err(ctx, GLOBE_ERR_ARG, "globe_set_graphs: on must be 0 or 1, got %d", on);
+    ctx->graphs = on;
+    return GLOBE_OK;
+}
+
+int globe_get_graphs(const globe_ctx* ctx) { return ctx ? ctx->graphs : -1; }
 
 int globe_get_stream(globe_ctx* ctx, void** stream) {
     if (!ctx || !stream) return GLOBE_ERR_ARG;

@@ -127,6 +127,11 @@ struct globe_ctx {
     std::vector<std::pair<void*, size_t>> allocs;  // persistent allocations (freed on destroy)
     double* hpin = nullptr;       // pinned host scratch for per-iteration scalars
     size_t hpin_n = 0;
+    // CUDA graphs of the block-PCG iteration body (globe_set_graphs), one per parity of the
+    // swapped r'z buffers; updated in place from each call's capture
+    int graphs = 1;
+    cudaGraphExec_t pcg_graph[2] = {nullptr, nullptr};
+    bool capturing = false;       // a stream capture is open: allocation is refused
     // event profiling (globe_prof_*)
     bool prof_on = false;
     struct ProfEv {

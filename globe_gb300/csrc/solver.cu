@@ -98,6 +98,47 @@ int pcg_dev(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_o
     return rc;
 }
 
+// Captures `body` (stream work only, nothing run) into a graph and makes ctx->pcg_graph[slot]
+// run it: the cached executable is updated in place when the topology matches, else
+// instantiated anew.  Allocation is refused while the capture is open.  Returns false, with
+// nothing run and the error message restored, if any step fails.
+template <class F>
+static bool capture_body(globe_ctx* ctx, int slot, F&& body, int64_t* nlaunch) {
+    const std::string err0 = ctx->err;
+    const int64_t l0 = ctx->launches;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    ctx->capturing = true;
+    const int rc = body();
+    ctx->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    *nlaunch = ctx->launches - l0;
+    ctx->launches = l0;
+    bool ok = rc == GLOBE_OK && e == cudaSuccess && g != nullptr;
+    if (ok) {
+        cudaGraphExec_t& x = ctx->pcg_graph[slot];
+        cudaGraphExecUpdateResultInfo upd;
+        if (!(x && cudaGraphExecUpdate(x, g, &upd) == cudaSuccess)) {
+            cudaGetLastError();
+            if (x) cudaGraphExecDestroy(x);
+            x = nullptr;
+            if (cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+                x = nullptr;
+                ok = false;
+            }
+        }
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        ctx->err = err0;
+    }
+    return ok;
+}
+
 static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info) {
     GLOBE_RET(check_ready(ctx));
     if (k < 1) return set_err(ctx, GLOBE_ERR_ARG, "number of right-hand sides must be >= 1");
@@ -183,6 +224,9 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     bool converged = false, stagnated = false;
     int64_t rhs_iters = 0;
     if (cols.empty()) converged = true;
+    bool use_graph = ctx->graphs && !ctx->prof_on;   // profiling times each pass with events
+    std::vector<int32_t> gcols[2];                   // column set each graph was captured for
+    int64_t glaunch[2] = {0, 0};                     // kernels per replay
     for (it = 0; it < o->maxit && !cols.empty(); ++it) {
         const int kact = (int)cols.size();
         ProfScope iter_scope(ctx, GLOBE_PROF_PCG_ITER);
@@ -190,14 +234,36 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
             GLOBE_CK(ctx, cudaMemcpyAsync(dcols, cols.data(), sizeof(int32_t) * kact, cudaMemcpyHostToDevice, ctx->stream));
             uploaded = cols;
         }
-        if (it > 0) GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kact, Zi, S1));
-        else GLOBE_RET(seg_sums(ctx, p, nullptr, nullptr, nullptr, dcols, kact, Zi, S1));
-        GLOBE_RET(grm_apply_dev(ctx, Zi, kact, GZ));
-        GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kact, Vp, pvp));
-        GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
-        GLOBE_RET(pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kact, rr, rz2));
-        GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-        GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+        // the iteration's stream work, up to the copies of the two k-vectors the host checks
+        auto body = [&](bool first) -> int {
+            if (!first) GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kact, Zi, S1));
+            else GLOBE_RET(seg_sums(ctx, p, nullptr, nullptr, nullptr, dcols, kact, Zi, S1));
+            GLOBE_RET(grm_apply_dev(ctx, Zi, kact, GZ));
+            GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kact, Vp, pvp));
+            GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
+            GLOBE_RET(pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kact, rr, rz2));
+            GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+            GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+            return GLOBE_OK;
+        };
+        // The first iteration runs directly (it also builds what the products make on first
+        // use).  Later ones replay a graph of the body, captured once per call, parity of the
+        // swapped r'z buffers and column set; a failed capture falls back to direct launches.
+        bool ran = false;
+        if (it > 0 && use_graph) {
+            const int slot = rz == scal ? 0 : 1;
+            if (gcols[slot] != cols) {
+                gcols[slot].clear();
+                if (capture_body(ctx, slot, [&]() { return body(false); }, &glaunch[slot])) gcols[slot] = cols;
+                else use_graph = false;
+            }
+            if (use_graph) {
+                GLOBE_CK(ctx, cudaGraphLaunch(ctx->pcg_graph[slot], ctx->stream));
+                ctx->launches += glaunch[slot];
+                ran = true;
+            }
+        }
+        if (!ran) GLOBE_RET(body(it == 0));
         GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
         rhs_iters += kact;
         for (int j : cols) {

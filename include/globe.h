@@ -213,6 +213,18 @@ int globe_set_precision(globe_ctx* ctx, int precision);
 int globe_set_digits(globe_ctx* ctx, int nd);
 int globe_get_digits(const globe_ctx* ctx);
 
+/* CUDA graphs in the block PCG (on = 1, the default; 0 = direct launches).
+ * Each globe_pcg call runs its first iteration directly. It then captures the
+ * iteration's stream work (record kernels, GRM product, the copies of the
+ * residual norms) once per parity of its swapped r'z buffers and column set,
+ * and replays it. The per-iteration host check of the stopping rule stays.
+ * Results are identical either way. Graphs are not used while event
+ * profiling is on (globe_prof_enable), so that each pass is timed, nor when a
+ * capture fails (e.g. a workspace would have to grow); the iteration then
+ * launches the same kernels directly.  No reference counterpart. */
+int globe_set_graphs(globe_ctx* ctx, int on);
+int globe_get_graphs(const globe_ctx* ctx);
+
 /* Test hook for the tensor-core kernels' bounded waits: the next tensor-core
  * GRM product's first launch (genotype or dense) leaves its first stage
  * unloaded.  The MMA issuer's wait for it runs out after ~2 s, the CTA raises
