@@ -250,7 +250,10 @@ int ensure_blk2(globe_ctx* ctx);   // individual-major tile-blocked copy (first 
 int load_bed_rows(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t stride, float min_maf, float max_miss,
                   int64_t* d_alt, int64_t* d_miss, float* d_maf, float* d_mr, uint8_t* d_keep, globe_bed_info* info);
 int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
-int tc_check_error(globe_ctx* ctx);
+int tc_err_word(globe_ctx* ctx, unsigned** err);   // the kernels' timeout word (cleared when created)
+int tc_check_error(globe_ctx* ctx);                 // reads and clears it: GLOBE_ERR_CUDA if set
+// rc of a call at `precision`, or the tensor-core timeout behind it (the root cause) if one was set
+int with_tc_check(globe_ctx* ctx, int precision, int rc);
 
 // solver.cu
 int grm_apply_dev(globe_ctx* ctx, const double* Z, int k, double* out);

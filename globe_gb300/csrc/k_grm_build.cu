@@ -334,8 +334,7 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     GLOBE_RET(B.get(&ps, (size_t)nbr));
     GLOBE_RET(B.get(&D, (size_t)G * GRM_NMMA * kpad));
     GLOBE_RET(B.get(&P, (size_t)G * spe * GRM_NMMA * ldp));
-    GLOBE_RET(ws(ctx, WS_TC_ERR, 4, &err));
-    GLOBE_CK(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream));
+    GLOBE_RET(tc_err_word(ctx, &err));
     // digit rows GRM_KG * NDIG .. GRM_NMMA - 1 of every group stay zero
     GLOBE_CK(ctx, cudaMemsetAsync(D, 0, (size_t)G * GRM_NMMA * kpad, ctx->stream));
     CUtensorMap mB;
@@ -382,7 +381,7 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
             P, spe, ldp, pz, N, jb, C2, info, 1.0 / (double)g.Mk, lt);
         GLOBE_LAUNCHED(ctx, "k_grm_combine");
     }
-    return tc_check_error(ctx);
+    return GLOBE_OK;
 }
 
 static int grm_build_f64(globe_ctx* ctx, float* lt) {
@@ -416,7 +415,7 @@ extern "C" int globe_grm_build_dev(globe_ctx* ctx, float* d_lt) {
     GLOBE_RET(grm_ready(ctx));
     if (!d_lt) return set_err(ctx, GLOBE_ERR_ARG, "globe_grm_build_dev: null output");
     ProfScope p(ctx, GLOBE_PROF_GRM_BUILD);
-    if (ctx->prec == GLOBE_PREC_MIXED) return grm_build_tc(ctx, d_lt);
+    if (ctx->prec == GLOBE_PREC_MIXED) return with_tc_check(ctx, GLOBE_PREC_MIXED, grm_build_tc(ctx, d_lt));
     return grm_build_f64(ctx, d_lt);
 }
 

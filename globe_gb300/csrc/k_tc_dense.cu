@@ -311,7 +311,7 @@ int dense_digit_planes(globe_ctx* ctx) {
         return GLOBE_OK;
     }
     unsigned* mx;   // words 1-2 of the error-flag slot (word 0 is the kernels' flag): max |A| bits, non-finite
-    GLOBE_RET(ws(ctx, WS_TC_ERR, 4, &mx));
+    GLOBE_RET(tc_err_word(ctx, &mx));
     GLOBE_CK(ctx, cudaMemsetAsync(mx + 1, 0, 2 * sizeof(unsigned), ctx->stream));
     const int64_t nelt = (int64_t)N * (N + 1) / 2;
     k_dense_absmax<<<(unsigned)std::min<int64_t>(div_up(nelt, 256), 152 * 8), 256, 0, ctx->stream>>>(g.grm, nelt,
@@ -422,8 +422,7 @@ static int dense_group(globe_ctx* ctx, const double* Z, int kg, double scale, do
     GLOBE_RET(ws(ctx, WS_TC_D1, (size_t)nmma * np, &D));
     GLOBE_RET(ws(ctx, WS_TC_P1, (size_t)splits * nmma * ldp, &P));
     GLOBE_RET(ws(ctx, WS_TC_SCAL, (size_t)(2 * kg + 2 * nbr * kg + 8), &cst));
-    GLOBE_RET(ws(ctx, WS_TC_ERR, 4, &err));
-    GLOBE_CK(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream));
+    GLOBE_RET(tc_err_word(ctx, &err));
     double* col = cst;
     double* pm = cst + 2 * kg;
     double* ps = pm + (size_t)nbr * kg;

@@ -710,8 +710,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     double* col2 = cst + 2 * kg;  // 2*kg
     pm = cst + 4 * kg;
     ps = pm + (size_t)nbr * kg;
-    GLOBE_RET(ws(ctx, WS_TC_ERR, 4, &err));
-    GLOBE_CK(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream));
+    GLOBE_RET(tc_err_word(ctx, &err));
     CUtensorMap mB1, mB2;
     GLOBE_RET(make_map(ctx, &mB1, D1, (uint64_t)kpad1, (uint64_t)nmma, BK, (uint32_t)nmma, true));
     GLOBE_RET(make_map(ctx, &mB2, D2, (uint64_t)kpad2, (uint64_t)nmma, BK, (uint32_t)nmma, true));
@@ -797,14 +796,32 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
     return GLOBE_OK;
 }
 
+// The tensor-core kernels' error word: word 0 of the WS_TC_ERR slot (words 1-2 serve
+// k_dense_absmax).  Cleared once, when the slot is created; the kernels only set bits in it
+// and tc_check_error reads and clears it, so a timeout in any product of a solve is still
+// reported when the solve ends.
+int tc_err_word(globe_ctx* ctx, unsigned** err) {
+    const bool fresh = ctx->ws[WS_TC_ERR].p == nullptr;
+    GLOBE_RET(ws(ctx, WS_TC_ERR, 4, err));
+    if (fresh) GLOBE_CK(ctx, cudaMemsetAsync(*err, 0, 4 * sizeof(unsigned), ctx->stream));
+    return GLOBE_OK;
+}
+
 int tc_check_error(globe_ctx* ctx) {
     unsigned h = 0;
     void* p = ctx->ws[WS_TC_ERR].p;
     if (!p) return GLOBE_OK;
     GLOBE_CK(ctx, cudaMemcpyAsync(&h, p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    if (h) return set_err(ctx, GLOBE_ERR_CUDA, "tensor-core GRM kernel timed out waiting (code 0x%x)", h);
-    return GLOBE_OK;
+    if (!h) return GLOBE_OK;
+    GLOBE_CK(ctx, cudaMemsetAsync(p, 0, sizeof(unsigned), ctx->stream));
+    return set_err(ctx, GLOBE_ERR_CUDA, "tensor-core GRM kernel timed out waiting (code 0x%x)", h);
+}
+
+int with_tc_check(globe_ctx* ctx, int precision, int rc) {
+    if (precision != GLOBE_PREC_MIXED) return rc;
+    const int rt = tc_check_error(ctx);
+    return rt != GLOBE_OK ? rt : rc;
 }
 
 }  // namespace globe

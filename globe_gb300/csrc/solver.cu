@@ -92,10 +92,9 @@ int pcg_dev(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_o
         return set_err(ctx, GLOBE_ERR_ARG, "unknown precision mode %d", o->precision);
     const int saved = ctx->prec;
     ctx->prec = o->precision;
-    int rc = pcg_run(ctx, B, X, k, o, info);
+    const int rc = pcg_run(ctx, B, X, k, o, info);
     ctx->prec = saved;
-    if (rc == GLOBE_OK && o->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
-    return rc;
+    return with_tc_check(ctx, o->precision, rc);
 }
 
 // Captures `body` (stream work only, nothing run) into a graph and makes ctx->pcg_graph[slot]
@@ -394,8 +393,8 @@ int globe_grm_apply(globe_ctx* ctx, const double* Z, double* out, int k) {
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
     size_t n = (size_t)ctx->coh.N * k;
-    GLOBE_RET(host_io(ctx, Z, n, out, n, [&](double* a, double* b) { return grm_apply_dev(ctx, a, k, b); }));
-    return ctx->prec == GLOBE_PREC_MIXED ? tc_check_error(ctx) : GLOBE_OK;
+    const int rc = host_io(ctx, Z, n, out, n, [&](double* a, double* b) { return grm_apply_dev(ctx, a, k, b); });
+    return with_tc_check(ctx, ctx->prec, rc);
 }
 
 int globe_vx_dev(globe_ctx* ctx, const double* d_x, double* d_out, int k) {
@@ -410,8 +409,8 @@ int globe_vx(globe_ctx* ctx, const double* x, double* out, int k) {
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
     size_t n = (size_t)ctx->coh.Nrec * k;
-    GLOBE_RET(host_io(ctx, x, n, out, n, [&](double* a, double* b) { return vx_dev(ctx, a, k, b); }));
-    return ctx->prec == GLOBE_PREC_MIXED ? tc_check_error(ctx) : GLOBE_OK;
+    const int rc = host_io(ctx, x, n, out, n, [&](double* a, double* b) { return vx_dev(ctx, a, k, b); });
+    return with_tc_check(ctx, ctx->prec, rc);
 }
 
 int globe_precond_apply(globe_ctx* ctx, const double* r, double* z, int k) {
@@ -714,8 +713,7 @@ int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* 
         PrecScope ps(ctx, opts->precision);
         rc = mme_impl(ctx, opts, beta, uhat, bhat, vinv_r, info);
     }
-    if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
-    return rc;
+    return with_tc_check(ctx, opts->precision, rc);
 }
 
 int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
@@ -727,8 +725,7 @@ int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t 
         PrecScope ps(ctx, opts->precision);
         rc = aireml_grad_impl(ctx, probes, numMC, seed, opts, f_theta, first, trace, grad, info);
     }
-    if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
-    return rc;
+    return with_tc_check(ctx, opts->precision, rc);
 }
 
 int globe_aireml_eval(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
@@ -740,8 +737,7 @@ int globe_aireml_eval(globe_ctx* ctx, const double* probes, int numMC, uint64_t 
         PrecScope ps(ctx, opts->precision);
         rc = aireml_eval_impl(ctx, probes, numMC, seed, opts, first, trace, grad, info);
     }
-    if (rc == GLOBE_OK && opts->precision == GLOBE_PREC_MIXED) rc = tc_check_error(ctx);
-    return rc;
+    return with_tc_check(ctx, opts->precision, rc);
 }
 
 int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai, globe_pcg_info* info) {

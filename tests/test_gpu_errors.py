@@ -94,3 +94,29 @@ def test_dense_tensor_core_wait_timeout_is_reported_and_recovered(orc):
         got = ctx.grm_apply(Z)
         s = orc.Solver(c["indiv"].astype(np.int32), c["X"], c["y"], N, VC_F, grm_lt=grm)
         assert rel(got, s.grm_apply(Z)) < 1e-9
+
+
+def test_timeout_inside_a_solve_is_reported_at_its_end(orc):
+    """A bounded-wait timeout in the first GRM product of a block PCG is reported when the
+    solve returns, although the later products (and the graph replays) ran without one:
+    the kernels only set bits in the error word, and the solve's final check reads and
+    clears it.  The next solve on the context is correct."""
+    from helpers import rel
+    c = cohort(23, 200, 300, recs=("uniform", 1, 3), miss=0.02)
+    N = c["N"]
+    indiv = c["indiv"].astype(np.int32)
+    B = np.column_stack([c["X"], c["y"]])
+    with G.Context(0) as ctx:
+        ctx.load_records(indiv, c["X"], c["y"], N)
+        ctx.load_bed(c["packed"])
+        ctx.set_vc(VC_F)
+        assert ctx._L.globe_debug_stall_next_gemm(ctx.h) == 0
+        with pytest.raises(G.GlobeError) as e:
+            ctx.pcg(B, tol=1e-10, maxit=6, rule=G.RULE_PCGSOLVER, precision=G.PREC_MIXED)
+        assert e.value.code == -2 and "timed out" in str(e.value)
+        X, info = ctx.pcg(B, tol=1e-10, rule=G.RULE_PCGSOLVER, precision=G.PREC_MIXED)
+        assert info["converged"]
+    s = orc.Solver(indiv, c["X"], c["y"], N, VC_F, packed=c["packed"])
+    s.precond_build()
+    Xo, _ = s.pcg(B, 1e-10, rule=0)
+    assert rel(X, Xo) < 1e-8
