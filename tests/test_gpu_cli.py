@@ -78,19 +78,21 @@ def _final_theta(log_path):
 
 def test_runaireml_geno_matches_grm_input(tmp_path):
     """runAIREML --geno (genetic relationships from the PLINK genotypes, on the fly)
-    against runAIREML on the .grm.bin built from the same genotypes; FP64 and mixed."""
+    against runAIREML on the .grm.bin built from the same genotypes; FP64 and mixed
+    (the dense mixed run takes the tensor-core digit-plane product)."""
     c = golden_case("geno_small")
     common = ["--numMC", "5", "--maxiter", "6", "--seed", "5", "--pcgTol", "1e-10"]
     th = {}
-    for name, extra in (("dense", []), ("geno", ["--geno", c["prefix"]]),
+    for name, extra in (("dense", []), ("dense_mixed", ["--precision", "mixed"]), ("geno", ["--geno", c["prefix"]]),
                         ("geno_mixed", ["--geno", c["prefix"], "--precision", "mixed"])):
         out = os.path.join(str(tmp_path), name)
-        grm_arg = c["prefix"] if name == "dense" else "-"
+        grm_arg = c["prefix"] if name.startswith("dense") else "-"
         r = _run([os.path.join(BIN, "runAIREML"), c["prefix"] + ".txt", grm_arg, out] + common + extra)
         assert r.returncode == 0, r.stderr
         th[name] = _final_theta(out + ".log")
     assert rel(th["geno"], th["dense"]) < 1e-4          # float32 rounding of the .grm.bin
     assert rel(th["geno_mixed"], th["geno"]) < 1e-6
+    assert rel(th["dense_mixed"], th["dense"]) < 1e-6
 
 
 def test_runpcgsolver_digits_flag(tmp_path):
