@@ -535,7 +535,8 @@ def run_ours(args, cfg):
     tf = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tf):
         passname = "pass2" if "pass 2" in dom[0] else "pass1"
-        traffic = json.load(open(tf)).get("%s:%s:%s:%s" % (args.config, args.precision, dom[0].split("(")[0], passname))
+        traffic = json.load(open(tf)).get("%s:%s:%s:%s" % (args.config, args.precision, dom[0].split("(")[0].strip(),
+                                                              passname))
     ngrm, msgrm = prof[G._lib.PROF_GRM]
     niter, msiter = prof[G._lib.PROF_PCG_ITER]
     roof = {"bound": "hbm", "kernel": dom[0], "achieved": achieved, "peak": hbm, "unit": "GB/s",
