@@ -196,3 +196,37 @@ def test_dense_digit_planes_and_bound(orc):
     indiv = c["indiv"].astype(np.int32)
     s = orc.Solver(indiv, c["X"], c["y"], N, (0.6, 1.0, 0.4, 0.2, 0.2), grm_lt=lt)
     assert rel(y, s.grm_apply(z[:, None])[:, 0]) < 1e-9
+
+
+def _fold_chunks(P, da, nd):
+    """k_dense_combine's recombination of the plane-by-digit sums P[d, j] (exact integers):
+    sums T_s by total weight s = d + j, three int64 chunks of five weights, then FP64."""
+    NT = 7 + nd - 1
+    T = [0] * NT
+    for d in range(da):
+        for j in range(nd):
+            T[d + j] += int(P[d, j])
+    C = [0, 0, 0]
+    for q in range(3):
+        for m in range(5):
+            C[q] = C[q] * 32 + (T[5 * q + m] if 5 * q + m < NT else 0)
+    assert all(abs(c) < 2 ** 63 for c in C)       # the int64 chunks cannot overflow
+    return 2.0 ** -20 * (float(C[0]) + np.ldexp(float(C[1]), -25) + np.ldexp(float(C[2]), -50))
+
+
+def test_dense_combine_chunks_are_exact():
+    """The three-chunk int64 fold of k_dense_combine equals sum_{d,j} 32^-(d+j) P[d, j]
+    evaluated in exact integer arithmetic, to FP64 rounding, at every digit count and with
+    partial sums at their bound (|P| <= 256 K, K = 2^20 individuals)."""
+    from fractions import Fraction
+    rng = np.random.default_rng(5)
+    K = 1 << 20
+    for nd in range(2, NDIG + 1):
+        for da in range(2, min(7, nd) + 1):
+            for trial in range(3):
+                P = rng.integers(-256 * K, 256 * K + 1, size=(da, nd), dtype=np.int64)
+                if trial == 0:
+                    P[:] = 256 * K                          # every partial at its bound
+                exact = sum(Fraction(int(P[d, j]), 32 ** (d + j)) for d in range(da) for j in range(nd))
+                got = _fold_chunks(P, da, nd)
+                assert abs(got - float(exact)) <= 4 * np.spacing(abs(float(exact))), (nd, da, trial)
