@@ -380,10 +380,11 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
             s0 = warp_sum(s0);
             s1 = warp_sum(s1);
             const double g0 = h00 * s0 + h01 * s1, g1 = h10 * s0 + h11 * s1;
+            const double g0e = g0 * inv_e, g1e = g1 * inv_e;   // z = r/sig2e - (g0 + g1 t)/sig2e
             double* zc = z + (size_t)col * ld;
             for (int q = st + lane; q < en; q += 32) {
                 double rn = rc[q];
-                double zv = (rn - g0 - g1 * t[q]) * inv_e;
+                double zv = fma(rn, inv_e, -fma(g1e, t[q], g0e));
                 zc[q] = zv;
                 rz += rn * zv;
             }
@@ -426,11 +427,12 @@ __global__ void k_pcg_update_t(int32_t nblk, int64_t ld, const int32_t* __restri
             s1 += t[q] * rn;
         }
         const double g0 = H[4 * b] * s0 + H[4 * b + 1] * s1, g1 = H[4 * b + 2] * s0 + H[4 * b + 3] * s1;
+        const double g0e = g0 * inv_e, g1e = g1 * inv_e;   // z = r/sig2e - (g0 + g1 t)/sig2e
         double* zc = z + (size_t)col * ld;
 #pragma unroll 4
         for (int q = st; q < en; ++q) {
             const double rn = rc[q];
-            const double zv = (rn - g0 - g1 * t[q]) * inv_e;
+            const double zv = fma(rn, inv_e, -fma(g1e, t[q], g0e));
             zc[q] = zv;
             acc[1] += rn * zv;
         }
@@ -495,9 +497,10 @@ __global__ void k_precond_apply(int32_t nblk, int64_t ld, const int32_t* __restr
             s0 = warp_sum(s0);
             s1 = warp_sum(s1);
             const double g0 = h00 * s0 + h01 * s1, g1 = h10 * s0 + h11 * s1;
+            const double g0e = g0 * inv_e, g1e = g1 * inv_e;   // z = r/sig2e - (g0 + g1 t)/sig2e
             double* zc = z + (size_t)col * ld;
             for (int q = st + lane; q < en; q += 32) {
-                double zv = (rc[q] - g0 - g1 * t[q]) * inv_e;
+                double zv = fma(rc[q], inv_e, -fma(g1e, t[q], g0e));
                 zc[q] = zv;
                 rz += rc[q] * zv;
             }
@@ -528,10 +531,11 @@ __global__ void k_precond_apply_t(int32_t nblk, int64_t ld, const int32_t* __res
             s1 += t[q] * rc[q];
         }
         const double g0 = H[4 * b] * s0 + H[4 * b + 1] * s1, g1 = H[4 * b + 2] * s0 + H[4 * b + 3] * s1;
+        const double g0e = g0 * inv_e, g1e = g1 * inv_e;   // z = r/sig2e - (g0 + g1 t)/sig2e
         double* zc = z + (size_t)col * ld;
 #pragma unroll 4
         for (int q = st; q < en; ++q) {
-            const double zv = (rc[q] - g0 - g1 * t[q]) * inv_e;
+            const double zv = fma(rc[q], inv_e, -fma(g1e, t[q], g0e));
             zc[q] = zv;
             rz[0] += rc[q] * zv;
         }
