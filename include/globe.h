@@ -16,6 +16,11 @@
  *    count (records, individuals or SNPs).
  *  - Host buffers are caller-owned and copied; "_dev" entry points take
  *    device pointers on the context's device and run on the context's stream.
+ *  - Every wait inside the tensor-core kernels is bounded; one that runs out
+ *    sets a device error word.  Calls that synchronise (the host-buffer
+ *    operators, PCG, MME, AIREML, the GRM builder) read and clear it and return
+ *    GLOBE_ERR_CUDA ("timed out"), ahead of any other error it caused; after an
+ *    asynchronous _dev operator the next such call reports it.
  *  - One context = one GPU and one CUDA stream.  Calls on one context are not
  *    reentrant; distinct contexts are independent.
  *  - Variance components are ordered (sig2e, sig2g, sig2b0, sigb01, sig2b1)
