@@ -24,6 +24,10 @@ namespace globe {
 constexpr int RB_THREADS = 256;  // 8 warps, one block of records per warp
 constexpr int RB_WARPS = RB_THREADS / 32;
 constexpr int TB_THREADS = 256;  // thread-per-block layout
+// limits of precond_apply_scratch, which may set no kernel attribute: columns are
+// grid rows (gridDim.y <= 65535), and dynamic shared memory stays at the default 48 KB
+constexpr int NOALLOC_MAX_COLS = 65535;
+constexpr size_t NOALLOC_SMEM_BYTES = 48 * 1024;
 
 // Launch shape of the record kernels: one thread per (block of <= SHORT_BLOCK records,
 // column) over all blocks -- nbt CTAs per column, longer blocks skipped -- and one
@@ -581,10 +585,21 @@ int precond_apply(globe_ctx* ctx, const double* H, const double* r, double* z, c
 int precond_apply_scratch(globe_ctx* ctx, const double* H, const double* r, double* z, int kact, double* part,
                           size_t part_cap, double* rz) {
     const RecShape rs = rec_shape(ctx);
+    if (kact > NOALLOC_MAX_COLS)
+        return set_err(ctx, GLOBE_ERR_ARG, "%d columns: at most %d per call (one grid row per column)", kact,
+                       NOALLOC_MAX_COLS);
     if (rz && (size_t)rs.S * kact > part_cap)
         return set_err(ctx, GLOBE_ERR_ARG,
                        "r'z partials need %zu doubles of scratch (%d CTAs x %d columns); the static buffer holds %zu",
                        (size_t)rs.S * kact, rs.S, kact, part_cap);
+    // the warp-per-block kernel stages its r'z partials in dynamic shared memory
+    // (RB_WARPS doubles per column) and runs at the default 48 KB limit
+    if (rz && rs.nbl && sizeof(double) * RB_WARPS * (size_t)kact > NOALLOC_SMEM_BYTES)
+        return set_err(ctx, GLOBE_ERR_ARG,
+                       "%d columns with r'z and individuals of more than %d records: at most %d columns (%zu bytes "
+                       "of shared memory per column, %d available)",
+                       kact, SHORT_BLOCK, (int)(NOALLOC_SMEM_BYTES / (sizeof(double) * RB_WARPS)),
+                       sizeof(double) * RB_WARPS, NOALLOC_SMEM_BYTES);
     GLOBE_RET(precond_launch(ctx, H, r, z, nullptr, kact, rz ? part : nullptr, rs));
     if (rz) GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, nullptr, rz));
     return GLOBE_OK;

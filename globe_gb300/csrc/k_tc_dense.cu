@@ -256,6 +256,7 @@ __global__ void k_dense_combine(const float* __restrict__ part, int nsplit, int 
     static_assert(NT <= 15, "three chunks of five weights");
     const int c = blockIdx.y;
     const double s0 = sA * ldexp(1.0, (int)colinfo[2 * c] - 20);   // 2^(e_c - 5*4) for chunk 0
+    const bool bad = isnan(colinfo[2 * c + 1]);   // a non-finite column (k_col_finish): NaN out
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         long long T[NT];
 #pragma unroll
@@ -282,7 +283,8 @@ __global__ void k_dense_combine(const float* __restrict__ part, int nsplit, int 
         for (int q = 0; q < 3; ++q)
 #pragma unroll
             for (int m = 0; m < 5; ++m) C[q] = C[q] * 32 + (5 * q + m < NT ? T[5 * q + m] : 0);
-        out[i + c * ldo] = s0 * ((double)C[0] + ldexp((double)C[1], -25) + ldexp((double)C[2], -50));
+        const double v = s0 * ((double)C[0] + ldexp((double)C[1], -25) + ldexp((double)C[2], -50));
+        out[i + c * ldo] = bad ? colinfo[2 * c + 1] : v;
     }
 }
 

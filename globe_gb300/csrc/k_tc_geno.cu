@@ -388,10 +388,14 @@ __global__ void k_col_finish(const double* __restrict__ pmax, const double* __re
         sm += __shfl_xor_sync(0xffffffffu, sm, o);
     }
     if (lane == 0) {
+        // A column holding NaN or +-Inf has a non-finite sum (fmax drops NaN, the sum keeps it).
+        // It is marked by a NaN sum and a zero exponent: k_digits gives it zero digits, and every
+        // epilogue writes NaN for it (through the centring term, or explicitly), as FP64 would.
+        const bool bad = !isfinite(sm) || !isfinite(mx);
         int E = 0;
-        if (mx > 0) frexp(mx, &E);
-        colinfo[2 * c] = (double)(E - (DBITS - 1));  // |x 2^-e| < 16
-        colinfo[2 * c + 1] = sm;
+        if (!bad && mx > 0) frexp(mx, &E);
+        colinfo[2 * c] = bad ? 0.0 : (double)(E - (DBITS - 1));  // |x 2^-e| < 16
+        colinfo[2 * c + 1] = bad ? __longlong_as_double(0x7ff8000000000000ll) : sm;
     }
 }
 

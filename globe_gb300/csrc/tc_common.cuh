@@ -105,7 +105,8 @@ __host__ __forceinline__ int col_parts(int64_t n) {
 }
 
 // per-column max |x| and sum over n rows (partials per CTA); colinfo[c] = {exponent e with
-// max |x 2^-e| < 16, column sum} from those partials (k_tc_geno.cu)
+// max |x 2^-e| < 16, column sum} from those partials, or {0, NaN} for a column holding a
+// NaN or an infinity (k_tc_geno.cu)
 __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld, double* __restrict__ pmax,
                              double* __restrict__ psum);
 __global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
@@ -124,6 +125,7 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
                          uint8_t* __restrict__ D, int64_t kpad) {
     const int c = blockIdx.y;
     const double sc = ldexp(1.0, DBITS * (ND - 1) - (int)colinfo[2 * c]);   // a power of two: x * sc is exact
+    const bool bad = isnan(colinfo[2 * c + 1]);   // non-finite column (k_col_finish): zero digits
     const int64_t nw = kpad >> 2;
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t P = w << 2, base = P & ~(int64_t)15;
@@ -133,7 +135,7 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
         for (int q = 0; q < 4; ++q) {
             const int pq = pl + q;
             const int64_t src = base + (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1);
-            I[q] = src < n ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
+            I[q] = (src < n && !bad) ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
         }
         uint32_t word[ND];
 #pragma unroll

@@ -225,3 +225,166 @@ def normal_stream(seed, n):
     out[0::2] = r * np.cos(th)
     out[1::2] = r * np.sin(th)
     return out[:n]
+
+
+# ---- portable cohorts ---------------------------------------------------------
+# Inputs that must come out bit-identical on every platform and numpy version (so a
+# fixture can hold the reference's outputs and a checksum of its inputs instead of
+# the inputs): every draw is a splitmix64 hash of (seed, stream, index) in uint64
+# arithmetic, and every value is formed by IEEE additions, multiplications,
+# divisions and square roots applied elementwise in a fixed order -- no library
+# random streams, no transcendental functions, no reductions whose order a BLAS or
+# SIMD loop may choose.
+
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+
+
+def _mix64(z):
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def hash_u64(seed, stream, idx):
+    """splitmix64 output for (seed, stream) at each index of ``idx`` (uint64 array)."""
+    with np.errstate(over="ignore"):
+        key = _mix64(np.uint64(seed) * _GOLD + np.uint64(stream) * np.uint64(0xD1B54A32D192ED03))
+        return _mix64(key + (np.asarray(idx, dtype=np.uint64) + np.uint64(1)) * _GOLD)
+
+
+def hash_uniform(seed, stream, idx):
+    """Uniform [0, 1) doubles with 53 random bits (exact conversions)."""
+    return (hash_u64(seed, stream, idx) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def hash_normal(seed, stream, idx):
+    """Approximately standard normal draws: the Irwin-Hall sum of 12 uniforms minus 6,
+    each uniform 24 bits, summed exactly in int64 (mean 0, variance 1, |x| <= 6)."""
+    s = np.zeros(np.shape(idx), dtype=np.int64)
+    for j in range(12):
+        s += (hash_u64(seed, 16 * stream + j, idx) >> np.uint64(40)).astype(np.int64)
+    return (s - 12 * (1 << 23)).astype(np.float64) * (1.0 / (1 << 24))
+
+
+def _poisson_plus1(u, lam):
+    """Poisson(lam) + 1 by inverse CDF.  exp(-lam) is summed as an exact rational
+    series and rounded once, so the CDF table is the same everywhere."""
+    from fractions import Fraction
+    x, term, e = Fraction(lam).limit_denominator(1 << 20), Fraction(1), Fraction(0)
+    for k in range(1, 400):
+        e += term
+        term = term * (-x) / k
+    p = float(e + term)
+    cdf, k, out = p, 0, np.ones(u.shape, dtype=np.int64)
+    while cdf < 1.0 - 1e-15 and k < 200:
+        out += (u >= cdf)
+        k += 1
+        p = p * lam / k
+        cdf += p
+    return out
+
+
+def portable_cohort(seed, N, M, recs, T, maf_lo=0.05, maf_hi=0.5, miss_rate=0.01, vc=VC_DEFAULT,
+                    freq_levels=0):
+    """The cohort of :func:`simulate_cohort` (same model, same distributions; the
+    normal draws are Irwin-Hall) with hash draws, so the record table text and the
+    PLINK bytes are identical wherever this runs.  ``recs``: ("uniform", lo, hi) or
+    ("poisson", lam) (Poisson(lam)+1).  ``freq_levels`` > 0 draws each SNP's allele
+    frequency from that many equally spaced values in [maf_lo, maf_hi] (the exact
+    GRM of :func:`portable_grm` groups SNPs by it); the frequency is also returned
+    as ``p_a1``."""
+    ind = np.arange(N, dtype=np.uint64)
+    if recs[0] == "uniform":
+        lo, hi = int(recs[1]), int(recs[2])
+        counts = lo + (hash_u64(seed, 1, ind) % np.uint64(hi - lo + 1)).astype(np.int64)
+    elif recs[0] == "poisson":
+        counts = _poisson_plus1(hash_uniform(seed, 1, ind), float(recs[1]))
+    else:
+        raise ValueError(recs)
+    Nrec = int(counts.sum())
+    indiv = np.repeat(np.arange(N, dtype=np.int64), counts)
+    ridx = np.arange(Nrec, dtype=np.uint64)
+    tq = int(round(T * 256))
+    tint = (hash_u64(seed, 2, ridx) % np.uint64(tq + 1)).astype(np.int64)
+    tint = tint[np.lexsort((tint, indiv))]            # sorted within each individual
+    times = tint.astype(np.float64) / 256.0
+    cov = np.column_stack([np.ones(Nrec)] + [np.round(hash_normal(seed, 3 + j, ridx) * 1024.0) / 1024.0
+                                             for j in range(2)])
+    # genotypes, SNP blocks of 512: g = [u1 < p] + [u2 < p], missing if u3 < miss_rate
+    sidx = np.arange(M, dtype=np.uint64)
+    if freq_levels > 0:
+        lev = (hash_u64(seed, 5, sidx) % np.uint64(freq_levels)).astype(np.float64)
+        p = maf_lo + (maf_hi - maf_lo) * (lev / max(freq_levels - 1, 1))
+    else:
+        p = maf_lo + (maf_hi - maf_lo) * hash_uniform(seed, 5, sidx)
+    flip = (hash_u64(seed, 6, sidx) >> np.uint64(63)) == np.uint64(1)
+    pa1 = np.where(flip, 1.0 - p, p)
+    G = np.empty((M, N), dtype=np.int8)
+    for s0 in range(0, M, 512):
+        s1 = min(M, s0 + 512)
+        e = (np.arange(s0, s1, dtype=np.uint64)[:, None] * np.uint64(N) + ind[None, :])
+        pp = pa1[s0:s1, None]
+        g = (hash_uniform(seed, 7, e) < pp).astype(np.int8) + (hash_uniform(seed, 8, e) < pp).astype(np.int8)
+        if miss_rate > 0:
+            g[hash_uniform(seed, 9, e) < miss_rate] = -1
+        G[s0:s1] = g
+    s2e, s2g, s2b0, sb01, s2b1 = vc
+    # genetic values u = Zs' w sqrt(s2g / M), summed SNP by SNP
+    w = hash_normal(seed, 10, sidx)
+    gsum = np.zeros(N)
+    sc = np.sqrt(s2g / M)
+    for s in range(M):
+        gs = np.where(G[s] < 0, 0, G[s]).astype(np.float64)
+        f = min(max(float(int(gs.sum())) / (2.0 * N), 1e-3), 1.0 - 1e-3)   # an integer sum: exact
+        gsum += (gs - 2.0 * f) * (w[s] / np.sqrt(2.0 * f * (1.0 - f)))
+    u = gsum * sc
+    # b_i ~ N(0, D) through the 2x2 Cholesky factor of D
+    l00 = np.sqrt(s2b0)
+    l10 = sb01 / l00
+    l11 = np.sqrt(s2b1 - l10 * l10)
+    z0, z1 = hash_normal(seed, 11, ind), hash_normal(seed, 12, ind)
+    b0, b1 = l00 * z0, l10 * z0 + l11 * z1
+    beta = (1.0, 0.5, -0.3, 0.1)
+    y = beta[0] * cov[:, 0]
+    y = y + beta[1] * cov[:, 1]
+    y = y + beta[2] * cov[:, 2]
+    y = y + beta[3] * times
+    y = y + u[indiv]
+    y = y + b0[indiv]
+    y = y + b1[indiv] * times
+    y = y + hash_normal(seed, 13, ridx) * np.sqrt(s2e)
+    y = np.round(y * 4096.0) / 4096.0
+    return dict(N=N, Nrec=Nrec, p=3, indiv=indiv, times=times, cov=cov, y=y, counts=counts, G=G,
+                packed=pack_genotypes(G), p_a1=pa1)
+
+
+def portable_grm(G, p_a1):
+    """A = Zs' Zs / M with zs = (g - 2p)/sqrt(2p(1-p)), p the generating A1 frequency
+    (missing g -> 0), as a float32 packed lower triangle.  SNPs are grouped by their
+    frequency (a few discrete levels, ``portable_cohort(freq_levels=...)``); within a
+    group A gets w (G'G - 2p (r 1' + 1 r') + 4 p^2 n) with G'G and r integer sums (a
+    float64 product of small integers is exact in any order), and the groups are added
+    in a fixed order -- so every platform writes the same bytes."""
+    M, N = G.shape
+    g = np.where(G < 0, 0, G).astype(np.float64)
+    A = np.zeros((N, N))
+    for pv in np.unique(p_a1):
+        sel = p_a1 == pv
+        Gg = g[sel]
+        T = Gg.T @ Gg
+        r = Gg.sum(axis=0)                  # integers: exact in any order
+        n = float(sel.sum())
+        wv = 1.0 / (2.0 * pv * (1.0 - pv))
+        A += wv * ((T - 2.0 * pv * (r[:, None] + r[None, :])) + 4.0 * pv * pv * n)
+    A = A / M
+    return A[np.tril_indices(N)].astype(np.float32)
+
+
+def file_sha256(path):
+    import hashlib
+    h = hashlib.sha256()
+    with open(path, "rb") as f:
+        for chunk in iter(lambda: f.read(1 << 20), b""):
+            h.update(chunk)
+    return h.hexdigest()

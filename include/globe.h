@@ -267,6 +267,9 @@ int globe_genetic_diag(globe_ctx* ctx, double* diag);
  *    call needing more -- k x (ceil(N/256) + ceil(L/8)) doubles, L the number
  *    of individuals with more than 48 records -- returns GLOBE_ERR_ARG before
  *    launching anything.  Nothing in the buffer needs to start at zero.
+ *  - Width limits, also checked before launching anything (GLOBE_ERR_ARG):
+ *    k <= 65535; and with d_rz and any individual of more than 48 records,
+ *    k <= 768 (64 bytes of shared memory per column, at the default 48 KB). */
  *  - The buffer is shared by every context on a device: calls that overlap
  *    on the GPU (other streams or contexts on the same device) race on it.
  *  - The preconditioner must already be built at the current components

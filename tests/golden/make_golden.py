@@ -25,6 +25,20 @@ seeds; the reference programs' outputs are stored next to them:
 
 ``python make_golden.py grm_build`` makes only the last fixture (from the
 committed geno_small inputs).
+
+Two fixtures at the benchmark configurations' sizes keep only the reference's
+outputs: their inputs come from ``globe_gb300.synth.portable_cohort``, which
+gives the same bytes on every platform, so the tests regenerate them and check
+their SHA-256 against the fixture instead of reading committed copies.
+
+* ``geno_2k_10k_ref.npz`` (``python make_golden.py portable_pcg``) -- the
+  runPCGsolver --geno configuration: N=2,000 individuals, 3-10 records each
+  (times U[0,5]), intercept + 2 covariates, M=10,000 SNPs, MAF U(0.05,0.5),
+  1% missing.  stats_*, f32_* and geno64_* as above.
+* ``aireml_dense_2k_ref.json`` (``python make_golden.py portable_aireml``) --
+  the dense-GRM runAIREML configuration's structure at N=2,000: Poisson(5)+1
+  records (times U[0,10]), a float32 .grm.bin from 5,000 SNPs (MAF
+  U(0.01,0.5)), numMC=15, runAIREML64 with injected probes.
 """
 import json
 import os
@@ -38,6 +52,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from globe_gb300 import synth  # noqa: E402
+
+sys.path.insert(0, os.path.dirname(HERE))
+from helpers import portable_inputs  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref")
 VC = (0.6, 0.4, 0.4, 0.2, 0.2)
@@ -197,6 +214,62 @@ def make_grm_build_case(tmp):
     print("geno_small_grmf64: reference --grm on the oracle-built GRM")
 
 
+PORTABLE_PCG = dict(name="geno_2k_10k", seed=2001, N=2000, M=10000, recs=["uniform", 3, 10], T=5.0,
+                    maf_lo=0.05, maf_hi=0.5, miss_rate=0.01)
+PORTABLE_AIREML = dict(name="aireml_dense_2k", seed=2002, N=2000, M=5000, recs=["poisson", 5], T=10.0,
+                       maf_lo=0.01, maf_hi=0.5, miss_rate=0.0, freq_levels=64, numMC=15, maxiter=50,
+                       probe_seed=9, vc=[0.6, 0.4, 0.4, 0.2, 0.2])
+
+
+def make_portable_pcg(tmp):
+    spec = PORTABLE_PCG
+    pre, coh = portable_inputs(spec, tmp)
+    name = spec["name"]
+    out = {}
+    r = subprocess.run([os.path.join(REF, "runPCGsolver_stats"), "--input", pre + ".txt", "--output",
+                        os.path.join(tmp, name + "_s"), "--geno", pre] + _vcargs(VC),
+                       capture_output=True, text=True, check=True)
+    rows = [ln.split() for ln in r.stdout.splitlines() if ln.startswith("[snpstat]")]
+    out["stats_alt"] = np.array([int(x[2]) for x in rows], np.int64)
+    out["stats_miss"] = np.array([int(x[3]) for x in rows], np.int64)
+    out["stats_maf"] = np.array([float.fromhex(x[4]) for x in rows], np.float32)
+    out["stats_miss_rate"] = np.array([float.fromhex(x[5]) for x in rows], np.float32)
+    out["stats_keep"] = np.array([int(x[6]) for x in rows], np.uint8)
+    for tag, exe in (("f32", "runPCGsolver"), ("geno64", "runPCGsolver64")):
+        o = os.path.join(tmp, name + "_" + tag)
+        subprocess.run([os.path.join(REF, exe), "--input", pre + ".txt", "--output", o, "--geno", pre] + _vcargs(VC),
+                       capture_output=True, text=True, check=True)
+        for v in ("beta", "uhat", "bhat"):
+            out["%s_%s" % (tag, v)] = _vec("%s_%s.bin" % (o, v))
+    out["spec"] = np.array(json.dumps(spec))
+    out["sha256_txt"] = np.array(synth.file_sha256(pre + ".txt"))
+    out["sha256_bed"] = np.array(synth.file_sha256(pre + ".bed"))
+    np.savez_compressed(os.path.join(HERE, name + "_ref.npz"), **out)
+    print(name, "N=%d Nrec=%d M=%d kept=%d" % (coh["N"], coh["Nrec"], spec["M"], int(out["stats_keep"].sum())))
+
+
+def make_portable_aireml(tmp):
+    spec = PORTABLE_AIREML
+    pre, coh = portable_inputs(spec, tmp)
+    name = spec["name"]
+    per = spec["numMC"] * (3 * coh["N"] + coh["Nrec"])
+    probe_file = os.path.join(tmp, name + "_probes.bin")
+    synth.normal_stream(spec["probe_seed"], per * 120).tofile(probe_file)
+    env = dict(os.environ, GLOBE_PROBE_FILE=probe_file)
+    out = os.path.join(tmp, name)
+    subprocess.run([os.path.join(REF, "runAIREML64"), pre + ".txt", pre, out, "--numMC", str(spec["numMC"]),
+                    "--maxiter", str(spec["maxiter"])], env=env, capture_output=True, text=True, check=True)
+    text = open(out + ".log", encoding="utf-8", errors="replace").read()
+    its, final = parse_aireml_log(text)
+    with open(os.path.join(HERE, name + "_ref.json"), "w") as f:
+        json.dump({"spec": spec, "numMC": spec["numMC"], "maxiter": spec["maxiter"], "probe_seed": spec["probe_seed"],
+                   "pcg_tol": 1e-12, "theta0": [0.5, 0.30000001192092896, 0.20000000298023224,
+                                                 0.10000000149011612, 0.10000000149011612],
+                   "N": coh["N"], "Nrec": coh["Nrec"], "sha256_txt": synth.file_sha256(pre + ".txt"),
+                   "sha256_grm": synth.file_sha256(pre + ".grm.bin"), "iterations": its, "final": final}, f, indent=1)
+    print(name, "N=%d Nrec=%d iterations=%d" % (coh["N"], coh["Nrec"], len(its)))
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "runPCGsolver64")):
         sys.exit("build the reference first: python oracle/build_ref.py")
@@ -204,6 +277,12 @@ def main():
     os.makedirs(tmp, exist_ok=True)
     if sys.argv[1:] == ["grm_build"]:
         make_grm_build_case(tmp)
+        return
+    if sys.argv[1:] == ["portable_pcg"]:
+        make_portable_pcg(tmp)
+        return
+    if sys.argv[1:] == ["portable_aireml"]:
+        make_portable_aireml(tmp)
         return
     for name, args in CASES.items():
         make_pcg_case(name, *args, tmp)

@@ -138,3 +138,48 @@ def dense_tc_emulation(A, Z, scale, nd, da=None):
         D, ez = tc_digits(Z[:, c], nd)
         Zr[:, c] = np.ldexp(D.T @ w, ez)
     return scale * (Ar @ Zr)
+
+
+def portable_inputs(spec, outdir):
+    """Write the inputs of a portable fixture (``spec`` as stored in it) under outdir:
+    the record table and the PLINK trio, or the .grm.bin when the spec has
+    ``freq_levels``.  Returns (prefix, cohort)."""
+    kw = dict(maf_lo=spec["maf_lo"], maf_hi=spec["maf_hi"], miss_rate=spec["miss_rate"])
+    if spec.get("freq_levels"):
+        kw["freq_levels"] = spec["freq_levels"]
+    if spec.get("vc"):
+        kw["vc"] = tuple(spec["vc"])
+    coh = synth.portable_cohort(spec["seed"], spec["N"], spec["M"], tuple(spec["recs"]), spec["T"], **kw)
+    pre = os.path.join(outdir, spec["name"])
+    synth.write_record_table(pre + ".txt", coh)
+    if spec.get("freq_levels"):
+        synth.write_grm_bin(pre, synth.portable_grm(coh["G"], coh["p_a1"]))
+    else:
+        synth.write_plink(pre, coh["packed"], coh["N"])
+    return pre, coh
+
+
+def portable_case(name, outdir):
+    """A fixture at a benchmark configuration's size whose inputs are regenerated
+    (globe_gb300.synth.portable_cohort) and checked byte for byte (SHA-256) against
+    the inputs the reference ran on.  Same keys as :func:`golden_case`."""
+    base = os.path.join(GOLDEN, name + "_ref")
+    if os.path.exists(base + ".npz"):
+        ref = dict(np.load(base + ".npz"))
+        spec = json.loads(str(ref["spec"]))
+        sums = {"txt": str(ref["sha256_txt"]), "bed": str(ref["sha256_bed"])}
+    else:
+        ref = json.load(open(base + ".json"))
+        spec = ref["spec"]
+        sums = {"txt": ref["sha256_txt"], "grm.bin": ref["sha256_grm"]}
+    pre, coh = portable_inputs(spec, outdir)
+    for ext, want in sums.items():
+        got = synth.file_sha256(pre + "." + ext)
+        assert got == want, "regenerated %s.%s differs from the reference's input" % (name, ext)
+    indiv, X, y, N = parse_records_py(pre + ".txt")
+    d = dict(prefix=pre, indiv=indiv, X=X, y=y, N=N, Nrec=len(indiv), ref=ref, spec=spec)
+    if "bed" in sums:
+        d["packed"] = read_bed_payload(pre, N)
+    else:
+        d["grm"] = np.fromfile(pre + ".grm.bin", np.float32)
+    return d

@@ -103,7 +103,7 @@ def test_rejects_sizes_beyond_static_buffer():
         assert b"static buffer" in ctx._L.globe_last_error(ctx.h)
         ctx.synchronize()
         assert float(dz.abs().max()) == 0.0    # rejected before any launch
-        # without r'z no partials are needed: any width is accepted
+        # without r'z no partials are needed: widths up to 65535 are accepted
         rc = _noalloc(ctx, dr.data_ptr(), dz.data_ptr(), k, 0)
         assert rc == 0, ctx._L.globe_last_error(ctx.h)
         ctx.synchronize()
@@ -119,3 +119,47 @@ def test_needs_a_built_preconditioner():
         rc = _noalloc(ctx, dr.data_ptr(), dz.data_ptr(), 1, 0)
         assert rc == GLOBE_ERR_STATE
         assert b"preconditioner" in ctx._L.globe_last_error(ctx.h)
+
+
+def _setup_widths(ctx, seed):
+    """88 records: one individual of 49 records (warp layout) and 39 of one record."""
+    rng = np.random.default_rng(seed)
+    counts = np.ones(40, dtype=np.int64)
+    counts[17] = 49
+    indiv = np.repeat(np.arange(40, dtype=np.int32), counts)
+    Nrec = len(indiv)
+    t = rng.uniform(0.0, 10.0, Nrec)
+    X = np.asfortranarray(np.column_stack([np.ones(Nrec), rng.standard_normal(Nrec), t]))
+    ctx.load_records(indiv, X, rng.standard_normal(Nrec), 40)
+    ctx.load_bed(synth.pack_genotypes(synth.simulate_genotypes(rng, 64, 40, 0.2, 0.5, 0.0)))
+    ctx.set_vc(VC_F)
+    return Nrec, rng
+
+
+def test_width_limits_checked_before_launch():
+    """Widths whose launch could not start are rejected up front: more than 65535
+    columns, and more than 768 columns with r'z when a block is longer than 48 records
+    (the warp-per-block kernel's shared-memory partials at the default 48 KB)."""
+    torch = pytest.importorskip("torch")
+    with G.Context(0) as ctx:
+        Nrec, rng = _setup_widths(ctx, 14)
+        r = rng.standard_normal((Nrec, 768))
+        z_ref = ctx.precond_apply(r)
+        rz_ref = (r * z_ref).sum(axis=0)
+        for k, with_rz, ok in ((768, True, True), (769, True, False), (65535, False, True), (65536, False, False)):
+            dr = torch.zeros((k, Nrec), dtype=torch.float64, device="cuda")
+            dr[:768] = _dev(torch, r)
+            dz = torch.zeros_like(dr)
+            drz = torch.zeros(k, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            rc = _noalloc(ctx, dr.data_ptr(), dz.data_ptr(), k, drz.data_ptr() if with_rz else 0)
+            ctx.synchronize()
+            if ok:
+                assert rc == 0, ctx._L.globe_last_error(ctx.h)
+                assert rel(dz[:768].cpu().numpy().T, z_ref) < 1e-13
+                if with_rz:
+                    assert rel(drz.cpu().numpy(), rz_ref) < 1e-12
+            else:
+                assert rc == GLOBE_ERR_ARG
+                assert b"at most" in ctx._L.globe_last_error(ctx.h)
+                assert float(dz.abs().max()) == 0.0      # rejected before any launch
