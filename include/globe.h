@@ -269,7 +269,7 @@ int globe_genetic_diag(globe_ctx* ctx, double* diag);
  *    launching anything.  Nothing in the buffer needs to start at zero.
  *  - Width limits, also checked before launching anything (GLOBE_ERR_ARG):
  *    k <= 65535; and with d_rz and any individual of more than 48 records,
- *    k <= 768 (64 bytes of shared memory per column, at the default 48 KB). */
+ *    k <= 768 (64 bytes of shared memory per column, at the default 48 KB).
  *  - The buffer is shared by every context on a device: calls that overlap
  *    on the GPU (other streams or contexts on the same device) race on it.
  *  - The preconditioner must already be built at the current components
