@@ -22,10 +22,16 @@ precision, and ``aireml_mixed_vs_fp64`` on a smaller cohort (N=20k, M=20k)
 where the plain FP64 path also finishes in seconds.  The phenotype's genetic
 term is computed from the generated genotypes (``genetic_values``).
 
+``aireml.parity`` checks the mixed path on this workload against plain FP64:
+one gradient evaluation (fitMME, probe solves, AI matrix) in each precision at
+the mixed AIREML estimate, same probes -- the MME outputs, gradient, AI matrix
+and the Newton step they give.
+
 ``--impl reference`` times the reference algorithm on the host cores: the
 FP32 OpenMP restatement of computeVx_multi with the reference's loop
-structure (oracle/globe_oracle.c, orc_ref_vx_f32) on a SNP subsample of the
-same workload, extrapolated to all SNPs (one PCG iteration = one V.x).
+structure (oracle/globe_oracle.c, orc_ref_vx_f32).  Each step runs one full
+50,000-SNP compute chunk over all individuals; the value scales it to all
+kept SNPs (one PCG iteration = one V.x) and the line says by what factor.
 
 Multi-GPU: the path does not shard across GPUs in this design (one GPU per
 solve); with torchrun each rank runs an independent replica and ``value`` is
@@ -243,23 +249,41 @@ def cpu_reference_vx(indiv, X, packed_rows, maf_rows, N, k, rng):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(indiv, X, N, Mk, k, sample_rows, sample_maf, budget_s=12.0):
-    """Time the reference algorithm on a SNP subsample and extrapolate to Mk SNPs.
-    Returns (RHS*iters/s, description, threads)."""
+REF_CHUNK = 50_000      # SNPs per compute chunk of computeVx_multi (SNP_CHUNK_SIZE, PCGsolver.cpp:1135)
+
+
+def chunk_rows(sample_rows, sample_maf, n=REF_CHUNK):
+    """One reference compute chunk of n SNP rows: the sample rows repeated (the
+    loop's cost does not depend on the genotype values)."""
+    reps = -(-n // sample_rows.shape[0])
+    rows = np.ascontiguousarray(np.tile(sample_rows, (reps, 1))[:n])
+    return rows, np.ascontiguousarray(np.tile(sample_maf, reps)[:n])
+
+
+def cpu_baseline(indiv, X, N, Mk, k, rows, maf, t_rec=None):
+    """Time the reference algorithm on one full compute chunk (rows, maf: REF_CHUNK
+    SNPs) and extrapolate to Mk SNPs.  Returns (RHS*iters/s, record, seconds of the
+    chunk's V.x)."""
     rng = np.random.default_rng(1)
-    t_rec = cpu_reference_vx(indiv, X, sample_rows[:0], sample_maf[:0], N, k, rng)
-    ms = min(16, sample_rows.shape[0])
-    t = cpu_reference_vx(indiv, X, sample_rows[:ms], sample_maf[:ms], N, k, rng)
-    per_snp = max(t - t_rec, 1e-9) / ms
-    ms2 = int(min(sample_rows.shape[0], max(ms, budget_s / per_snp)))
-    t2 = cpu_reference_vx(indiv, X, sample_rows[:ms2], sample_maf[:ms2], N, k, rng)
-    per_snp = max(t2 - t_rec, 1e-9) / ms2
+    if t_rec is None:
+        t_rec = cpu_reference_vx(indiv, X, rows[:0], maf[:0], N, k, rng)
+    t = cpu_reference_vx(indiv, X, rows, maf, N, k, rng)
+    n = rows.shape[0]
+    per_snp = max(t - t_rec, 1e-9) / n
     t_matvec = t_rec + per_snp * Mk
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    desc = ("FP32 reference-structure V.x (orc_ref_vx_f32, OpenMP) on %d of %d SNPs x %d individuals, k=%d, "
-            "record ops %.3fs; per-SNP %.3g s extrapolated to all SNPs: %.2f s per PCG iteration"
-            % (ms2, Mk, N, k, t_rec, per_snp, t_matvec))
-    return k / t_matvec, desc, threads
+    rec = {"value": k / t_matvec, "unit": "RHS*iters/s", "cores": threads, "kind": "port",
+           "sample": ("FP32 reference-structure V.x (orc_ref_vx_f32, OpenMP) over one %d-SNP compute chunk x %d "
+                      "individuals, k=%d: %.3f s (record ops %.3f s); scaled to all %d kept SNPs: %.2f s per PCG "
+                      "iteration" % (n, N, k, t, t_rec, Mk, t_matvec)),
+           "extrapolated_from": {"snps_timed": n, "snps_total": int(Mk), "factor": Mk / n,
+                                 "chunk_seconds": t, "record_ops_seconds": t_rec}}
+    return k / t_matvec, rec, t
+
+
+def common_config(args, cfg, k, Nrec):
+    """The workload keys both arms print under "config" (same keys, same values)."""
+    return {"workload": args.config, "shape": cfg["label"], "seed": SEED, "rhs": k, "records": int(Nrec)}
 
 
 AIREML_THETA0 = (0.5, 0.3, 0.2, 0.1, 0.1)
@@ -299,6 +323,45 @@ def aireml_compare(G):
             "theta_fp64": [float(v) for v in rf["theta"]]}
 
 
+def headline_parity(G, ctx, theta, numMC, seed, tol=1e-5):
+    """The mixed path against plain FP64 on the benchmark workload itself, at the
+    mixed AIREML estimate theta: one gradient evaluation in each precision with the
+    same probes and fresh solves as runAIREML makes them (fitMME from x0 = Q^-1 b,
+    the probe solves, the AI solve; PCG tolerance 1e-5).  Both precisions follow the
+    same Krylov path, so they take the same iterations and their results agree to
+    far below the tolerance.  From each evaluation the Newton step p = AI^-1 g is
+    formed: the FP64 step's distance from the mixed one, relative to theta, bounds
+    how far one FP64 iteration from theta lands from the mixed iteration; the FP64
+    step's own size is how far theta is from the FP64 fixed point (for these probes)."""
+    res = {}
+    for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+        ctx.set_vc(theta)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        m = ctx.mme(tol=tol, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND, precision=prec)
+        g = ctx.aireml_grad(numMC, seed=seed, tol=tol, precision=prec)
+        ai = ctx.aireml_ai(tol=tol, precision=prec)
+        res[name] = dict(seconds=time.perf_counter() - t0, mme=m, grad=g["grad"], ai=ai, iters=[m["iters"], g["iters"]])
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+    mx, sf = res["mixed"], res["fp64"]
+    th = np.asarray(theta, np.float64)
+    p_m = np.linalg.solve(mx["ai"], mx["grad"])
+    p_f = np.linalg.solve(sf["ai"], sf["grad"])
+    mme = {v: rel(mx["mme"][v], sf["mme"][v]) for v in ("beta", "uhat", "bhat")}
+    return {"what": "one AIREML gradient evaluation at the mixed estimate theta*, mixed vs plain FP64 GPU, same "
+                    "probes (seed %d, numMC %d), PCG tol %g" % (seed, numMC, tol),
+            "theta": [float(v) for v in th],
+            "mme_max_rel": mme, "max_rel": max(mme.values()),
+            "grad_max_rel": rel(mx["grad"], sf["grad"]), "ai_max_rel": rel(mx["ai"], sf["ai"]),
+            "newton_step_diff_rel_theta": float(np.abs(p_m - p_f).max() / np.abs(th).max()),
+            "fp64_newton_step_rel_theta": float(np.abs(p_f).max() / np.abs(th).max()),
+            "iterations": {"mixed": mx["iters"], "fp64": sf["iters"]},
+            "seconds": {"mixed": mx["seconds"], "fp64": sf["seconds"]}}
+
+
 def aggregate_replicas(torch, t_ms, units, device):
     """Whole-job figures of independent replicas: the slowest rank's time and the
     units of all ranks (an initialised process group; any backend)."""
@@ -315,6 +378,9 @@ def dist_info():
 
 
 def run_reference(args, cfg):
+    """The reference algorithm on the host cores: each step times one full compute
+    chunk (REF_CHUNK SNPs x all individuals, every record op) of the FP32 V.x and
+    scales it to all kept SNPs (one PCG iteration = one V.x)."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
@@ -322,28 +388,33 @@ def run_reference(args, cfg):
     from oracle import oracle
     oracle.build()
     indiv, X, y, N = make_records(cfg)
-    k = 5
+    k = int(cfg.get("k", 5))
     rng = np.random.default_rng(2)
-    nsample = 4096 if cfg["N"] >= 50_000 else min(cfg["M"], 4096)
+    nsample = min(cfg["M"], 4096)
     G = synth.simulate_genotypes(rng, nsample, N, cfg["maf_lo"], cfg["maf_hi"], cfg["miss"])
     packed = synth.pack_genotypes(G)
+    del G
     alt, miss, maf, _, keep = oracle.bed_stats(packed, N)
-    rows, mafk = packed[keep], maf[keep]
     Mk = int(round(cfg["M"] * keep.mean()))
-    per_step_budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
-    vals = []
+    rows, mafc = chunk_rows(packed[keep], maf[keep], min(REF_CHUNK, Mk))
+    t_rec = cpu_reference_vx(indiv, X, rows[:0], mafc[:0], N, k, np.random.default_rng(1))
+    vals, secs = [], []
     for s in range(args.warmup + args.steps):
-        v, desc, threads = cpu_baseline(indiv, X, N, Mk, k, rows, mafk, budget_s=per_step_budget)
+        v, rec, t = cpu_baseline(indiv, X, N, Mk, k, rows, mafc, t_rec=t_rec)
         if s >= args.warmup:
             vals.append(v)
+            secs.append(t)
     value = float(np.mean(vals))
+    rec["value"] = value
     line = {"metric": METRIC, "value": value, "unit": "RHS*iters/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * k / value, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.config, "shape": cfg["label"], "seed": SEED},
+            "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(secs)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": common_config(args, cfg, k, len(indiv)),
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "RHS*iters/s", "cores": threads, "kind": "port",
-                             "sample": desc},
+            "step": "one %d-SNP compute chunk of the V.x (ms_per_step is its measured time); value scales it to "
+                    "all %d kept SNPs (extrapolated_from)" % (rows.shape[0], Mk),
+            "extrapolated_from": rec["extrapolated_from"],
+            "cpu_baseline": rec,
             "e2e": {"value": value, "unit": "RHS*iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -502,6 +573,8 @@ def run_ours(args, cfg):
                   "seconds_to_converge": t_air, "converged": bool(r["converged"]), "iterations": r["iterations"],
                   "grad_evals": r["grad_evals"], "pcg_rhs_iters": r["pcg_rhs_iters"],
                   "theta": [float(v) for v in r["theta"]], "numMC": numMC, "tol": 1e-3}
+        if not args.no_parity and prec == G.PREC_MIXED and not dense:
+            aireml["parity"] = headline_parity(G, ctx, r["theta"], numMC, SEED + 99)
         if 9 in runs and nd0 != 9:
             t9, r9 = runs[9]
             aireml["nine_digits"] = {"seconds_to_converge": t9, "iterations": r9["iterations"],
@@ -557,13 +630,13 @@ def run_ours(args, cfg):
                       "e4m3 x e4m3 -> f32 (exact digits of A and Z), f64 PCG"),
             "data": "synthetic (GPU counter-based genotypes%s, seeded numpy records)" % (
                 ", GRM built from them" if dense else ""),
-            "config": {"workload": args.config, "shape": cfg["label"], "precision": args.precision,
-                       "iters_per_step": args.iters, "kept_snps": Mk, "records": Nrec,
-                       "l2": ("inputs larger than L2 (%s %.1f GB)" % (
-                           ("dense GRM", N * (N + 1) / 2 * 4 / 1e9) if dense else ("packed genotypes", Mk * stride / 1e9))),
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "cuda_graphs": "off in the timed region (per-pass CUDA events); on in e2e and "
-                                      "device_unprofiled"},
+            "config": common_config(args, cfg, k, Nrec),
+            "run": {"precision": args.precision, "iters_per_step": args.iters, "kept_snps": Mk,
+                    "l2": ("inputs larger than L2 (%s %.1f GB)" % (
+                        ("dense GRM", N * (N + 1) / 2 * 4 / 1e9) if dense else ("packed genotypes", Mk * stride / 1e9))),
+                    "parallelism": "replicas" if world > 1 else "single GPU",
+                    "cuda_graphs": "off in the timed region (per-pass CUDA events); on in e2e and "
+                                   "device_unprofiled"},
             "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches),
             "device_unprofiled": graphs_line}
     if fp64 is not None:
@@ -579,8 +652,10 @@ def run_ours(args, cfg):
     if rank == 0 and not args.no_cpu_baseline and not dense:
         from oracle import oracle
         alt, miss, maf, _, keep = oracle.bed_stats(sample_rows, N)
-        v, desc, threads = cpu_baseline(indiv, X, N, Mk, k, sample_rows[keep], maf[keep])
-        line["cpu_baseline"] = {"value": v, "unit": "RHS*iters/s", "cores": threads, "kind": "port", "sample": desc}
+        rows, mafc = chunk_rows(sample_rows[keep], maf[keep], min(REF_CHUNK, Mk))
+        del sample_rows
+        v, rec, _ = cpu_baseline(indiv, X, N, Mk, k, rows, mafc)
+        line["cpu_baseline"] = rec
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
@@ -602,6 +677,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the in-run FP64-plain comparison")
     ap.add_argument("--no-aireml", action="store_true", help="skip the AIREML time-to-converge runs")
     ap.add_argument("--no-grm-build", action="store_true", help="skip the GRM build (N=20k, M=50k) measurement")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the mixed-vs-FP64 evaluation at the AIREML estimate on this workload")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     if args.iters <= 0:

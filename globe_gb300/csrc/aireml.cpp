@@ -27,6 +27,10 @@
 
 #include "globe.h"
 
+namespace globe {
+int set_err(globe_ctx* ctx, int code, const char* fmt, ...);   // api.cu
+}
+
 namespace {
 
 struct Cons {
@@ -548,10 +552,14 @@ static int aireml_run_impl(globe_ctx* ctx, const globe_aireml_opts* o, const cha
             double p[5] = {0, 0, 0, 0, 0};
             int st = 0;
             if (nc == 5) {
-                TRY(globe_trust_region_step(theta, grad, ai, Delta, p, &st));
+                rc = globe_trust_region_step(theta, grad, ai, Delta, p, &st);
             } else {
                 const double ai2[4] = {ai[0], ai[1], ai[5], ai[6]};
-                TRY(globe_trust_region_step_no_time(theta, grad, ai2, Delta, p, &st));
+                rc = globe_trust_region_step_no_time(theta, grad, ai2, Delta, p, &st);
+            }
+            if (rc != GLOBE_OK) {
+                d.err = "trust-region step: the gradient or the AI matrix is not finite";
+                goto out;
             }
             if (st != 0) {
                 d.log.printf("Step solver failed (status %d). Reducing trust region radius.\n", st);
@@ -681,7 +689,8 @@ static int aireml_run_impl(globe_ctx* ctx, const globe_aireml_opts* o, const cha
     res->pcg_rhs_iters = d.rhs_iters;
 out:
 #undef TRY
-    if (rc != GLOBE_OK && d.log.f) d.log.printf("[error] %s\n", d.err.empty() ? globe_last_error(ctx) : d.err.c_str());
+    if (rc != GLOBE_OK && !d.err.empty()) globe::set_err(ctx, rc, "%s", d.err.c_str());
+    if (rc != GLOBE_OK && d.log.f) d.log.printf("[error] %s\n", globe_last_error(ctx));
     if (d.log.f) std::fclose(d.log.f);
     // restore the context's components to the final estimate
     if (rc == GLOBE_OK) globe_set_vc(ctx, theta);

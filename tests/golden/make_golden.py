@@ -119,7 +119,8 @@ def parse_aireml_log(text, nc=5):
              "steps": [_floats(m) for m in re.findall(r"Predicted step:\s*([^\n]+)", blk)],
              "nlopt": [int(m) for m in re.findall(r"NLopt result: (-?\d+)", blk)],
              "rho": [float(m) for m in re.findall(r"Rho: ([^\n]+)", blk)],
-             "theta_new": [_floats(m) for m in re.findall(r"theta_new: ([^\n]+)", blk)]}
+             "theta_new": [_floats(m) for m in re.findall(r"theta_new: ([^\n]+)", blk)],
+             "delta_after": [float(m) for m in re.findall(r"Trust region radius: ([^\n]+)", blk)]}
         if nc == 5:
             m = re.search(r"Estimated variance components:\s*sig2e = ([^,]+), sig2g = ([^,]+), sig2b0 = ([^,]+), "
                           r"sigb01 = ([^,]+), sig2b1 = ([^\n]+)", blk)

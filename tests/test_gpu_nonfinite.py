@@ -13,6 +13,9 @@ from helpers import VC_F, golden_case, rel
 
 pytestmark = pytest.mark.gpu
 
+# mixed vs FP64 on finite columns: the genotype product is exact up to the 45-bit rounding
+# of each column; the dense one also holds A to 2^-34 max|A| (its 7 digit planes)
+TOL = {"genotypes": 1e-11, "dense": 1e-9}
 BAD = (("nan", 1, 3, np.nan), ("inf", 2, 7, np.inf), ("-inf", 4, 0, -np.inf))
 
 
@@ -35,7 +38,7 @@ def _both(gctx, fn, Z):
     return out[G.PREC_FP64], out[G.PREC_MIXED]
 
 
-def _check(f64, mixed, clean, poisoned):
+def _check(f64, mixed, clean, poisoned, tol):
     # the FP64 path: every entry of a poisoned column is non-finite, the rest finite
     assert np.isfinite(f64[:, clean]).all()
     assert not np.isfinite(f64[:, poisoned]).any()
@@ -43,7 +46,7 @@ def _check(f64, mixed, clean, poisoned):
     assert np.array_equal(np.isfinite(mixed), np.isfinite(f64))
     assert np.isnan(mixed[:, poisoned]).all()
     for c in clean:
-        assert rel(mixed[:, c], f64[:, c]) < 1e-11, c
+        assert rel(mixed[:, c], f64[:, c]) < tol, c
 
 
 def _setup(gctx, source):
@@ -62,7 +65,7 @@ def test_grm_apply_propagates_nonfinite(gctx, source):
     c = _setup(gctx, source)
     Z = _poison(np.random.default_rng(3).standard_normal((c["N"], 7)))
     f64, mixed = _both(gctx, gctx.grm_apply, Z)
-    _check(f64, mixed, clean=[0, 3, 6], poisoned=[1, 2, 4, 5])
+    _check(f64, mixed, clean=[0, 3, 6], poisoned=[1, 2, 4, 5], tol=TOL[source])
 
 
 @pytest.mark.parametrize("source", ["genotypes", "dense"])
@@ -72,7 +75,7 @@ def test_vx_propagates_nonfinite(gctx, source):
     c = _setup(gctx, source)
     x = _poison(np.random.default_rng(4).standard_normal((c["Nrec"], 7)))
     f64, mixed = _both(gctx, gctx.vx, x)
-    _check(f64, mixed, clean=[0, 3, 6], poisoned=[1, 2, 4, 5])
+    _check(f64, mixed, clean=[0, 3, 6], poisoned=[1, 2, 4, 5], tol=TOL[source])
 
 
 def test_clean_call_after_nonfinite(gctx):

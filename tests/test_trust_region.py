@@ -1,11 +1,14 @@
 """The AIREML step subproblem (oneIter_AIREML, varCompEst.cpp:1148-1199):
 our interior-point solver against the steps NLopt's MMA took in the
 reference run, and against scipy SLSQP on constrained cases."""
+import json
+import os
+
 import numpy as np
 import pytest
 
 from globe_gb300 import trust_region_step
-from helpers import golden_case, rel
+from helpers import GOLDEN, golden_case, rel
 
 
 def test_steps_match_reference_run():
@@ -64,3 +67,41 @@ def test_constrained_cases_vs_slsqp(seed):
         # the problem is convex: ours is at least as good as SLSQP's, and close
         assert m(p) >= m(r.x) - 1e-7 * max(1.0, abs(m(r.x)))
         assert abs(m(p) - m(r.x)) <= 1e-5 * max(1.0, abs(m(r.x)))
+
+
+def _feasible(theta, A, delta, p, slack=1e-9):
+    x = theta + p
+    return (np.all(np.abs(p) <= 10 + slack) and all(x[k] >= 1e-5 - slack for k in (0, 1, 2, 4))
+            and x[3] ** 2 <= x[2] * x[4] - 1e-3 + slack and np.dot(np.diag(A), p) <= delta + 1e-7 * abs(delta))
+
+
+def test_active_trust_region_beats_the_reference_step():
+    """Where the trust-region constraint binds, NLopt's MMA stops short of the
+    subproblem's optimum.  The reference's constraint function is the signed sum
+    sum_k AI_kk p_k - Delta but the gradient it hands MMA is 2 AI_kk^2 p_k
+    (varCompEst.cpp:1068-1089), so MMA's local models of the constraint are wrong and
+    it stops on its x tolerance (result 4) at a point that is feasible but not
+    stationary.  Seen in the dense N=2,000, numMC=15 run at iteration 6, the first
+    step taken with Delta finite (10.93, after the rejection of iteration 5): the
+    reference's step has model value 0.039, ours (the exact optimum, equal to
+    SLSQP's) 0.147, and both lie on the constraint.  So the two runs agree through
+    iteration 5 and part from there."""
+    pytest.importorskip("scipy")
+    ref = json.load(open(os.path.join(GOLDEN, "aireml_dense_2k_ref.json")))
+    it5, it6 = ref["iterations"][4], ref["iterations"][5]
+    theta = np.array(it5["theta"])
+    g, A = np.array(it5["gradients"][-1]), np.array(it5["ai"][-1])
+    delta = it5["delta_after"][0]
+    p_ref = np.array(it6["steps"][0])
+    assert it6["nlopt"] == [4]
+
+    def q(p):
+        return g @ p - 0.5 * p @ A @ p
+    p, st = trust_region_step(theta, g, A, delta)
+    assert st == 0
+    assert _feasible(theta, A, delta, p) and _feasible(theta, A, delta, p_ref)
+    assert abs(np.dot(np.diag(A), p) - delta) < 1e-6 * delta              # the constraint binds
+    assert abs(np.dot(np.diag(A), p_ref) - delta) < 1e-6 * delta
+    assert q(p) > 3.0 * q(p_ref) > 0
+    r = _scipy_step(theta, g, A, delta)
+    assert rel(p, r.x) < 1e-5 and abs(q(p) - (-r.fun)) < 1e-9 * abs(q(p))
