@@ -40,8 +40,9 @@ __global__ void k_grm_u4(const double* __restrict__ zs, const double* __restrict
 }
 
 // Per SNP s < kpad and tile code c: the 9 e4m3 digits of I = round(u 2^(40-e)) (bytes 0..8 of
-// dig[4s+c], most significant first) and 2 f_s u~ with u~ = I 2^(e-40) the rounded value, as a
-// float pair hi + lo (hi = the float nearest, lo = the float nearest the rest: ~48 bits).
+// dig[4s+c], most significant first; times geno_digit_mult(s)) and 2 f_s u~ with u~ = I 2^(e-40)
+// the rounded value, as a float pair hi + lo (hi = the float nearest, lo = the float nearest
+// the rest: ~48 bits).
 // SNPs >= Mk (padding of the K range) get zero digits and zero.
 __global__ void k_grm_table(const double* __restrict__ U4, const double* __restrict__ f, int64_t Mk, int64_t kpad,
                             const double* __restrict__ info, uint4* __restrict__ dig, float2* __restrict__ c2v) {
@@ -56,13 +57,14 @@ __global__ void k_grm_table(const double* __restrict__ U4, const double* __restr
             long long I = __double2ll_rn(U4[x] * sc);
             cv = 2.0 * f[s] * ((double)I * back);
             uint32_t b[NDIG];
+            const int mult = geno_digit_mult(s);   // even SNPs: 4 d (their genotypes decode to 2^-9 g)
 #pragma unroll
             for (int j = NDIG - 1; j > 0; --j) {
                 const int d = (int)((I + DHALF) & (2 * DHALF - 1)) - DHALF;
                 I = (I - d) >> DBITS;
-                b[j] = e4m3_int(d);
+                b[j] = e4m3_int(mult * d);
             }
-            b[0] = e4m3_int((int)I);
+            b[0] = e4m3_int(mult * (int)I);
             out.x = b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
             out.y = b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24);
             out.z = b[8];
@@ -95,7 +97,7 @@ __device__ __forceinline__ uint32_t gather_byte(uint32_t a0, uint32_t a1, uint32
 
 // Digit operand of the batch's columns jb .. jb + ncols - 1.  Column jj = z * GRM_KG + c
 // goes to digit rows z * GRM_NMMA + c * NDIG + j, K positions in the decode order of the A
-// operand (position P of a group of 16 holds SNP 2P for P < 8, 2(P-8)+1 otherwise).
+// operand (kpos_g: position P of a group of 16 holds SNP 4 (P % 4) + P / 4).
 // A CTA covers 512 SNPs (32 groups of 16, one per lane) for 32 columns (four per warp): the
 // table entries of its SNPs are staged once in shared memory, each lane reads the 16 codes
 // of its group for one column (one 32-bit word of blk2, tile codes), gathers the 16 table
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(256) k_grm_digits(const uint8_t* __restrict__ 
 #pragma unroll
                     for (int b = 0; b < 4; ++b) {
                         const int P = 4 * wq + b;
-                        const int m = P < 8 ? 2 * P : 2 * (P - 8) + 1;
+                        const int m = 4 * (P & 3) + (P >> 2);
                         const int code = (int)((w >> (2 * m)) & 3u);
                         e[b] = te[m * 4 + code];
                         const float2 cv = tc[m * 4 + code];

@@ -16,8 +16,8 @@
 namespace globe {
 
 __device__ __forceinline__ double zsel(unsigned code, double t0, double t1, double t2) {
-    // tile code 00 -> t0 (g=2), 01 -> t2 (g=1), 10 / 11 -> t1 (g=0 or missing)
-    return code == 0u ? t0 : (code == 1u ? t2 : t1);
+    // tile code 00 -> t1 (g=0 or missing), 01 -> t2 (g=1), 10 -> t0 (g=2)
+    return code == 1u ? t2 : (code == 2u ? t0 : t1);
 }
 
 template <int KC>
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(P2_THREADS) k_geno_p2(const uint8_t* __restric
     }
 }
 
-// zsq[4 s + t] = zs^2 of tile code t as a (hi, lo) float pair (t: 0 -> g=2, 1 -> g=1, 2/3 -> g=0)
+// zsq[4 s + t] = zs^2 of tile code t as a (hi, lo) float pair (t: 0/3 -> g=0, 1 -> g=1, 2 -> g=2)
 __global__ void k_zs_square(const double* __restrict__ zs, int64_t Mk, float2* __restrict__ zsq) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= 4 * Mk) return;

@@ -438,7 +438,7 @@ static int dense_group(globe_ctx* ctx, const double* Z, int kg, double scale, do
     GLOBE_LAUNCHED(ctx, "k_col_finish");
     if (nmma > kg * ND)   // digit rows past the kg columns stay zero
         GLOBE_CK(ctx, cudaMemsetAsync(D + (size_t)kg * ND * np, 0, (size_t)(nmma - kg * ND) * np, ctx->stream));
-    k_digits<ND><<<dim3((unsigned)std::min<int64_t>(div_up(np / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
+    k_digits<ND, false><<<dim3((unsigned)std::min<int64_t>(div_up(np / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
         Z, N, N, kg, col, D, np);
     GLOBE_LAUNCHED(ctx, "k_digits");
     {

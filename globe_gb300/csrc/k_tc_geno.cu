@@ -7,13 +7,15 @@
 //            u[s,c]  = inv_s^2 (P1[s,c] - 2 f_s sum_i Z[i,c])
 //   pass 2:  P2[i,c] = sum_s g(s,i) u[s,c]        (rows = individuals, K = SNPs)
 //            out[i,c] = scale (P2[i,c] - sum_s 2 f_s u[s,c])
-// g in {0,1,2} is exact in FP8 e4m3.  Each right-hand-side column is split
+// g in {0,1,2} is decoded to e4m3 as 2^-9 g or 2^-7 g (the tile code masked in
+// place; even and odd genotypes of a word).  Each right-hand-side column is split
 // into balanced base-32 digits: x = 2^e sum_j d_j 32^-j with integer d_j in
-// [-16,16], also exact in e4m3 (every integer up to 16 is).  |g d| <= 32, so an
-// FP32 sum of up to 2^19 such products is an exact integer: the tensor-core
-// accumulation carries no rounding, and the digits are recombined in int64 /
-// FP64.  With 9 digits (45 bits) the product matches an FP64 evaluation to
-// ~1e-13 relative.
+// [-16,16], exact in e4m3 (every integer up to 16 is, and 4x that), the digit
+// operand holding 4 d where the genotype carries 2^-9.  Every product is
+// g d 2^-7 with |g d| <= 32, so an FP32 sum of up to 2^19 of them is an exact
+// multiple of 2^-7: the tensor-core accumulation carries no rounding, and the
+// digits are recombined in int64 / FP64.  With 9 digits (45 bits) the product
+// matches an FP64 evaluation to ~1e-13 relative.
 //
 // Kernel (one CTA = MT x 128 rows x one K range, M=128 x N=NMMA MMAs per tile):
 //   warp 0     bulk copies of the packed 2-bit tiles (tile-blocked layout: each
@@ -27,9 +29,8 @@
 // Keeping the decoded operand out of shared memory matters: staged through
 // smem it costs ~4 bytes of smem traffic per genotype and caps the kernel
 // near 40% of HBM bandwidth.
-// The decode of 16 genotypes (one 32-bit word) is 3 logic ops, 2 shifts and
-// 4 byte permutes; it permutes K within each group of 16, which the digit
-// tiles repeat (kpos()).
+// The decode of 16 genotypes (one 32-bit word) is 4 masks and 1 shift; it
+// permutes K within each group of 16, which the digit tiles repeat (kpos_g()).
 // Every mbarrier wait is bounded (globaltimer); on timeout the CTA records
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
 #include "tc_ptx.cuh"
@@ -79,10 +80,6 @@ struct Geo {
     static constexpr int DPT = MT >= 2 ? 4 : 8;            // warps of one set per tile (adfull count)
     static constexpr int ES = MT >= 2 ? 2 : 4;             // warps sharing a (tile, quadrant) epilogue
 };
-// byte tables of the decode (prmt operands a, b): a = {2.0, 1.0, 0, 0}, b = {1.0, 0, 0, 0} in e4m3
-constexpr uint32_t LUT_A = 0x00003840u;
-constexpr uint32_t LUT_B = 0x00000038u;
-
 
 // MT row tiles of 128 share every digit tile.  TMEM columns: accumulators
 // [0, MT*NMMA), then DSTAGES x MT decoded A tiles of 32 columns (K = 128 e4m3).
@@ -106,25 +103,19 @@ __device__ __forceinline__ void tmem_st_unit(uint32_t taddr, const uint32_t (&v)
         tmem_st16(taddr, v);
     }
 }
-__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
-    uint32_t r;
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
-    return r;
-}
-// 16 tile codes -> 16 e4m3 bytes.  prmt takes 4 selector nibbles from the low half of its
-// selector: 3 bits pick a byte of {b, a}, and a set top bit replicates that byte's sign bit.
-//   even codes: w & 0x33..  nibble = code        -> a[0] = 2.0, a[1] = 1.0, a[2] = 0
-//   odd codes:  w & 0xCC..  nibble = code << 2   -> 0: a[0] = 2.0, 4: b[0] = 1.0,
-//                                                   8: sign of a[0] (0) replicated = 0
-// 8 integer instructions per 16 genotypes.  Output order: r0 = genotypes 0,2,4,6,
-// r1 = 8..14 even, r2 = 1,3,5,7, r3 = 9..15 odd (the K permutation kpos inverts).
+// 16 tile codes (genotype j of the word at bits 2j) -> 16 e4m3 bytes, by masks in place:
+//   r0 = w & 0x03030303         genotypes 0, 4, 8, 12   as 0x00 / 0x01 / 0x02 = 2^-9 g
+//   r1 = w & 0x0C0C0C0C         genotypes 1, 5, 9, 13   as 0x00 / 0x04 / 0x08 = 2^-7 g
+//   r2 = (w >> 4) & 0x03030303  genotypes 2, 6, 10, 14  (2^-9 g)
+//   r3 = (w >> 4) & 0x0C0C0C0C  genotypes 3, 7, 11, 15  (2^-7 g)
+// 5 integer instructions per 16 genotypes.  The K order is kpos_g; the digit operand carries
+// 4 d at the even genotypes (r0, r2), so every product is g d 2^-7.
 __device__ __forceinline__ void decode_word(uint32_t w, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
-    const uint32_t e = w & 0x33333333u;
-    const uint32_t o = w & 0xCCCCCCCCu;
-    r0 = prmt(LUT_A, LUT_B, e);
-    r1 = prmt(LUT_A, LUT_B, e >> 16);
-    r2 = prmt(LUT_A, LUT_B, o);
-    r3 = prmt(LUT_A, LUT_B, o >> 16);
+    const uint32_t h = w >> 4;
+    r0 = w & 0x03030303u;
+    r1 = w & 0x0C0C0C0Cu;
+    r2 = h & 0x03030303u;
+    r3 = h & 0x0C0C0C0Cu;
 }
 
 // A operand: tile-blocked packed genotypes, block (tile t, chunk c) = 128 rows x 32 B contiguous at
@@ -470,7 +461,7 @@ __global__ void __launch_bounds__(256) k_blk_transpose(const uint8_t* __restrict
         const bool have = t1 < ntiles1 && c1 < nch1;
         {   // row r, logical half h (physical halves swapped when bit 2 of r is set)
             const int r = tid >> 1, h = tid & 1;
-            uint4 v = make_uint4(0xAAAAAAAAu, 0xAAAAAAAAu, 0xAAAAAAAAu, 0xAAAAAAAAu);
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (have)
                 v = *reinterpret_cast<const uint4*>(blk1 + (((t1 * nch1 + c1) * BM + r) * 2 + (h ^ ((r >> 2) & 1))) * 16);
             const uint32_t w[4] = {v.x, v.y, v.z, v.w};
@@ -728,7 +719,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     if (nmma > kg * ND)
         GLOBE_CK(ctx, cudaMemsetAsync(D1 + (size_t)kg * ND * kpad1, 0, (size_t)(nmma - kg * ND) * kpad1,
                                       ctx->stream));
-    k_digits<ND><<<dim3((unsigned)std::min<int64_t>(div_up(kpad1 / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
+    k_digits<ND, true><<<dim3((unsigned)std::min<int64_t>(div_up(kpad1 / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(
         Z, N, N, kg, col1, D1, kpad1);
     GLOBE_LAUNCHED(ctx, "k_digits");
     // ---- pass 1
@@ -748,7 +739,7 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     if (nmma > kg * ND)
         GLOBE_CK(ctx, cudaMemsetAsync(D2 + (size_t)kg * ND * kpad2, 0, (size_t)(nmma - kg * ND) * kpad2,
                                       ctx->stream));
-    k_digits<ND><<<dim3((unsigned)std::min<int64_t>(div_up(kpad2 / 4, 256), 2048), kg), 256, 0, ctx->stream>>>(
+    k_digits<ND, true><<<dim3((unsigned)std::min<int64_t>(div_up(kpad2 / 4, 256), 2048), kg), 256, 0, ctx->stream>>>(
         U, g.Mk, g.Mk, kg, col2, D2, kpad2);
     GLOBE_LAUNCHED(ctx, "k_digits");
     {

@@ -25,15 +25,18 @@ constexpr int NDIG = 9;           // digits per right-hand-side column by defaul
 constexpr int MIN_DIG = 2;        // fewest digits a context may ask for (globe_set_digits)
 
 // The tile-blocked genotype copies hold "tile codes", 2 bits per genotype like the PLINK
-// codes they are made from (re-encoded once, by recode_tile):
-//   00 = genotype 2, 01 = genotype 1, 10 = genotype 0 or missing (11 is not produced).
-// With them the decode needs no shift for the odd codes of a word (see decode_word).
+// codes they are made from (re-encoded once, by recode_tile), equal to the genotype:
+//   00 = genotype 0 or missing, 01 = genotype 1, 10 = genotype 2 (11 is not produced).
+// A field masked in place is then an e4m3 byte proportional to its genotype: at bit offset 0
+// of a byte 0x00 / 0x01 / 0x02 = 0, 2^-9, 2^-8 (subnormals); at offset 2 0x00 / 0x04 / 0x08 =
+// 0, 2^-7, 2^-6.  So the decode is four masks and one shift (decode_word in k_tc_geno.cu).
 __host__ __device__ __forceinline__ uint32_t recode_tile(uint32_t w) {
     const uint32_t lo = w & 0x55555555u, hi = (w >> 1) & 0x55555555u;   // PLINK bit 0 / bit 1 of each code
-    return (hi & ~lo) | (lo << 1);                                      // 00->00, 10->01, 01->10, 11->10
+    // PLINK 00 (g=2) -> 10, 10 (g=1) -> 01, 11 (g=0) and 01 (missing) -> 00
+    return ((~hi & ~lo & 0x55555555u) << 1) | (hi & ~lo);
 }
-// the PLINK code each tile code stands for (missing and genotype 0 share tile code 10)
-__host__ __device__ constexpr int tile_to_plink(int t) { return t == 0 ? 0 : (t == 1 ? 2 : 3); }
+// the PLINK code each tile code stands for (missing and genotype 0 share tile code 00)
+__host__ __device__ constexpr int tile_to_plink(int t) { return t == 1 ? 2 : (t == 2 ? 0 : 3); }
 
 // (sh, sl) += (h, l) in double-float: Knuth's two-sum of the high parts, the rounding error and
 // the low parts into sl (GB300's FP32 pipe is many times its FP64 pipe)
@@ -57,30 +60,44 @@ __host__ __device__ __forceinline__ int64_t blk_offset(int64_t row, int64_t b, i
 }
 
 __device__ __forceinline__ int kpos(int64_t i) {
-    // K position of element i after the decode permutation within groups of 16
+    // K position of element i within groups of 16 in the dense product's operands (digit planes
+    // of A and digits of Z): evens first, then odds
     const int q = (int)(i & 15);
     return (int)(i & ~15ll) + ((q & 1) ? 8 + (q >> 1) : (q >> 1));
 }
+// K position of genotype i of a 16-genotype word after decode_word (k_tc_geno.cu): word r holds
+// the genotypes at field r of the word's four bytes, so position 4 (i % 4) + i / 4.  Its own
+// inverse.  Even genotypes (fields 0 and 2) decode to 2^-9 g, odd ones to 2^-7 g, so the digit
+// operand of the genotype products carries 4 d at even genotypes (geno_digit_mult): every
+// product is then g d 2^-7.
+__host__ __device__ __forceinline__ int kpos_g(int64_t i) {
+    const int q = (int)(i & 15);
+    return (int)(i & ~15ll) + 4 * (q & 3) + (q >> 2);
+}
+__host__ __device__ constexpr int geno_digit_mult(int64_t i) { return (i & 1) ? 1 : 4; }
+constexpr float GENO_UNIT_INV = 128.0f;   // genotype-product partials are multiples of 2^-7
 
-__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], exact in e4m3
+__device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], or 4x that: exact in e4m3
     return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
 }
 
-// 2^e sum_j 32^-j P_j of one row, ND digits per column (rows c*ND + j of the partials).
-// Every FP32 partial is an exact integer (|P| < 2^24), so the split partials are summed in
-// int64 and the digits combined in two exact int64 halves (hi = digits 0..ND_HI-1, lo = the
-// rest); the only rounding is the final FP64 addition.
+// 2^e sum_j 32^-j P_j of one row of a genotype product, ND digits per column (rows c*ND + j
+// of the partials).  Every FP32 partial is an exact multiple of 2^-7 (|P| < 2^17), so it is
+// scaled to an integer, the split partials are summed in int64 and the digits combined in two
+// exact int64 halves (hi = digits 0..ND_HI-1, lo = the rest); the only rounding is the final
+// FP64 addition.
 template <int ND>
 __device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
                                            int64_t row, double s_hi, double s_lo) {
     constexpr int NH = (ND + 1) / 2;
     long long pj[ND];
 #pragma unroll
-    for (int j = 0; j < ND; ++j) pj[j] = (long long)__float2int_rn(part[((int64_t)c * ND + j) * ldp + row]);
+    for (int j = 0; j < ND; ++j)
+        pj[j] = (long long)__float2int_rn(part[((int64_t)c * ND + j) * ldp + row] * GENO_UNIT_INV);
     for (int y = 1; y < nsplit; ++y) {
 #pragma unroll
         for (int j = 0; j < ND; ++j)
-            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * ND + j) * ldp + row]);
+            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * ND + j) * ldp + row] * GENO_UNIT_INV);
     }
     long long hi = 0, lo = 0;
 #pragma unroll
@@ -112,15 +129,17 @@ __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld
 __global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
                              double* __restrict__ colinfo);
 
-// ND digits of X (n x k, FP64) into D[(c*ND + j) * kpad + kpos(r)]  (e4m3); every position
+// ND digits of X (n x k, FP64) into D[(c*ND + j) * kpad + pos(r)]  (e4m3); every position
 // in [0, kpad) of the column's digit rows is written (rows >= n give digit 0).  One thread
-// fills 4 consecutive positions P..P+3 (a 32-bit word): within a group of 16, position
-// P < 8 holds row 2P and P >= 8 holds row 2(P-8)+1 (the inverse of kpos).
+// fills 4 consecutive positions P..P+3 (a 32-bit word).  GENO: the operand of a genotype
+// product -- pos = kpos_g (position P + q of a group of 16 holds row 4 q + P/4) and digits
+// times geno_digit_mult(row); otherwise the dense product's kpos (position P < 8 holds row
+// 2P, P >= 8 row 2(P-8)+1).
 // x 2^-e is rounded once to the integer I = round(x 2^-e 32^(ND-1)), |I| <= 2^(5 ND - 1); its
 // balanced base-32 digits are peeled off from the least significant end in integer
 // arithmetic (d = ((I + 16) mod 32) - 16, in [-16, 15]); the leading digit is what
 // remains, in [-16, 16].  sum_j d_j 32^-j equals x 2^-e rounded to 5 (ND-1) fraction bits.
-template <int ND>
+template <int ND, bool GENO>
 __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, int k, const double* __restrict__ colinfo,
                          uint8_t* __restrict__ D, int64_t kpad) {
     const int c = blockIdx.y;
@@ -130,11 +149,12 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
     for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += (int64_t)gridDim.x * blockDim.x) {
         const int64_t P = w << 2, base = P & ~(int64_t)15;
         const int pl = (int)(P & 15);
+        const int mult = GENO ? geno_digit_mult(pl >> 2) : 1;   // GENO: rows 4 q + pl/4 share its parity
         long long I[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int pq = pl + q;
-            const int64_t src = base + (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1);
+            const int64_t src = base + (GENO ? 4 * q + (pl >> 2) : (pq < 8 ? 2 * pq : 2 * (pq - 8) + 1));
             I[q] = (src < n && !bad) ? __double2ll_rn(X[src + c * ld] * sc) : 0ll;
         }
         uint32_t word[ND];
@@ -146,9 +166,9 @@ __global__ void k_digits(const double* __restrict__ X, int64_t n, int64_t ld, in
             for (int j = ND - 1; j > 0; --j) {
                 const int d = (int)((I[q] + DHALF) & (2 * DHALF - 1)) - DHALF;
                 I[q] = (I[q] - d) >> DBITS;   // exact: I - d is a multiple of 32
-                word[j] |= e4m3_int(d) << (8 * q);
+                word[j] |= e4m3_int(mult * d) << (8 * q);
             }
-            word[0] |= e4m3_int((int)I[q]) << (8 * q);
+            word[0] |= e4m3_int(mult * (int)I[q]) << (8 * q);
         }
 #pragma unroll
         for (int j = 0; j < ND; ++j) *reinterpret_cast<uint32_t*>(D + ((int64_t)c * ND + j) * kpad + P) = word[j];

@@ -1,49 +1,51 @@
 """CPU emulation of the tensor-core genotype product's data layout
 (globe_gb300/csrc/k_tc_geno.cu): the PLINK -> tile-code recoding, the 2-bit ->
-e4m3 byte-permute decode (prmt with its sign-replicate mode), the
-K permutation it induces, base-16 digit slicing of the right-hand sides, the
-exact integer accumulation and the FP64 recombination -- checked against the
-oracle's FP64 GRM product.  Runs without a GPU."""
+e4m3 decode by masks (subnormal bytes 2^-9 g and 2^-7 g), the K permutation it
+induces and the 4x digits at even genotypes that equalise the products, base-32
+digit slicing of the right-hand sides, the exact accumulation (multiples of 2^-7)
+and the FP64 recombination -- checked against the oracle's FP64 GRM product.
+Runs without a GPU."""
 import numpy as np
 
 from helpers import cohort, rel
 
-LUT_A, LUT_B = 0x00003840, 0x00000038
-E4M3 = {0x00: 0.0, 0x38: 1.0, 0x40: 2.0}
+# e4m3 bytes the decode produces: subnormals m 2^-9 (m = 1, 2, 4) and the smallest normal
+E4M3 = {0x00: 0.0, 0x01: 2.0 ** -9, 0x02: 2.0 ** -8, 0x04: 2.0 ** -7, 0x08: 2.0 ** -6}
 NDIG = 9      # balanced base-32 digits
 DBITS = 5
 
 
-def prmt(a, b, s):
-    """PTX prmt.b32 (default mode): selector nibble i of s[15:0] picks byte s&7 of {b, a};
-    with its top bit set, the picked byte's sign bit is replicated."""
-    src = a | (b << 32)
-    out = 0
-    for i in range(4):
-        nib = (s >> (4 * i)) & 0xF
-        byte = (src >> (8 * (nib & 7))) & 0xFF
-        if nib & 8:
-            byte = 0xFF if byte & 0x80 else 0x00
-        out |= byte << (8 * i)
-    return out
+def e4m3_value(byte):
+    """OCP e4m3 (no infinities): sign, 4 exponent bits (bias 7), 3 mantissa bits."""
+    sgn = -1.0 if byte & 0x80 else 1.0
+    e, m = (byte >> 3) & 15, byte & 7
+    return sgn * (m * 2.0 ** -9 if e == 0 else (1 + m / 8) * 2.0 ** (e - 7))
 
 
 def recode_tile(w):
-    """PLINK codes -> tile codes (00 = genotype 2, 01 = 1, 10 = 0 or missing)."""
+    """PLINK codes -> tile codes (00 = genotype 0 or missing, 01 = 1, 10 = 2)."""
     lo, hi = w & 0x55555555, (w >> 1) & 0x55555555
-    return ((hi & ~lo) | (lo << 1)) & 0xFFFFFFFF
+    return (((~hi & ~lo & 0x55555555) << 1) | (hi & ~lo)) & 0xFFFFFFFF
 
 
 def decode_word(w):
-    e = w & 0x33333333
-    o = w & 0xCCCCCCCC
-    return [prmt(LUT_A, LUT_B, e), prmt(LUT_A, LUT_B, e >> 16),
-            prmt(LUT_A, LUT_B, o), prmt(LUT_A, LUT_B, o >> 16)]
+    h = w >> 4
+    return [w & 0x03030303, w & 0x0C0C0C0C, h & 0x03030303, h & 0x0C0C0C0C]
 
 
-def kpos(i):
+def kpos_g(i):
     q = i & 15
-    return (i & ~15) + (8 + (q >> 1) if q & 1 else q >> 1)
+    return (i & ~15) + 4 * (q & 3) + (q >> 2)
+
+
+def unit(i):
+    """Value of genotype 1 at genotype position i after the decode."""
+    return 2.0 ** -9 if i % 2 == 0 else 2.0 ** -7
+
+
+def mult(i):
+    """Digit multiplier at genotype position i: every product becomes g d 2^-7."""
+    return 4.0 if i % 2 == 0 else 1.0
 
 
 def decode_row(packed_row):
@@ -84,7 +86,21 @@ def test_decode_permutation_matches_kpos():
     dec = decode_row(row)
     g = np.where(G[0] < 0, 0, G[0]).astype(float)
     for i in range(64):
-        assert dec[kpos(i)] == g[i]
+        assert dec[kpos_g(i)] == g[i] * unit(i)
+    assert sorted(kpos_g(i) for i in range(64)) == list(range(64))
+    assert all(kpos_g(kpos_g(i)) == i for i in range(64))     # its own inverse
+
+
+def test_decoded_bytes_are_e4m3_multiples():
+    """The masked fields are e4m3 bytes whose values are 0, 1, 2 times one unit."""
+    for off, u in ((0, 2.0 ** -9), (2, 2.0 ** -7)):
+        for code in (0, 1, 2):
+            assert e4m3_value(code << off) == code * u
+    for d in range(-16, 17):     # digits and 4x digits are exact in e4m3 (3 mantissa bits, max 448)
+        for m in (1, 4):
+            v = m * d
+            e = np.frexp(abs(v))[1] if v else 0
+            assert v == 0 or (abs(v) <= 448 and float(np.ldexp(np.rint(np.ldexp(v, 4 - e)), e - 4)) == v)
 
 
 def test_product_emulation_matches_oracle(orc):
@@ -98,7 +114,7 @@ def test_product_emulation_matches_oracle(orc):
     Mk = kept.shape[0]
     rng = np.random.default_rng(5)
     Z = rng.standard_normal((N, 3)) * np.array([1.0, 1e-3, 40.0])
-    # pass 1: rows = SNPs, K = individuals in kpos order
+    # pass 1: rows = SNPs, K = individuals in kpos_g order
     K1 = ((N + 127) // 128) * 128
     A1 = np.zeros((Mk, K1))
     for sidx in range(Mk):
@@ -109,8 +125,8 @@ def test_product_emulation_matches_oracle(orc):
         D, e = digits(Z[:, c])
         B = np.zeros((NDIG, K1))
         for i in range(N):
-            B[:, kpos(i)] = D[:, i]
-        P = A1 @ B.T                       # exact integers
+            B[:, kpos_g(i)] = D[:, i] * mult(i)
+        P = (A1 @ B.T) * 128.0               # exact integers (multiples of 2^-7 before scaling)
         assert np.all(P == np.rint(P)) and np.abs(P).max() < 2 ** 24
         gv = np.ldexp(P @ (32.0 ** -np.arange(NDIG)), e)
         U[:, c] = inv ** 2 * (gv - 2 * f * Z[:, c].sum())
@@ -133,10 +149,11 @@ def test_tile_code_decode_all_words():
     for w in [0, 0xFFFFFFFF, 0x55555555, 0xAAAAAAAA] + [int(x) for x in rng.integers(0, 2 ** 32, 2000)]:
         out = decode_word(recode_tile(w))
         vals = [E4M3[(r >> (8 * i)) & 0xFF] for r in out for i in range(4)]
-        # output order: r0 = genotypes 0,2,4,6; r1 = 8,10,12,14; r2 = 1,3,5,7; r3 = 9,11,13,15
-        order = [0, 2, 4, 6, 8, 10, 12, 14, 1, 3, 5, 7, 9, 11, 13, 15]
-        want = [g_of[(w >> (2 * q)) & 3] for q in order]
+        # output order: r0 = genotypes 0,4,8,12; r1 = 1,5,9,13; r2 = 2,6,10,14; r3 = 3,7,11,15
+        order = [0, 4, 8, 12, 1, 5, 9, 13, 2, 6, 10, 14, 3, 7, 11, 15]
+        want = [g_of[(w >> (2 * q)) & 3] * unit(q) for q in order]
         assert vals == want
+        assert [kpos_g(q) for q in order] == list(range(16))
 
 
 def test_digit_count_error_bound(orc):
