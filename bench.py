@@ -323,17 +323,54 @@ def aireml_compare(G):
             "theta_fp64": [float(v) for v in rf["theta"]]}
 
 
-def headline_parity(G, ctx, theta, numMC, seed, tol=1e-5):
-    """The mixed path against plain FP64 on the benchmark workload itself, at the
-    mixed AIREML estimate theta: one gradient evaluation in each precision with the
-    same probes and fresh solves as runAIREML makes them (fitMME from x0 = Q^-1 b,
-    the probe solves, the AI solve; PCG tolerance 1e-5).  Both precisions follow the
-    same Krylov path, so they take the same iterations and their results agree to
-    far below the tolerance.  From each evaluation the Newton step p = AI^-1 g is
-    formed: the FP64 step's distance from the mixed one, relative to theta, bounds
-    how far one FP64 iteration from theta lands from the mixed iteration; the FP64
-    step's own size is how far theta is from the FP64 fixed point (for these probes)."""
-    res = {}
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _gls(X, S):
+    """beta = (X'V^-1X)^-1 X'V^-1y and V^-1 r = V^-1y - V^-1X beta from S = V^-1 [X y]."""
+    p1 = X.shape[1]
+    beta = np.linalg.solve(X.T @ S[:, :p1], X.T @ S[:, p1])
+    return beta, S[:, p1] - S[:, :p1] @ beta
+
+
+def headline_parity(G, ctx, theta, numMC, seed, X, y, tol=1e-5):
+    """The mixed path against plain FP64 on the benchmark workload itself, at the mixed
+    AIREML estimate theta.
+
+    mme: the mixed solve of V [X y] to relative residual 1e-10; its residual under the FP64
+    operator (b - V x with the FP64 GRM product); an FP64 solve continued from it to 1e-12;
+    beta and V^-1 r (which u-hat and b-hat are linear in) from both.
+
+    evaluation: one AIREML gradient evaluation in each precision with the same probes and
+    fresh solves as runAIREML makes them (fitMME from x0 = Q^-1 b, the probe solves, the AI
+    solve; PCG tolerance 1e-5).  Both take the same iterations; rounding separates their
+    Krylov paths by far less than the tolerance.  From each, the Newton step p = AI^-1 g:
+    the FP64 step's distance from the mixed one, relative to theta, is how far one FP64
+    iteration from theta lands from the mixed iteration; the FP64 step's own size is how
+    far theta is from the FP64 fixed point for these probes (Monte-Carlo noise at numMC)."""
+    ctx.set_vc(theta)
+    B = np.asfortranarray(np.column_stack([X, y]))
+    t0 = time.perf_counter()
+    Xm, im = ctx.pcg(B, tol=1e-10, rule=G.RULE_AIREML, precision=G.PREC_MIXED)
+    t_m = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.set_precision(G.PREC_FP64)
+    try:
+        R = B - ctx.vx(Xm)
+    finally:
+        ctx.set_precision(G.PREC_FP64)
+    res = float(np.max(np.linalg.norm(R, axis=0) / np.linalg.norm(B, axis=0)))
+    X64, i64 = ctx.pcg(B, X0=Xm, tol=1e-12, rule=G.RULE_AIREML, precision=G.PREC_FP64)
+    t_f = time.perf_counter() - t0
+    bm, rm = _gls(X, Xm)
+    bf, rf = _gls(X, X64)
+    mme = {"mixed_tol": 1e-10, "mixed_iterations": im["iters"], "fp64_residual_of_mixed": res,
+           "fp64_continuation_tol": 1e-12, "fp64_iterations": i64["iters"],
+           "beta_max_rel": _rel(bm, bf), "vinv_r_max_rel": _rel(rm, rf), "solution_max_rel": _rel(Xm, X64),
+           "seconds": {"mixed": t_m, "fp64": t_f}}
+    res_ev = {}
     for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
         ctx.set_vc(theta)
         ctx.synchronize()
@@ -341,25 +378,23 @@ def headline_parity(G, ctx, theta, numMC, seed, tol=1e-5):
         m = ctx.mme(tol=tol, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND, precision=prec)
         g = ctx.aireml_grad(numMC, seed=seed, tol=tol, precision=prec)
         ai = ctx.aireml_ai(tol=tol, precision=prec)
-        res[name] = dict(seconds=time.perf_counter() - t0, mme=m, grad=g["grad"], ai=ai, iters=[m["iters"], g["iters"]])
-
-    def rel(a, b):
-        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
-        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-    mx, sf = res["mixed"], res["fp64"]
+        res_ev[name] = dict(seconds=time.perf_counter() - t0, mme=m, grad=g["grad"], ai=ai,
+                            iters=[m["iters"], g["iters"]])
+    mx, sf = res_ev["mixed"], res_ev["fp64"]
     th = np.asarray(theta, np.float64)
     p_m = np.linalg.solve(mx["ai"], mx["grad"])
     p_f = np.linalg.solve(sf["ai"], sf["grad"])
-    mme = {v: rel(mx["mme"][v], sf["mme"][v]) for v in ("beta", "uhat", "bhat")}
-    return {"what": "one AIREML gradient evaluation at the mixed estimate theta*, mixed vs plain FP64 GPU, same "
-                    "probes (seed %d, numMC %d), PCG tol %g" % (seed, numMC, tol),
-            "theta": [float(v) for v in th],
-            "mme_max_rel": mme, "max_rel": max(mme.values()),
-            "grad_max_rel": rel(mx["grad"], sf["grad"]), "ai_max_rel": rel(mx["ai"], sf["ai"]),
-            "newton_step_diff_rel_theta": float(np.abs(p_m - p_f).max() / np.abs(th).max()),
-            "fp64_newton_step_rel_theta": float(np.abs(p_f).max() / np.abs(th).max()),
-            "iterations": {"mixed": mx["iters"], "fp64": sf["iters"]},
-            "seconds": {"mixed": mx["seconds"], "fp64": sf["seconds"]}}
+    ev = {"what": "one AIREML gradient evaluation at theta*, same probes (seed %d, numMC %d), PCG tol %g" % (
+              seed, numMC, tol),
+          "mme_max_rel": {v: _rel(mx["mme"][v], sf["mme"][v]) for v in ("beta", "uhat", "bhat")},
+          "grad_max_rel": _rel(mx["grad"], sf["grad"]), "ai_max_rel": _rel(mx["ai"], sf["ai"]),
+          "newton_step_diff_rel_theta": float(np.abs(p_m - p_f).max() / np.abs(th).max()),
+          "fp64_newton_step_rel_theta": float(np.abs(p_f).max() / np.abs(th).max()),
+          "iterations": {"mixed": mx["iters"], "fp64": sf["iters"]},
+          "seconds": {"mixed": mx["seconds"], "fp64": sf["seconds"]}}
+    return {"what": "mixed vs plain FP64 GPU on this workload at the mixed AIREML estimate theta*",
+            "theta": [float(v) for v in th], "max_rel": max(mme["beta_max_rel"], mme["vinv_r_max_rel"]),
+            "theta_check": ev["newton_step_diff_rel_theta"], "mme": mme, "evaluation": ev}
 
 
 def aggregate_replicas(torch, t_ms, units, device):
@@ -574,7 +609,7 @@ def run_ours(args, cfg):
                   "grad_evals": r["grad_evals"], "pcg_rhs_iters": r["pcg_rhs_iters"],
                   "theta": [float(v) for v in r["theta"]], "numMC": numMC, "tol": 1e-3}
         if not args.no_parity and prec == G.PREC_MIXED and not dense:
-            aireml["parity"] = headline_parity(G, ctx, r["theta"], numMC, SEED + 99)
+            aireml["parity"] = headline_parity(G, ctx, r["theta"], numMC, SEED + 99, X, y)
         if 9 in runs and nd0 != 9:
             t9, r9 = runs[9]
             aireml["nine_digits"] = {"seconds_to_converge": t9, "iterations": r9["iterations"],
@@ -637,6 +672,7 @@ def run_ours(args, cfg):
                     "parallelism": "replicas" if world > 1 else "single GPU",
                     "cuda_graphs": "off in the timed region (per-pass CUDA events); on in e2e and "
                                    "device_unprofiled"},
+            "autotune": ctx.autotune_log(), "device_loop_solves": ctx.device_loop_runs(),
             "e2e": e2e, "roofline": roof, "clocks": clk, "gpu_launches": int(launches),
             "device_unprofiled": graphs_line}
     if fp64 is not None:

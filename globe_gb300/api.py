@@ -187,6 +187,36 @@ class Context:
     def get_graphs(self):
         return bool(self._L.globe_get_graphs(self.h))
 
+    def set_device_loop(self, on):
+        """Run a solve's iterations after the first as one device-side loop (default on)."""
+        self._ck(self._L.globe_set_device_loop(self.h, int(on)))
+
+    def get_device_loop(self):
+        return bool(self._L.globe_get_device_loop(self.h))
+
+    def device_loop_runs(self):
+        """Solves that ran their iterations as the device-side loop."""
+        return int(self._L.globe_device_loop_runs(self.h))
+
+    def set_autotune(self, on):
+        """Time split counts and column groupings of the tensor-core product on first use (default on)."""
+        self._ck(self._L.globe_set_autotune(self.h, int(on)))
+
+    def get_autotune(self):
+        return bool(self._L.globe_get_autotune(self.h))
+
+    def autotune_log(self):
+        """The autotuner's decisions (list of dicts)."""
+        import json
+        n = int(self._L.globe_autotune_log(self.h, None, 0))
+        buf = C.create_string_buffer(n + 1)
+        self._L.globe_autotune_log(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
+    def debug_force_splits(self, splits):
+        """Test hook: every tensor-core genotype pass uses this split count (0 = off)."""
+        self._ck(self._L.globe_debug_force_splits(self.h, int(splits)))
+
     def set_model(self, model):
         """MODEL_FULL (default) or MODEL_NO_TIME (components sig2e, sig2g only)."""
         self._ck(self._L.globe_set_model(self.h, model))

@@ -25,6 +25,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "globe.h"
 
 namespace globe {
@@ -32,6 +34,12 @@ int set_err(globe_ctx* ctx, int code, const char* fmt, ...);   // api.cu
 }
 
 namespace {
+
+// NVTX range for a scope (AIREML iterations and gradient evaluations on a profiler timeline)
+struct Nvtx {
+    explicit Nvtx(const char* name) { nvtxRangePushA(name); }
+    ~Nvtx() { nvtxRangePop(); }
+};
 
 struct Cons {
     // c(p) <= 0 ; gradient; Hessian (only the covariance constraint has one)
@@ -413,6 +421,7 @@ struct Driver {
     std::string err;
 
     int eval_grad(const double* th, double* grad) {
+        Nvtx nvtx("AIREML gradient evaluation");
         int rc = globe_set_vc(ctx, th);
         if (rc) return rc;
         globe_pcg_info info{};
@@ -520,6 +529,7 @@ static int aireml_run_impl(globe_ctx* ctx, const globe_aireml_opts* o, const cha
         if (rc != GLOBE_OK) goto out; \
     } while (0)
     for (i = 0; i < o->maxiter; ++i) {
+        Nvtx nvtx_iter("AIREML iteration");
         d.log.printf("\n=================================\n---------- Iteration %d ----------\n"
                      "=================================\n", i + 1);
         if (i == 0) {

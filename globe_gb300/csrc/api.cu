@@ -190,6 +190,7 @@ void globe_destroy(globe_ctx* ctx) {
     if (ctx->hpin) cudaFreeHost(ctx->hpin);
     for (auto& g : ctx->pcg_graph)
         if (g) cudaGraphExecDestroy(g);
+    if (ctx->pcg_loop) cudaGraphExecDestroy(ctx->pcg_loop);
     for (auto& e : ctx->prof_pool) {
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
@@ -208,6 +209,45 @@ int globe_set_graphs(globe_ctx* ctx, int on) {
 }
 
 int globe_get_graphs(const globe_ctx* ctx) { return ctx ? ctx->graphs : -1; }
+
+int globe_set_device_loop(globe_ctx* ctx, int on) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (on != 0 && on != 1)
+        return set_err(ctx, GLOBE_ERR_ARG, "globe_set_device_loop: on must be 0 or 1, got %d", on);
+    ctx->device_loop = on;
+    return GLOBE_OK;
+}
+
+int globe_get_device_loop(const globe_ctx* ctx) { return ctx ? ctx->device_loop : -1; }
+
+int64_t globe_device_loop_runs(const globe_ctx* ctx) { return ctx ? ctx->device_loop_runs : -1; }
+
+int globe_set_autotune(globe_ctx* ctx, int on) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (on != 0 && on != 1) return set_err(ctx, GLOBE_ERR_ARG, "globe_set_autotune: on must be 0 or 1, got %d", on);
+    ctx->autotune = on;
+    return GLOBE_OK;
+}
+
+int globe_get_autotune(const globe_ctx* ctx) { return ctx ? ctx->autotune : -1; }
+
+int64_t globe_autotune_log(const globe_ctx* ctx, char* buf, int64_t cap) {
+    if (!ctx) return -1;
+    const std::string s = "[" + ctx->tune_log + "]";
+    if (buf && cap > 0) {
+        const int64_t n = std::min<int64_t>(cap - 1, (int64_t)s.size());
+        std::memcpy(buf, s.data(), (size_t)n);
+        buf[n] = 0;
+    }
+    return (int64_t)s.size();
+}
+
+int globe_debug_force_splits(globe_ctx* ctx, int splits) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (splits < 0 || splits > 4096) return set_err(ctx, GLOBE_ERR_ARG, "force_splits: %d not in [0, 4096]", splits);
+    ctx->force_splits = splits;
+    return GLOBE_OK;
+}
 
 int globe_get_stream(globe_ctx* ctx, void** stream) {
     if (!ctx || !stream) return GLOBE_ERR_ARG;

@@ -2,10 +2,12 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -83,7 +85,7 @@ enum SlotId {
     WS_R, WS_Z, WS_P, WS_VP, WS_ZI, WS_GZ, WS_S1, WS_PART, WS_SCAL, WS_COLS, WS_W,
     WS_GPART, WS_B, WS_TMP1, WS_TMP2, WS_TMP3, WS_TMP4, WS_H, WS_HSTAR, WS_PROBE,
     WS_UH, WS_SMALL, WS_IO1, WS_IO2, WS_BHAT, WS_FB, WS_FX,
-    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_COUNT
+    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_LOOP, WS_COUNT
 };
 
 // Scalars kept on the device during a solve (per column, k entries each).
@@ -113,6 +115,13 @@ struct globe_ctx {
     int model = GLOBE_MODEL_FULL; // GLOBE_MODEL_NO_TIME: components (sig2e, sig2g) only
     int digits = 9;               // base-32 digits per column of the tensor-core product (globe_set_digits)
     int stall_next_gemm = 0;      // test hook of the bounded waits (globe_debug_stall_next_gemm)
+    // autotuning of the tensor-core genotype product (k_tc_geno.cu): split-K counts per
+    // (pass, MMA width, rows, K stages) and column groupings per (columns, digits), timed on
+    // first use; 0 = the cost model only (globe_set_autotune)
+    int autotune = 1;
+    int force_splits = 0;         // test hook: every tensor-core launch uses this split count
+    std::map<std::vector<int64_t>, int> tuned;
+    std::string tune_log;         // one JSON object per decision, comma separated
     int nvc() const { return model == GLOBE_MODEL_NO_TIME ? 2 : 5; }
     bool precond_ok = false;      // H built for the current vc
     globe::Slot ws[globe::WS_COUNT];
@@ -131,6 +140,10 @@ struct globe_ctx {
     // swapped r'z buffers; updated in place from each call's capture
     int graphs = 1;
     cudaGraphExec_t pcg_graph[2] = {nullptr, nullptr};
+    // the device-side PCG loop of the last call (one WHILE conditional node), and whether to use it
+    cudaGraphExec_t pcg_loop = nullptr;
+    int device_loop = 1;
+    int64_t device_loop_runs = 0;
     bool capturing = false;       // a stream capture is open: allocation is refused
     // event profiling (globe_prof_*)
     bool prof_on = false;
@@ -184,10 +197,26 @@ inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 // profiling scopes: prof_begin returns a handle (or -1 when off)
 int prof_begin(globe_ctx* ctx, int kind);
 void prof_end(globe_ctx* ctx, int h);
+// An NVTX range for the lifetime of a scope: the solve's structure (solves, iterations,
+// GRM products and their passes, AIREML steps) on an Nsight Systems or ncu --nvtx
+// timeline.  Without a tool attached the calls return at once.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+inline const char* prof_kind_name(int kind) {
+    static const char* names[GLOBE_PROF_KINDS] = {"GRM product", "GRM pass 1", "GRM pass 2", "PCG iteration",
+                                                  "GRM build", "GRM build GEMM", "profile kind 6", "profile kind 7"};
+    return (kind >= 0 && kind < GLOBE_PROF_KINDS) ? names[kind] : "profile kind";
+}
+// CUDA-event timing of one kind of work (globe_prof_enable) and its NVTX range
 struct ProfScope {
     globe_ctx* c;
     int h;
-    ProfScope(globe_ctx* ctx, int kind) : c(ctx), h(prof_begin(ctx, kind)) {}
+    NvtxRange r;
+    ProfScope(globe_ctx* ctx, int kind) : c(ctx), h(prof_begin(ctx, kind)), r(prof_kind_name(kind)) {}
     ~ProfScope() { prof_end(c, h); }
 };
 

@@ -33,6 +33,11 @@
 // permutes K within each group of 16, which the digit tiles repeat (kpos_g()).
 // Every mbarrier wait is bounded (globaltimer); on timeout the CTA records
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
 #include "tc_ptx.cuh"
 
 namespace globe {
@@ -648,31 +653,108 @@ int eff_splits(int nchunks, int splits) {
     return (nchunks + cps - 1) / cps;
 }
 
-// Split-K count for `tiles` CTA row blocks of `nchunks` K stages.  One CTA runs per SM, so
-// the pass takes about ceil(CTAs / SMs) waves of (stages per CTA + a fixed CTA cost: setup,
-// pipeline fill and drain, epilogue).  The count minimising that estimate is taken, within
-// K per CTA <= 2^19 (exact FP32 sums) and >= 8 stages per CTA.  Example: 196 row blocks x
-// 3907 stages gives 10 splits (1960 CTAs, 12.9 waves on 152 SMs) where aiming at ~8 waves
-// gave 7 (1372 CTAs, 9.03 waves: a tenth wave of 4 CTAs).
-static int pick_splits(globe_ctx* ctx, int tiles, int nchunks) {
+// Split-K candidates for `tiles` CTA row blocks of `nchunks` K stages.  One CTA runs per SM,
+// so the pass takes about ceil(CTAs / SMs) waves of (stages per CTA + a fixed CTA cost: setup,
+// pipeline fill and drain, epilogue).  The count minimising that estimate comes first, within
+// K per CTA <= 2^19 (exact FP32 sums) and >= 8 stages per CTA; then up to 4 more effective
+// counts whose estimate is within 25% of it (the autotuner times them).  Example: 196 row
+// blocks x 3907 stages gives 10 splits (1960 CTAs, 12.9 waves on 152 SMs) where aiming at ~8
+// waves gave 7 (1372 CTAs, 9.03 waves: a tenth wave of 4 CTAs).
+static std::vector<int> split_candidates(globe_ctx* ctx, int tiles, int nchunks) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || sms < 1) sms = 152;
     constexpr int CTA_COST = 8;                       // fixed cost of a CTA, in stages
     const int lo = std::max(1, (nchunks + 4095) / 4096);
     const int hi = std::max(lo, std::min(64, nchunks / 8));
-    int best = lo;
-    double best_cost = 1e300;
+    std::vector<std::pair<double, int>> est;          // (cost, split count) per effective count
+    int prev_se = -1;
     for (int s = lo; s <= hi; ++s) {
         const int cps = (nchunks + s - 1) / s;
         const int se = (nchunks + cps - 1) / cps;
+        if (se == prev_se) continue;
+        prev_se = se;
         const double waves = std::ceil((double)tiles * se / sms);
-        const double cost = waves * (cps + CTA_COST);
-        if (cost < best_cost * 0.999) {
-            best_cost = cost;
-            best = s;
-        }
+        est.push_back({waves * (cps + CTA_COST), s});
     }
-    return best;
+    std::stable_sort(est.begin(), est.end(),
+                     [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first < b.first * 0.999; });
+    std::vector<int> out;
+    for (const auto& e : est)
+        if (out.size() < 5 && e.first <= est[0].first * 1.25) out.push_back(e.second);
+    return out;
+}
+
+static void tune_note(globe_ctx* ctx, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (!ctx->tune_log.empty()) ctx->tune_log += ",";
+    ctx->tune_log += buf;
+}
+
+// Time each of `nc` variants (run(i) issues variant i on the stream) over `rounds` rounds with
+// CUDA events on the context's stream; the last round's times go to ms[].  Returns the index
+// of the fastest, the first variant unless another is more than 1% faster.
+template <class F>
+static int time_variants(globe_ctx* ctx, int nc, int rounds, F&& run, std::vector<float>& ms, int* best) {
+    std::vector<cudaEvent_t> ev(2 * nc, nullptr);
+    for (auto& e : ev) GLOBE_CK(ctx, cudaEventCreate(&e));
+    int rc = GLOBE_OK;
+    for (int r = 0; r < rounds && rc == GLOBE_OK; ++r)
+        for (int i = 0; i < nc && rc == GLOBE_OK; ++i) {
+            cudaEventRecord(ev[2 * i], ctx->stream);
+            rc = run(i);
+            cudaEventRecord(ev[2 * i + 1], ctx->stream);
+        }
+    if (rc == GLOBE_OK) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GLOBE_OK : GLOBE_ERR_CUDA;
+    ms.assign(nc, 0.0f);
+    *best = 0;
+    for (int i = 0; i < nc && rc == GLOBE_OK; ++i) {
+        cudaEventElapsedTime(&ms[i], ev[2 * i], ev[2 * i + 1]);
+        if (ms[i] < ms[*best] * 0.99f) *best = i;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (rc != GLOBE_OK) return set_err(ctx, rc, "autotuning: %s", cudaGetErrorString(cudaGetLastError()));
+    return GLOBE_OK;
+}
+
+// The split count of one genotype pass: the test override, the tuned choice of this shape, or
+// -- on its first use, with autotuning on, outside graph capture and event profiling -- each
+// candidate launched twice and timed, the fastest kept for the context.  Every count gives the
+// same result bits (the split partials are exact and are summed in int64), so the candidates
+// run on the real operands and the pass's own launch follows.
+static int tune_splits(globe_ctx* ctx, int pass, int nmma, const uint8_t* blk, const CUtensorMap& mB, int rows,
+                       int nchunks, const std::vector<int>& cand, float* part, int64_t ldp, unsigned* err, int* out) {
+    if (ctx->force_splits > 0) {   // at least the count that keeps K per CTA <= 2^19
+        *out = std::max(ctx->force_splits, (nchunks + 4095) / 4096);
+        return GLOBE_OK;
+    }
+    const std::vector<int64_t> key = {1, pass, nmma, rows, nchunks};
+    const auto hit = ctx->tuned.find(key);
+    if (hit != ctx->tuned.end()) {
+        *out = hit->second;
+        return GLOBE_OK;
+    }
+    *out = cand[0];
+    if (!ctx->autotune || ctx->capturing || ctx->prof_on || cand.size() < 2) return GLOBE_OK;
+    std::vector<float> ms;
+    int best = 0;
+    GLOBE_RET(time_variants(ctx, (int)cand.size(), 2, [&](int i) {
+        return gemm_dispatch(ctx, nmma, blk, mB, rows, nchunks, cand[i], part, ldp, err, ZGrid());
+    }, ms, &best));
+    *out = cand[best];
+    ctx->tuned[key] = *out;
+    std::string t;
+    for (size_t i = 0; i < cand.size(); ++i) {
+        char b[48];
+        std::snprintf(b, sizeof b, "%s\"%d\": %.4f", i ? ", " : "", cand[i], ms[i]);
+        t += b;
+    }
+    tune_note(ctx, "{\"kind\": \"splits\", \"pass\": %d, \"mma_width\": %d, \"rows\": %d, \"k_stages\": %d, "
+              "\"model\": %d, \"choice\": %d, \"ms\": {%s}}", pass, nmma, rows, nchunks, cand[0], *out, t.c_str());
+    return GLOBE_OK;
 }
 
 // out (N x k) = scale * Zs'(Zs Z) for one group of <= 256 / ND columns, ND digits per column
@@ -688,7 +770,13 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     const int64_t kpad2 = (int64_t)nch2 * BK;
     const int rpc = rows_per_cta(nmma);
     const int tiles1 = (int)((g.Mk + rpc - 1) / rpc), tiles2 = (N + rpc - 1) / rpc;
-    const int sp1 = pick_splits(ctx, tiles1, nch1), sp2 = pick_splits(ctx, tiles2, nch2);
+    const std::vector<int> cand1 = split_candidates(ctx, tiles1, nch1), cand2 = split_candidates(ctx, tiles2, nch2);
+    auto most = [&](const std::vector<int>& c, int nch) {   // partial slots for any count used below
+        int m = std::max(ctx->force_splits, (nch + 4095) / 4096);
+        for (int v : c) m = std::max(m, v);
+        return m;
+    };
+    const int spmax1 = most(cand1, nch1), spmax2 = most(cand2, nch2);
     const int64_t ldp1 = (int64_t)tiles1 * rpc, ldp2 = (int64_t)tiles2 * rpc;
     uint8_t *D1, *D2;
     float *P1, *P2;
@@ -696,8 +784,8 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     unsigned* err;
     GLOBE_RET(ws(ctx, WS_TC_D1, (size_t)nmma * kpad1, &D1));
     GLOBE_RET(ws(ctx, WS_TC_D2, (size_t)nmma * kpad2, &D2));
-    GLOBE_RET(ws(ctx, WS_TC_P1, (size_t)(sp1 + 1) * nmma * ldp1, &P1));
-    GLOBE_RET(ws(ctx, WS_TC_P2, (size_t)(sp2 + 1) * nmma * ldp2, &P2));
+    GLOBE_RET(ws(ctx, WS_TC_P1, (size_t)(spmax1 + 1) * nmma * ldp1, &P1));
+    GLOBE_RET(ws(ctx, WS_TC_P2, (size_t)(spmax2 + 1) * nmma * ldp2, &P2));
     GLOBE_RET(ws(ctx, WS_TC_U, (size_t)g.Mk * kg + 1, &U));
     const int nbr = 304;
     GLOBE_RET(ws(ctx, WS_TC_SCAL, (size_t)(4 * kg + 2 * nbr * kg + 8), &cst));
@@ -723,6 +811,8 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
         Z, N, N, kg, col1, D1, kpad1);
     GLOBE_LAUNCHED(ctx, "k_digits");
     // ---- pass 1
+    int sp1 = 0;
+    GLOBE_RET(tune_splits(ctx, 1, nmma, g.blk1, mB1, (int)g.Mk, nch1, cand1, P1, ldp1, err, &sp1));
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS1);
         ZGrid zg;
@@ -742,6 +832,8 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     k_digits<ND, true><<<dim3((unsigned)std::min<int64_t>(div_up(kpad2 / 4, 256), 2048), kg), 256, 0, ctx->stream>>>(
         U, g.Mk, g.Mk, kg, col2, D2, kpad2);
     GLOBE_LAUNCHED(ctx, "k_digits");
+    int sp2 = 0;
+    GLOBE_RET(tune_splits(ctx, 2, nmma, g.blk2, mB2, N, nch2, cand2, P2, ldp2, err, &sp2));
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS2);
         GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, mB2, N, nch2, sp2, P2, ldp2, err, ZGrid()));
@@ -783,12 +875,39 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
     const int gmax = 256 / nd, gtwo = 192 / nd;
     int ng = (k + gmax - 1) / gmax;
     if (ng > 1) ng = (k + gtwo - 1) / gtwo;
-    for (int gi = 0, c0 = 0; gi < ng; ++gi) {
-        const int kg = k / ng + (gi < k % ng ? 1 : 0);
-        GLOBE_RET(tc_group_nd(ctx, nd, Z + (size_t)c0 * N, kg, scale, out + (size_t)c0 * N));
-        c0 += kg;
+    auto run = [&](int ngroups) -> int {
+        for (int gi = 0, c0 = 0; gi < ngroups; ++gi) {
+            const int kg = k / ngroups + (gi < k % ngroups ? 1 : 0);
+            GLOBE_RET(tc_group_nd(ctx, nd, Z + (size_t)c0 * N, kg, scale, out + (size_t)c0 * N));
+            c0 += kg;
+        }
+        return GLOBE_OK;
+    };
+    // Column grouping: the rule above, or -- for 9 or more columns, on first use of (k, digits),
+    // with autotuning on, outside capture and profiling -- the fastest of it, one group more and
+    // twice as many groups, timed over two rounds (the first also tunes the groups' split
+    // counts).  Each column's digits and sums do not depend on its group, so every grouping
+    // gives the same bits and the last run's output stands.
+    const std::vector<int64_t> key = {2, k, nd};
+    const auto hit = ctx->tuned.find(key);
+    if (hit != ctx->tuned.end()) return run(hit->second);
+    if (!ctx->autotune || ctx->capturing || ctx->prof_on || ctx->force_splits > 0 || k < 9) return run(ng);
+    std::vector<int> cand = {ng};
+    for (int alt : {ng + 1, 2 * ng})
+        if (alt <= k && std::find(cand.begin(), cand.end(), alt) == cand.end()) cand.push_back(alt);
+    std::vector<float> ms;
+    int best = 0;
+    GLOBE_RET(time_variants(ctx, (int)cand.size(), 2, [&](int i) { return run(cand[i]); }, ms, &best));
+    ctx->tuned[key] = cand[best];
+    std::string t;
+    for (size_t i = 0; i < cand.size(); ++i) {
+        char b[48];
+        std::snprintf(b, sizeof b, "%s\"%d\": %.4f", i ? ", " : "", cand[i], ms[i]);
+        t += b;
     }
-    return GLOBE_OK;
+    tune_note(ctx, "{\"kind\": \"groups\", \"columns\": %d, \"digits\": %d, \"model\": %d, \"choice\": %d, "
+              "\"ms\": {%s}}", k, nd, ng, cand[best], t.c_str());
+    return run(cand[best]);
 }
 
 // The tensor-core kernels' error word: word 0 of the WS_TC_ERR slot (words 1-2 serve

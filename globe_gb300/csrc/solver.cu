@@ -138,6 +138,164 @@ static bool capture_body(globe_ctx* ctx, int slot, F&& body, int64_t* nlaunch) {
     return ok;
 }
 
+// ---- the PCG iterations after the first, as one device-side loop -------------------
+//
+// One graph: a kernel that arms a WHILE conditional node, then the node, whose body is
+// one iteration (the same kernels, in the same order, as a host-driven iteration) followed
+// by k_pcg_check, which applies the stopping rule of the host loop below to the device
+// copies of r'r and p'Vp and sets the node's condition, and by the beta / r'z shift.
+// So the iterations run without a host synchronisation each, with bit-identical
+// results and iteration counts.  The condition's launch default is 0: only the arming
+// kernel opens the loop, so a condition that could not be set leaves the loop unrun
+// (the host then sees no iteration and carries on itself); inside it every path of the
+// check sets it, and the iteration cap always closes it.
+
+struct PcgLoopState {
+    double last;          // last max ratio (PCGsolver rule, stagnation)
+    long long rhs_iters;  // sum over iterations of active columns
+    int it;               // iterations completed
+    int stag;             // iterations in a row with < 0.5% improvement
+    int status;           // 0 running, 1 converged, 2 stagnated, 3 iteration cap, 4 breakdown
+    int err_col;          // column of a breakdown
+};
+
+__global__ void k_pcg_loop_arm(cudaGraphConditionalHandle h) { cudaGraphSetConditional(h, 1u); }
+
+// the host loop's stopping rule (pcg_run) on the device: one thread, after iteration st->it + 1
+__global__ void k_pcg_check(const double* __restrict__ rr, const double* __restrict__ pvp,
+                            const double* __restrict__ bb, const int32_t* __restrict__ cols, int kact, int k,
+                            double tol, int rule, int maxit, PcgLoopState* st, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int it = st->it + 1;
+    st->it = it;
+    st->rhs_iters += kact;
+    for (int c = 0; c < kact; ++c) {
+        const int j = cols[c];
+        if (!(pvp[j] > 0.0) || !isfinite(rr[j])) {
+            st->status = 4;
+            st->err_col = j;
+            cudaGraphSetConditional(h, 0u);
+            return;
+        }
+    }
+    bool stop = false;
+    if (rule == GLOBE_RULE_PCGSOLVER) {
+        const double small_b = (double)1e-12f;  // PCGsolver.cpp:1365, :1393
+        double mx = 0.0;
+        for (int j = 0; j < k; ++j) {
+            const double nb = sqrt(bb[j]);
+            const double q = nb > small_b ? sqrt(rr[j]) / nb : 0.0;
+            if (q > mx) mx = q;
+        }
+        if (mx < tol) {
+            st->status = 1;
+            stop = true;
+        } else {
+            const double last = st->last;
+            if (last - mx < (double)5e-3f * last) ++st->stag;
+            else st->stag = 0;
+            st->last = mx;
+            if (st->stag >= 10) {
+                st->status = 2;
+                stop = true;
+            }
+        }
+    } else {
+        bool all = true;
+        for (int j = 0; j < k; ++j)
+            if (bb[j] > 0.0 && !(sqrt(rr[j]) < tol * sqrt(bb[j]))) {
+                all = false;
+                break;
+            }
+        if (all) {
+            st->status = 1;
+            stop = true;
+        }
+    }
+    if (!stop && it >= maxit) {
+        st->status = 3;
+        stop = true;
+    }
+    cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
+// beta = r'z(new) / r'z(old) (0 where r'z(old) = 0, as k_scal_div), then r'z(old) = r'z(new)
+__global__ void k_pcg_beta_shift(double* __restrict__ rz, const double* __restrict__ rz2, double* __restrict__ beta,
+                                 int k) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < k) {
+        const double o = rz[c], nw = rz2[c];
+        beta[c] = (o != 0.0) ? nw / o : 0.0;
+        rz[c] = nw;
+    }
+}
+
+// Build and run the loop graph; body(h) issues one iteration and its check on the stream.
+// Returns GLOBE_OK with *ran = false (nothing run) when the graph cannot be built.
+template <class F>
+static int run_device_loop(globe_ctx* ctx, F&& body, int64_t* nlaunch, bool* ran) {
+    *ran = false;
+    const std::string err0 = ctx->err;
+    const int64_t l0 = ctx->launches;
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle h;
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+              cudaGraphConditionalHandleCreate(&h, g, 0u, cudaGraphCondAssignDefault) == cudaSuccess;
+    // the arming kernel, captured into g
+    cudaGraphNode_t arm = nullptr;
+    if (ok) {
+        ok = cudaStreamBeginCaptureToGraph(ctx->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+             cudaSuccess;
+        if (ok) {
+            k_pcg_loop_arm<<<1, 1, 0, ctx->stream>>>(h);
+            cudaGraph_t gg = nullptr;
+            ok = cudaStreamEndCapture(ctx->stream, &gg) == cudaSuccess && gg == g;
+            size_t nn = 1;
+            ok = ok && cudaGraphGetNodes(g, &arm, &nn) == cudaSuccess && nn == 1;
+        }
+    }
+    cudaGraph_t bodyg = nullptr;
+    if (ok) {
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        ok = cudaGraphAddNode(&node, g, &arm, nullptr, 1, &np) == cudaSuccess;
+        if (ok) bodyg = np.conditional.phGraph_out[0];
+    }
+    int rc = GLOBE_OK;
+    if (ok) {
+        ok = cudaStreamBeginCaptureToGraph(ctx->stream, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+             cudaSuccess;
+        if (ok) {
+            ctx->capturing = true;
+            rc = body(h);
+            ctx->capturing = false;
+            cudaGraph_t gb = nullptr;
+            ok = cudaStreamEndCapture(ctx->stream, &gb) == cudaSuccess && rc == GLOBE_OK;
+        }
+    }
+    *nlaunch = ctx->launches - l0;
+    ctx->launches = l0;
+    if (ok) {
+        if (ctx->pcg_loop) cudaGraphExecDestroy(ctx->pcg_loop);
+        ctx->pcg_loop = nullptr;
+        ok = cudaGraphInstantiate(&ctx->pcg_loop, g, 0) == cudaSuccess;
+        if (!ok) ctx->pcg_loop = nullptr;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        ctx->err = err0;
+        return GLOBE_OK;
+    }
+    GLOBE_CK(ctx, cudaGraphLaunch(ctx->pcg_loop, ctx->stream));
+    *ran = true;
+    return GLOBE_OK;
+}
+
 static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info) {
     GLOBE_RET(check_ready(ctx));
     if (k < 1) return set_err(ctx, GLOBE_ERR_ARG, "number of right-hand sides must be >= 1");
@@ -158,6 +316,8 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     GLOBE_RET(ws(ctx, WS_SCAL, (size_t)8 * k, &scal));
     GLOBE_RET(ws(ctx, WS_COLS, (size_t)k, &dcols));
     GLOBE_RET(ws(ctx, WS_PART, (size_t)std::max<int64_t>(div_up(N, 8), 304) * k * 2, &part));
+    PcgLoopState* dstate;
+    GLOBE_RET(ws(ctx, WS_LOOP, 1, &dstate));
     const double* H = Hptr(ctx);
     double* rz = scal;
     double* rz2 = scal + k;
@@ -294,6 +454,51 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
         }
         GLOBE_RET(scal_alpha(ctx, rz2, rz, beta, k));
         std::swap(rz, rz2);
+        // after the first iteration, the rest as one device-side loop (no per-iteration
+        // synchronisation) when graphs are on and the column set cannot change
+        if (it == 0 && use_graph && ctx->device_loop && !o->mask && o->maxit > 1) {
+            const PcgLoopState st0{last, 0, 1, stag, 0, -1};
+            GLOBE_CK(ctx, cudaMemcpyAsync(dstate, &st0, sizeof st0, cudaMemcpyHostToDevice, ctx->stream));
+            const int kc = kact;
+            auto loop_body = [&](cudaGraphConditionalHandle h) -> int {
+                GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kc, Zi, S1));
+                GLOBE_RET(grm_apply_dev(ctx, Zi, kc, GZ));
+                GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kc, Vp, pvp));
+                GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
+                GLOBE_RET(pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kc, rr, rz2));
+                k_pcg_check<<<1, 32, 0, ctx->stream>>>(rr, pvp, bb, dcols, kc, k, o->tol, o->rule, o->maxit, dstate,
+                                                       h);
+                GLOBE_LAUNCHED(ctx, "k_pcg_check");
+                k_pcg_beta_shift<<<div_up(k, 128), 128, 0, ctx->stream>>>(rz, rz2, beta, k);
+                GLOBE_LAUNCHED(ctx, "k_pcg_beta_shift");
+                return GLOBE_OK;
+            };
+            int64_t per_it = 0;
+            bool ran = false;
+            GLOBE_RET(run_device_loop(ctx, loop_body, &per_it, &ran));
+            if (ran) {
+                PcgLoopState st;
+                double* h_scr = ctx->hpin + 3 * k;   // k doubles: the final r'r
+                GLOBE_CK(ctx, cudaMemcpyAsync(&st, dstate, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+                GLOBE_CK(ctx, cudaMemcpyAsync(h_scr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+                GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+                GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+                if (st.it > 1) {   // the loop ran (see run_device_loop)
+                    ctx->launches += per_it * (st.it - 1) + 1;
+                    ctx->device_loop_runs += 1;
+                    rhs_iters += st.rhs_iters;
+                    for (int j : cols) nr[j] = std::sqrt(h_scr[j]);
+                    if (st.status == 4)
+                        return set_err(ctx, GLOBE_ERR_NUMERIC, "PCG breakdown in column %d at iteration %d (p'Vp = %g)",
+                                       st.err_col, st.it, h_pvp[st.err_col]);
+                    converged = st.status == 1;
+                    stagnated = st.status == 2;
+                    it = st.it;
+                    break;
+                }
+            }
+            use_graph = use_graph && ran;
+        }
     }
     if (info) {
         info->iters = it;
@@ -435,12 +640,14 @@ int globe_genetic_diag(globe_ctx* ctx, double* diag) {
 
 int globe_pcg_dev(globe_ctx* ctx, const double* d_B, double* d_X, int k, const globe_pcg_opts* opts,
                   globe_pcg_info* info) {
+    NvtxRange nvtx("globe_pcg_dev");
     if (!ctx || !d_B || !d_X) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     return pcg_dev(ctx, d_B, d_X, k, opts, info);
 }
 
 int globe_pcg(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* opts, globe_pcg_info* info) {
+    NvtxRange nvtx("globe_pcg");
     if (!ctx || !B || !X || k < 1) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));
@@ -706,6 +913,7 @@ static int check_prec(globe_ctx* ctx, const globe_pcg_opts* o) {
 
 int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* uhat, double* bhat, double* vinv_r,
               globe_pcg_info* info) {
+    NvtxRange nvtx("globe_mme");
     if (!ctx || !opts) return GLOBE_ERR_ARG;
     GLOBE_RET(check_prec(ctx, opts));
     int rc;
@@ -718,6 +926,7 @@ int globe_mme(globe_ctx* ctx, const globe_pcg_opts* opts, double* beta, double* 
 
 int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
                       double* f_theta, double* first, double* trace, double* grad, globe_pcg_info* info) {
+    NvtxRange nvtx("globe_aireml_grad");
     if (!ctx || !opts) return GLOBE_ERR_ARG;
     GLOBE_RET(check_prec(ctx, opts));
     int rc;
@@ -730,6 +939,7 @@ int globe_aireml_grad(globe_ctx* ctx, const double* probes, int numMC, uint64_t 
 
 int globe_aireml_eval(globe_ctx* ctx, const double* probes, int numMC, uint64_t seed, const globe_pcg_opts* opts,
                       double* first, double* trace, double* grad, globe_pcg_info* info) {
+    NvtxRange nvtx("globe_aireml_eval");
     if (!ctx || !opts) return GLOBE_ERR_ARG;
     GLOBE_RET(check_prec(ctx, opts));
     int rc;
@@ -741,6 +951,7 @@ int globe_aireml_eval(globe_ctx* ctx, const double* probes, int numMC, uint64_t 
 }
 
 int globe_aireml_ai(globe_ctx* ctx, const globe_pcg_opts* opts, double* ai, globe_pcg_info* info) {
+    NvtxRange nvtx("globe_aireml_ai");
     if (!ctx || !opts || !ai) return GLOBE_ERR_ARG;
     cudaSetDevice(ctx->device);
     GLOBE_RET(check_ready(ctx));

@@ -222,13 +222,52 @@ int globe_get_digits(const globe_ctx* ctx);
  * Each globe_pcg call runs its first iteration directly. It then captures the
  * iteration's stream work (record kernels, GRM product, the copies of the
  * residual norms) once per parity of its swapped r'z buffers and column set,
- * and replays it. The per-iteration host check of the stopping rule stays.
+ * and replays it, with the host checking the stopping rule after each
+ * iteration (or, by default, once per solve: globe_set_device_loop).
  * Results are identical either way. Graphs are not used while event
  * profiling is on (globe_prof_enable), so that each pass is timed, nor when a
  * capture fails (e.g. a workspace would have to grow); the iteration then
  * launches the same kernels directly.  No reference counterpart. */
 int globe_set_graphs(globe_ctx* ctx, int on);
 int globe_get_graphs(const globe_ctx* ctx);
+
+/* Device-side PCG loop (on = 1, the default; needs graphs on).  Without
+ * per-column masking the column set of a solve cannot change, so after the
+ * first iteration the rest run as one CUDA graph whose WHILE conditional node
+ * repeats the iteration; a one-thread kernel at the end of each iteration
+ * applies the stopping rule of the reference -- max_j |r_j|/|b_j| < tol and the
+ * stagnation stop (PCGsolver.cpp:1373-1415), or all_j |r_j| < tol |b_j|
+ * (varCompEst.cpp:505-508) -- to the device copies of the residual norms and
+ * sets the node's condition.  No host synchronisation per iteration; the same
+ * kernels in the same order, so the same results and iteration counts as the
+ * host-checked loop (on = 0).  With masking, while profiling, or if the graph
+ * cannot be built, the host checks every iteration.  globe_device_loop_runs
+ * counts the solves that used it.  No reference counterpart. */
+int globe_set_device_loop(globe_ctx* ctx, int on);
+int globe_get_device_loop(const globe_ctx* ctx);
+int64_t globe_device_loop_runs(const globe_ctx* ctx);
+
+/* Autotuning of the tensor-core genotype product (on = 1, the default; 0 =
+ * the analytic choices only).  On first use of a shape in a context -- outside
+ * graph capture and event profiling -- the product times its candidates with
+ * CUDA events on the context's stream and keeps the fastest:
+ *  - the split-K count of each pass (per MMA width, rows and K stages): the
+ *    wave-quantisation cost model's count and up to 4 more within 25% of its
+ *    estimate, two launches each;
+ *  - for 9 or more right-hand-side columns, the column grouping (per column
+ *    count and digit count): the rule's group count, one more and twice as
+ *    many, two rounds each.
+ * Every candidate gives the same result bits (exact sums in any split or
+ * group), so the choice changes speed only.  globe_autotune_log writes the
+ * decisions as a JSON array into buf (cap bytes, NUL-terminated, truncated if
+ * short) and returns the full length.  globe_debug_force_splits(ctx, s), s > 0,
+ * makes every tensor-core genotype pass use s splits (a test hook; 0 = off).
+ * The reference hard-codes its SNP chunk instead (SNP_CHUNK_SIZE,
+ * PCGsolver.cpp:1135). */
+int globe_set_autotune(globe_ctx* ctx, int on);
+int globe_get_autotune(const globe_ctx* ctx);
+int64_t globe_autotune_log(const globe_ctx* ctx, char* buf, int64_t cap);
+int globe_debug_force_splits(globe_ctx* ctx, int splits);
 
 /* Test hook for the tensor-core kernels' bounded waits: the next tensor-core
  * GRM product's first launch (genotype or dense) leaves its first stage

@@ -146,3 +146,82 @@ def test_graph_replay_matches_direct_launches(gctx, src, prec):
         assert ng == nd_
     with pytest.raises(G.GlobeError):
         gctx.set_graphs(2)
+
+
+def _solve(ctx, B, device_loop, **kw):
+    ctx.set_device_loop(device_loop)
+    try:
+        runs0 = ctx.device_loop_runs()
+        X, info = ctx.pcg(B, **kw)
+        return X, info, ctx.device_loop_runs() - runs0
+    finally:
+        ctx.set_device_loop(True)
+
+
+@pytest.fixture(scope="module")
+def own(orc):
+    """A context of its own (the shared one is reloaded by other tests of this module)."""
+    c = golden_case("geno_small")
+    with G.Context(0) as ctx:
+        ctx.load_records(c["indiv"], c["X"], c["y"], c["N"])
+        ctx.load_bed(c["packed"])
+        ctx.set_vc(VC_F)
+        s = orc.Solver(c["indiv"], c["X"], c["y"], c["N"], VC_F, packed=c["packed"])
+        s.precond_build()
+        yield ctx, s, np.column_stack([c["X"], c["y"]])
+
+
+CASES = [dict(tol=1e-12, rule=G.RULE_PCGSOLVER), dict(tol=1e-11, rule=G.RULE_AIREML),
+         dict(tol=1e-11, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND), dict(tol=1e-14, rule=G.RULE_AIREML, maxit=4),
+         dict(tol=1e-12, rule=G.RULE_PCGSOLVER, precision=G.PREC_MIXED)]
+
+
+@pytest.mark.parametrize("kw", CASES, ids=["pcgsolver", "aireml", "aireml-x0", "cap", "mixed"])
+def test_device_loop_matches_host_loop(own, kw):
+    """The device-side loop (WHILE graph node, stopping rule checked on the device) gives
+    the host-checked loop's solution bit for bit and the same iteration counts."""
+    ctx, s, B = own
+    assert ctx.get_graphs()
+    Xh, ih, nh = _solve(ctx, B, False, **kw)
+    Xd, idv, nd = _solve(ctx, B, True, **kw)
+    assert nh == 0 and nd == 1
+    assert np.array_equal(Xd, Xh)
+    for key in ("iters", "rhs_iters", "converged", "stagnated"):
+        assert idv[key] == ih[key], key
+    assert idv["max_rel_res"] == ih["max_rel_res"]
+
+
+def _ill_conditioned(seed=1, N=1500):
+    """A dense GRM with eigenvalues spaced evenly in [1e-9, 1] and every other variance
+    component 1e-10: kappa(V) ~ 1e9, so after its fast start CG gains well under 0.5% per
+    iteration on the slowest column."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((N, N)))
+    A = (Q * np.linspace(1e-9, 1.0, N)) @ Q.T
+    lt = ((A + A.T) / 2)[np.tril_indices(N)].astype(np.float32)
+    t = rng.uniform(0, 5, N)
+    X = np.asfortranarray(np.column_stack([np.ones(N), rng.standard_normal(N), t]))
+    return np.arange(N, dtype=np.int32), X, rng.standard_normal(N), N, (1e-10, 1.0, 1e-10, 0.0, 1e-10), lt
+
+
+def test_stagnation_stop(orc):
+    """runPCGsolver's stagnation stop (PCGsolver.cpp:1373-1415): 10 iterations in a row
+    with < 0.5% improvement of the largest relative residual end the solve unconverged --
+    on the device loop and the host loop alike (same iterations, same bits), where the
+    oracle stops."""
+    indiv, X, y, N, vc, lt = _ill_conditioned()
+    B = np.column_stack([X, y])
+    s = orc.Solver(indiv, X, y, N, vc, grm_lt=lt)
+    s.precond_build()
+    _, it8 = s.pcg(B, 1e-8, rule=0)
+    _, it11 = s.pcg(B, 1e-11, rule=0)
+    assert it8 == it11 < 200            # the oracle stagnates too (the tolerance plays no part)
+    with G.Context(0) as ctx:
+        ctx.load_records(indiv, X, y, N)
+        ctx.load_grm(lt, N)
+        ctx.set_vc(vc)
+        Xh, ih, _ = _solve(ctx, B, False, tol=1e-8, rule=G.RULE_PCGSOLVER)
+        Xd, idv, nd = _solve(ctx, B, True, tol=1e-8, rule=G.RULE_PCGSOLVER)
+    assert nd == 1 and ih["stagnated"] and idv["stagnated"] and not idv["converged"]
+    assert idv["iters"] == ih["iters"] and np.array_equal(Xd, Xh)
+    assert abs(idv["iters"] - it8) <= 2
