@@ -47,7 +47,7 @@ namespace tc {
 #define TC_ASTAGES 6
 #endif
 #ifndef TC_BSTAGES
-#define TC_BSTAGES 3
+#define TC_BSTAGES 4
 #endif
 #ifndef TC_DSTAGES
 #define TC_DSTAGES 2
