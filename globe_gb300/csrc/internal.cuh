@@ -115,13 +115,12 @@ struct globe_ctx {
     int model = GLOBE_MODEL_FULL; // GLOBE_MODEL_NO_TIME: components (sig2e, sig2g) only
     int digits = 9;               // base-32 digits per column of the tensor-core product (globe_set_digits)
     int stall_next_gemm = 0;      // test hook of the bounded waits (globe_debug_stall_next_gemm)
-    // autotuning of the tensor-core genotype product (k_tc_geno.cu): split-K counts per
-    // (pass, MMA width, rows, K stages) and column groupings per (columns, digits), timed on
-    // first use; 0 = the cost model only (globe_set_autotune)
+    // autotuning of the tensor-core genotype product (k_tc_geno.cu): split-K counts and column
+    // groupings, timed on first use and shared by the process's contexts; 0 = the cost model
+    // only (globe_set_autotune)
     int autotune = 1;
     int force_splits = 0;         // test hook: every tensor-core launch uses this split count
-    std::map<std::vector<int64_t>, int> tuned;
-    std::string tune_log;         // one JSON object per decision, comma separated
+    std::string tune_log;         // this context's decisions, JSON objects, comma separated
     int nvc() const { return model == GLOBE_MODEL_NO_TIME ? 2 : 5; }
     bool precond_ok = false;      // H built for the current vc
     globe::Slot ws[globe::WS_COUNT];

@@ -34,6 +34,8 @@
 // Every mbarrier wait is bounded (globaltimer); on timeout the CTA records
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <cstdarg>
 #include <cstdio>
 #include <vector>
@@ -657,7 +659,7 @@ int eff_splits(int nchunks, int splits) {
 // so the pass takes about ceil(CTAs / SMs) waves of (stages per CTA + a fixed CTA cost: setup,
 // pipeline fill and drain, epilogue).  The count minimising that estimate comes first, within
 // K per CTA <= 2^19 (exact FP32 sums) and >= 8 stages per CTA; then up to 4 more effective
-// counts whose estimate is within 25% of it (the autotuner times them).  Example: 196 row
+// counts whose estimate is within 25% of it, 3 in all (the autotuner times them).  Example: 196 row
 // blocks x 3907 stages gives 10 splits (1960 CTAs, 12.9 waves on 152 SMs) where aiming at ~8
 // waves gave 7 (1372 CTAs, 9.03 waves: a tenth wave of 4 CTAs).
 static std::vector<int> split_candidates(globe_ctx* ctx, int tiles, int nchunks) {
@@ -680,8 +682,28 @@ static std::vector<int> split_candidates(globe_ctx* ctx, int tiles, int nchunks)
                      [](const std::pair<double, int>& a, const std::pair<double, int>& b) { return a.first < b.first * 0.999; });
     std::vector<int> out;
     for (const auto& e : est)
-        if (out.size() < 5 && e.first <= est[0].first * 1.25) out.push_back(e.second);
+        if (out.size() < 3 && e.first <= est[0].first * 1.25) out.push_back(e.second);
     return out;
+}
+
+// Tuned choices shared by every context of the process, per device and shape: a shape is
+// timed once however many contexts use it.
+static std::mutex g_tune_mu;
+static std::map<std::vector<int64_t>, int> g_tuned;
+
+static bool tuned_lookup(globe_ctx* ctx, std::vector<int64_t> key, int* out) {
+    key.push_back(ctx->device);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const auto hit = g_tuned.find(key);
+    if (hit == g_tuned.end()) return false;
+    *out = hit->second;
+    return true;
+}
+
+static void tuned_store(globe_ctx* ctx, std::vector<int64_t> key, int v) {
+    key.push_back(ctx->device);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[key] = v;
 }
 
 static void tune_note(globe_ctx* ctx, const char* fmt, ...) {
@@ -695,15 +717,16 @@ static void tune_note(globe_ctx* ctx, const char* fmt, ...) {
 }
 
 // Time each of `nc` variants (run(i) issues variant i on the stream) over `rounds` rounds with
-// CUDA events on the context's stream; the last round's times go to ms[].  Returns the index
-// of the fastest, the first variant unless another is more than 1% faster.
+// CUDA events on the context's stream; the last round's times go to ms[].  Within a round the
+// variants run last to first, so a first-launch cost falls on an alternative, not on variant 0.
+// Returns the index of the fastest: variant 0 unless another is more than 1% faster.
 template <class F>
 static int time_variants(globe_ctx* ctx, int nc, int rounds, F&& run, std::vector<float>& ms, int* best) {
     std::vector<cudaEvent_t> ev(2 * nc, nullptr);
     for (auto& e : ev) GLOBE_CK(ctx, cudaEventCreate(&e));
     int rc = GLOBE_OK;
     for (int r = 0; r < rounds && rc == GLOBE_OK; ++r)
-        for (int i = 0; i < nc && rc == GLOBE_OK; ++i) {
+        for (int i = nc - 1; i >= 0 && rc == GLOBE_OK; --i) {
             cudaEventRecord(ev[2 * i], ctx->stream);
             rc = run(i);
             cudaEventRecord(ev[2 * i + 1], ctx->stream);
@@ -721,8 +744,8 @@ static int time_variants(globe_ctx* ctx, int nc, int rounds, F&& run, std::vecto
 }
 
 // The split count of one genotype pass: the test override, the tuned choice of this shape, or
-// -- on its first use, with autotuning on, outside graph capture and event profiling -- each
-// candidate launched twice and timed, the fastest kept for the context.  Every count gives the
+// -- on its first use in the process, with autotuning on, outside graph capture and event
+// profiling -- each candidate launched once and timed, the fastest kept.  Every count gives the
 // same result bits (the split partials are exact and are summed in int64), so the candidates
 // run on the real operands and the pass's own launch follows.
 static int tune_splits(globe_ctx* ctx, int pass, int nmma, const uint8_t* blk, const CUtensorMap& mB, int rows,
@@ -732,20 +755,17 @@ static int tune_splits(globe_ctx* ctx, int pass, int nmma, const uint8_t* blk, c
         return GLOBE_OK;
     }
     const std::vector<int64_t> key = {1, pass, nmma, rows, nchunks};
-    const auto hit = ctx->tuned.find(key);
-    if (hit != ctx->tuned.end()) {
-        *out = hit->second;
-        return GLOBE_OK;
-    }
     *out = cand[0];
-    if (!ctx->autotune || ctx->capturing || ctx->prof_on || cand.size() < 2) return GLOBE_OK;
+    if (!ctx->autotune || cand.size() < 2) return GLOBE_OK;
+    if (tuned_lookup(ctx, key, out)) return GLOBE_OK;
+    if (ctx->capturing || ctx->prof_on) return GLOBE_OK;
     std::vector<float> ms;
     int best = 0;
-    GLOBE_RET(time_variants(ctx, (int)cand.size(), 2, [&](int i) {
+    GLOBE_RET(time_variants(ctx, (int)cand.size(), 1, [&](int i) {
         return gemm_dispatch(ctx, nmma, blk, mB, rows, nchunks, cand[i], part, ldp, err, ZGrid());
     }, ms, &best));
     *out = cand[best];
-    ctx->tuned[key] = *out;
+    tuned_store(ctx, key, *out);
     std::string t;
     for (size_t i = 0; i < cand.size(); ++i) {
         char b[48];
@@ -883,22 +903,20 @@ int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* 
         }
         return GLOBE_OK;
     };
-    // Column grouping: the rule above, or -- for 9 or more columns, on first use of (k, digits),
-    // with autotuning on, outside capture and profiling -- the fastest of it, one group more and
-    // twice as many groups, timed over two rounds (the first also tunes the groups' split
-    // counts).  Each column's digits and sums do not depend on its group, so every grouping
+    // Column grouping: the rule above, or -- for 9 or more columns, on first use of (k, digits,
+    // N, SNPs), with autotuning on, outside capture and profiling -- the faster of it and one
+    // group more, timed over two rounds (the first also tunes the groups' split counts).  Each column's digits and sums do not depend on its group, so every grouping
     // gives the same bits and the last run's output stands.
-    const std::vector<int64_t> key = {2, k, nd};
-    const auto hit = ctx->tuned.find(key);
-    if (hit != ctx->tuned.end()) return run(hit->second);
-    if (!ctx->autotune || ctx->capturing || ctx->prof_on || ctx->force_splits > 0 || k < 9) return run(ng);
-    std::vector<int> cand = {ng};
-    for (int alt : {ng + 1, 2 * ng})
-        if (alt <= k && std::find(cand.begin(), cand.end(), alt) == cand.end()) cand.push_back(alt);
+    const std::vector<int64_t> key = {2, k, nd, N, (int64_t)g.Mk};
+    if (!ctx->autotune || ctx->force_splits > 0 || k < 9) return run(ng);
+    int chosen = ng;
+    if (tuned_lookup(ctx, key, &chosen)) return run(chosen);
+    if (ctx->capturing || ctx->prof_on || ng + 1 > k) return run(ng);
+    const std::vector<int> cand = {ng, ng + 1};
     std::vector<float> ms;
     int best = 0;
     GLOBE_RET(time_variants(ctx, (int)cand.size(), 2, [&](int i) { return run(cand[i]); }, ms, &best));
-    ctx->tuned[key] = cand[best];
+    tuned_store(ctx, key, cand[best]);
     std::string t;
     for (size_t i = 0; i < cand.size(); ++i) {
         char b[48];

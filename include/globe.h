@@ -248,22 +248,23 @@ int globe_get_device_loop(const globe_ctx* ctx);
 int64_t globe_device_loop_runs(const globe_ctx* ctx);
 
 /* Autotuning of the tensor-core genotype product (on = 1, the default; 0 =
- * the analytic choices only).  On first use of a shape in a context -- outside
- * graph capture and event profiling -- the product times its candidates with
- * CUDA events on the context's stream and keeps the fastest:
+ * the analytic choices only).  On first use of a shape in the process --
+ * outside graph capture and event profiling -- the product times its
+ * candidates with CUDA events on the context's stream and keeps the fastest
+ * for every context on that device:
  *  - the split-K count of each pass (per MMA width, rows and K stages): the
- *    wave-quantisation cost model's count and up to 4 more within 25% of its
- *    estimate, two launches each;
+ *    wave-quantisation cost model's count and up to 2 more within 25% of its
+ *    estimate, one launch each;
  *  - for 9 or more right-hand-side columns, the column grouping (per column
- *    count and digit count): the rule's group count, one more and twice as
- *    many, two rounds each.
+ *    count, digit count and genotype shape): the rule's group count and one
+ *    more, two rounds each.
  * Every candidate gives the same result bits (exact sums in any split or
- * group), so the choice changes speed only.  globe_autotune_log writes the
- * decisions as a JSON array into buf (cap bytes, NUL-terminated, truncated if
- * short) and returns the full length.  globe_debug_force_splits(ctx, s), s > 0,
- * makes every tensor-core genotype pass use s splits (a test hook; 0 = off).
- * The reference hard-codes its SNP chunk instead (SNP_CHUNK_SIZE,
- * PCGsolver.cpp:1135). */
+ * group), so the choice changes speed only.  globe_autotune_log writes this
+ * context's timing decisions as a JSON array into buf (cap bytes,
+ * NUL-terminated, truncated if short) and returns the full length.
+ * globe_debug_force_splits(ctx, s), s > 0, makes every tensor-core genotype
+ * pass use s splits (a test hook; 0 = off).  The reference hard-codes its SNP
+ * chunk instead (SNP_CHUNK_SIZE, PCGsolver.cpp:1135). */
 int globe_set_autotune(globe_ctx* ctx, int on);
 int globe_get_autotune(const globe_ctx* ctx);
 int64_t globe_autotune_log(const globe_ctx* ctx, char* buf, int64_t cap);
