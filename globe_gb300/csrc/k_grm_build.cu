@@ -377,7 +377,7 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
         zg.skipz = GRM_KG;
         {
             ProfScope p(ctx, GLOBE_PROF_GRM_BUILD_GEMM);
-            GLOBE_RET(gemm_dispatch(ctx, GRM_NMMA, g.blk2, mB, N, nch, splits, P, ldp, err, zg));
+            GLOBE_RET(gemm_dispatch(ctx, GRM_NMMA, g.blk2, g.ntiles2, mB, N, nch, splits, P, ldp, err, zg));
         }
         k_grm_combine<<<dim3((unsigned)div_up(N - jb, 32), (unsigned)gb), 256, 0, ctx->stream>>>(
             P, spe, ldp, pz, N, jb, C2, info, 1.0 / (double)g.Mk, lt);

@@ -69,7 +69,13 @@ constexpr int DSTAGES = TC_DSTAGES;  // decoded-A ring
 // Row tiles per CTA (one MMA-issuing warp each): an M=128, K=32 MMA occupies
 // its issuing context ~157 cycles whatever N is, so small-N products need
 // several concurrent issue streams to use the tensor pipe; TMEM (512
-// columns) bounds MT * NMMA + DSTAGES * MT * 32.
+// columns) bounds MT * NMMA + DSTAGES * MT * 32.  At k = 5 a stage takes ~1000
+// cycles: copies without the TMEM stores or without the MMAs run 12% / 16%
+// faster, but a deeper decoded-A ring (3 tiles, 3 slots; or 4 slots at width
+// 128) does not help, and the stage time stays ~1000 cycles with 3 tiles per CTA
+// as with 4 -- the stores and the MMAs' TMEM reads of A share what bounds it.
+// Moving one or two tiles' decoded A to shared memory (MMA from two descriptors)
+// is slower still (+10%, +30%): shared memory is the tighter of the two.
 // Decoders: two sets of 8 warps take the stages in turn (set = stage parity, so
 // each set owns one slot of the decoded-A ring) -- one set's load / TMEM-store
 // latency overlaps the other set's decode.  Within a set, warp (quadrant q, j)
@@ -560,8 +566,8 @@ static int blockify(globe_ctx* ctx, const uint8_t* src, int64_t nrows, int64_t s
                     int* ntiles) {
     *nch = (int)((stride + PKB - 1) / PKB);
     *ntiles = (int)((nrows + BM - 1) / BM);
-    // whole CTAs: round the tile count up to a multiple of 4 (a CTA may own four tiles)
-    *ntiles = (*ntiles + 3) / 4 * 4;
+    // whole CTAs: round the tile count up to a multiple of TILE_PAD (a CTA owns 1 to 4 tiles)
+    *ntiles = (*ntiles + TILE_PAD - 1) / TILE_PAD * TILE_PAD;
     GLOBE_RET(dalloc(ctx, dst, (size_t)(*ntiles) * (*nch) * BM * PKB));
     const int64_t total = (int64_t)(*ntiles) * (*nch) * (BM * PKB / 16);
     k_blockify<<<(unsigned)std::min<int64_t>((total + 255) / 256, 65535), 256, 0, ctx->stream>>>(
@@ -594,7 +600,7 @@ int ensure_blk2(globe_ctx* ctx) {
     if (g.strideT < PKB) g.strideT = PKB;
     g.nch2 = (int)(g.strideT / PKB);
     g.ntiles2 = (int)((N + BM - 1) / BM);
-    g.ntiles2 = (g.ntiles2 + 3) / 4 * 4;   // whole CTAs of four tiles
+    g.ntiles2 = (g.ntiles2 + TILE_PAD - 1) / TILE_PAD * TILE_PAD;   // whole CTAs of 1 to 4 tiles
     GLOBE_RET(dalloc(ctx, &g.blk2, (size_t)g.ntiles2 * g.nch2 * BM * PKB));
     const int64_t nblk = (int64_t)g.ntiles2 * g.nch2;
     k_blk_transpose<<<(unsigned)std::min<int64_t>(nblk, 152 * 16), 256, 0, ctx->stream>>>(g.blk1, g.nch1, g.ntiles1,
@@ -605,9 +611,14 @@ int ensure_blk2(globe_ctx* ctx) {
 }
 
 template <int NMMA>
-static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB, int rows, int nchunks, int splits,
-                       float* part, int64_t ldp, unsigned* err, const ZGrid& zg) {
+static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, int ntiles, const CUtensorMap& mB, int rows, int nchunks,
+                       int splits, float* part, int64_t ldp, unsigned* err, const ZGrid& zg) {
     using G = Geo<NMMA>;
+    // every CTA bulk-copies all G::MT of its row tiles: the last one must lie inside blk
+    const int64_t ctas_x = (rows + G::MT * BM - 1) / (G::MT * BM);
+    if (ctas_x * G::MT > ntiles)
+        return set_err(ctx, GLOBE_ERR_ARG, "k_tc_gemm: %lld CTAs of %d row tiles need %lld tiles; the copy holds %d",
+                       (long long)ctas_x, G::MT, (long long)(ctas_x * G::MT), ntiles);
     const int cps = (nchunks + splits - 1) / splits;
     splits = (nchunks + cps - 1) / cps;
     const size_t smem = sizeof(Smem<NMMA, G::MT>) + 1024;
@@ -627,25 +638,25 @@ static int launch_gemm(globe_ctx* ctx, const uint8_t* blk, const CUtensorMap& mB
 
 int rows_per_cta(int nmma) { return BM * (nmma <= 64 ? 4 : (nmma <= 192 ? 2 : 1)); }
 
-int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* mA, const CUtensorMap& mB, int rows, int nchunks,
+int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* mA, int ntiles, const CUtensorMap& mB, int rows, int nchunks,
                   int splits, float* part, int64_t ldp, unsigned* err, const ZGrid& zg) {
     switch (nmma) {
-        case 16: return launch_gemm<16>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 32: return launch_gemm<32>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 48: return launch_gemm<48>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 64: return launch_gemm<64>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 80: return launch_gemm<80>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 96: return launch_gemm<96>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 112: return launch_gemm<112>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 128: return launch_gemm<128>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 144: return launch_gemm<144>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 160: return launch_gemm<160>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 176: return launch_gemm<176>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 192: return launch_gemm<192>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 208: return launch_gemm<208>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 224: return launch_gemm<224>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 240: return launch_gemm<240>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
-        case 256: return launch_gemm<256>(ctx, mA, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 16: return launch_gemm<16>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 32: return launch_gemm<32>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 48: return launch_gemm<48>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 64: return launch_gemm<64>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 80: return launch_gemm<80>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 96: return launch_gemm<96>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 112: return launch_gemm<112>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 128: return launch_gemm<128>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 144: return launch_gemm<144>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 160: return launch_gemm<160>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 176: return launch_gemm<176>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 192: return launch_gemm<192>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 208: return launch_gemm<208>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 224: return launch_gemm<224>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 240: return launch_gemm<240>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
+        case 256: return launch_gemm<256>(ctx, mA, ntiles, mB, rows, nchunks, splits, part, ldp, err, zg);
     }
     return set_err(ctx, GLOBE_ERR_ARG, "unsupported MMA width %d", nmma);
 }
@@ -748,8 +759,9 @@ static int time_variants(globe_ctx* ctx, int nc, int rounds, F&& run, std::vecto
 // profiling -- each candidate launched once and timed, the fastest kept.  Every count gives the
 // same result bits (the split partials are exact and are summed in int64), so the candidates
 // run on the real operands and the pass's own launch follows.
-static int tune_splits(globe_ctx* ctx, int pass, int nmma, const uint8_t* blk, const CUtensorMap& mB, int rows,
-                       int nchunks, const std::vector<int>& cand, float* part, int64_t ldp, unsigned* err, int* out) {
+static int tune_splits(globe_ctx* ctx, int pass, int nmma, const uint8_t* blk, int ntiles, const CUtensorMap& mB,
+                       int rows, int nchunks, const std::vector<int>& cand, float* part, int64_t ldp, unsigned* err,
+                       int* out) {
     if (ctx->force_splits > 0) {   // at least the count that keeps K per CTA <= 2^19
         *out = std::max(ctx->force_splits, (nchunks + 4095) / 4096);
         return GLOBE_OK;
@@ -762,7 +774,7 @@ static int tune_splits(globe_ctx* ctx, int pass, int nmma, const uint8_t* blk, c
     std::vector<float> ms;
     int best = 0;
     GLOBE_RET(time_variants(ctx, (int)cand.size(), 1, [&](int i) {
-        return gemm_dispatch(ctx, nmma, blk, mB, rows, nchunks, cand[i], part, ldp, err, ZGrid());
+        return gemm_dispatch(ctx, nmma, blk, ntiles, mB, rows, nchunks, cand[i], part, ldp, err, ZGrid());
     }, ms, &best));
     *out = cand[best];
     tuned_store(ctx, key, *out);
@@ -832,13 +844,13 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     GLOBE_LAUNCHED(ctx, "k_digits");
     // ---- pass 1
     int sp1 = 0;
-    GLOBE_RET(tune_splits(ctx, 1, nmma, g.blk1, mB1, (int)g.Mk, nch1, cand1, P1, ldp1, err, &sp1));
+    GLOBE_RET(tune_splits(ctx, 1, nmma, g.blk1, g.ntiles1, mB1, (int)g.Mk, nch1, cand1, P1, ldp1, err, &sp1));
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS1);
         ZGrid zg;
         zg.stall = ctx->stall_next_gemm;
         ctx->stall_next_gemm = 0;
-        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, zg));
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, g.ntiles1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, zg));
     }
     const int sp1e = eff_splits(nch1, sp1);
     k_combine1<ND><<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
@@ -853,10 +865,10 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
         U, g.Mk, g.Mk, kg, col2, D2, kpad2);
     GLOBE_LAUNCHED(ctx, "k_digits");
     int sp2 = 0;
-    GLOBE_RET(tune_splits(ctx, 2, nmma, g.blk2, mB2, N, nch2, cand2, P2, ldp2, err, &sp2));
+    GLOBE_RET(tune_splits(ctx, 2, nmma, g.blk2, g.ntiles2, mB2, N, nch2, cand2, P2, ldp2, err, &sp2));
     {
         ProfScope p(ctx, GLOBE_PROF_GRM_PASS2);
-        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, mB2, N, nch2, sp2, P2, ldp2, err, ZGrid()));
+        GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk2, g.ntiles2, mB2, N, nch2, sp2, P2, ldp2, err, ZGrid()));
     }
     const int sp2e = eff_splits(nch2, sp2);
     k_combine2<ND><<<dim3(div_up(N, 256) < 1024 ? div_up(N, 256) : 1024, kg), 256, 0, ctx->stream>>>(

@@ -190,7 +190,11 @@ struct ZGrid {
 
 int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t box_in,
              uint32_t box_out, bool sw128);
-int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* blk, const CUtensorMap& mB, int rows, int nchunks,
+// Tile-blocked genotype copies hold a multiple of TILE_PAD row tiles of 128, so that CTAs of
+// 1, 2, 3 or 4 tiles never run past them; gemm_dispatch checks it for each launch (ntiles:
+// the row tiles of blk).
+constexpr int TILE_PAD = 12;
+int gemm_dispatch(globe_ctx* ctx, int nmma, const uint8_t* blk, int ntiles, const CUtensorMap& mB, int rows, int nchunks,
                   int splits, float* part, int64_t ldp, unsigned* err, const ZGrid& zg);
 int rows_per_cta(int nmma);
 int eff_splits(int nchunks, int splits);
