@@ -86,6 +86,7 @@ SIGNATURES = {
     "globe_get_autotune": (C.c_int, [_vp]),
     "globe_autotune_log": (C.c_int64, [_vp, C.c_char_p, C.c_int64]),
     "globe_debug_force_splits": (C.c_int, [_vp, C.c_int]),
+    "globe_debug_bounds": (C.c_int, [C.POINTER(C.c_uint32)]),
     "globe_grm_build": (C.c_int, [_vp, _fp]),
     "globe_grm_build_dev": (C.c_int, [_vp, _vp]),
     "globe_write_grm": (C.c_int, [C.c_char_p, _fp, C.c_int32, C.c_char_p, C.c_int]),

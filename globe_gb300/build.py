@@ -2,7 +2,9 @@
 
 nvcc compiles every translation unit for sm_103a only (one -gencode), in
 parallel, into ``globe_gb300/_build``; the shared library lands in
-``globe_gb300/`` and the command-line programs in ``globe_gb300/bin``.
+``globe_gb300/`` and the command-line programs in ``globe_gb300/bin``.  The
+bounds-checked debug library (``libglobe_gb300_bounds.so``, -DGLOBE_CHECK_BOUNDS)
+is built beside it from the same sources.
 """
 import glob
 import os
@@ -17,9 +19,20 @@ SRC = os.path.join(HERE, "csrc")
 # depths) next to the default one: lib<tag>.so, objects in _build_<tag>.
 TAG = os.environ.get("GLOBE_BUILD_TAG", "")
 EXTRA = os.environ.get("GLOBE_NVCC_FLAGS", "").split()
-BUILD = os.path.join(HERE, "_build" + ("_" + TAG if TAG else ""))
 BIN = os.path.join(HERE, "bin")
-LIB = os.path.join(HERE, "libglobe_gb300%s.so" % ("_" + TAG if TAG else ""))
+# variants build() also makes: the bounds-checked debug library (globe_debug_bounds)
+VARIANTS = {"bounds": ["-DGLOBE_CHECK_BOUNDS"]}
+
+
+def lib_path(tag=TAG):
+    return os.path.join(HERE, "libglobe_gb300%s.so" % ("_" + tag if tag else ""))
+
+
+def _build_dir(tag):
+    return os.path.join(HERE, "_build" + ("_" + tag if tag else ""))
+
+
+LIB = lib_path()
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", os.path.join(ROOT, "include"), "-I", SRC,
@@ -44,11 +57,11 @@ def _headers():
         [os.path.join(ROOT, "include", "globe.h")]
 
 
-def _compile(src):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src, build_dir, extra):
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     if not _newer(obj, [src] + _headers()):
         return obj
-    cmd = [NVCC] + COMMON + EXTRA + (ARCH if src.endswith(".cu") else []) + ["-c", src, "-o", obj]
+    cmd = [NVCC] + COMMON + extra + (ARCH if src.endswith(".cu") else []) + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-6000:]))
@@ -57,25 +70,37 @@ def _compile(src):
     return obj
 
 
-def build(verbose=True):
-    os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(BIN, exist_ok=True)
+def _build_lib(tag, extra, workers):
+    build_dir, lib = _build_dir(tag), lib_path(tag)
+    os.makedirs(build_dir, exist_ok=True)
     srcs = [os.path.join(SRC, s) for s in LIB_SOURCES]
-    with ThreadPoolExecutor(max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(_compile, srcs))
-    if _newer(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+    with ThreadPoolExecutor(workers) as ex:
+        objs = list(ex.map(lambda f: _compile(f, build_dir, extra), srcs))
+    if _newer(lib, objs):
+        cmd = [NVCC] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
         subprocess.check_call(cmd)
+    return lib
+
+
+def build(verbose=True, variants=True):
+    """The library (and, with no GLOBE_BUILD_TAG, the programs and the VARIANTS libraries)."""
+    os.makedirs(BIN, exist_ok=True)
+    workers = max(1, min(2 * len(LIB_SOURCES), os.cpu_count() or 4))
+    jobs = [(TAG, EXTRA)] + ([(t, f) for t, f in VARIANTS.items()] if variants and not TAG else [])
+    with ThreadPoolExecutor(len(jobs)) as ex:
+        libs = list(ex.map(lambda j: _build_lib(j[0], j[1], workers), jobs))
+    lib = libs[0]
     for name, (src, flags) in (CLI.items() if not TAG else []):
         s = os.path.join(SRC, src)
         exe = os.path.join(BIN, name)
-        if os.path.exists(s) and _newer(exe, [s, LIB] + _headers()):
+        if os.path.exists(s) and _newer(exe, [s, lib] + _headers()):
             cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include")] + flags + [s, "-o", exe,
                    "-L", HERE, "-lglobe_gb300", "-Wl,-rpath,$ORIGIN/.."]
             subprocess.check_call(cmd)
     if verbose:
-        print("built", LIB)
-    return LIB
+        for l in libs:
+            print("built", l)
+    return lib
 
 
 if __name__ == "__main__":

@@ -145,6 +145,28 @@ static void free_genetic(globe_ctx* ctx) {
     ctx->mme_ok = ctx->fth_ok = false;
 }
 
+// registry of the bounds-check words (one per translation unit of a checked build)
+static std::vector<int (*)(unsigned*, bool)>& bounds_queries() {
+    static std::vector<int (*)(unsigned*, bool)> q;
+    return q;
+}
+int register_bounds_word(int (*query)(unsigned* code, bool clear)) {
+    bounds_queries().push_back(query);
+    return (int)bounds_queries().size();
+}
+int query_bounds_words(unsigned* first_code) {
+    int found = 0;
+    for (auto q : bounds_queries()) {
+        unsigned c = 0;
+        if (q(&c, true) != 0) return -1;
+        if (c != 0 && !found) {
+            *first_code = c;
+            found = 1;
+        }
+    }
+    return found;
+}
+
 }  // namespace globe
 
 using namespace globe;
@@ -222,6 +244,7 @@ int globe_get_device_loop(const globe_ctx* ctx) { return ctx ? ctx->device_loop 
 
 int64_t globe_device_loop_runs(const globe_ctx* ctx) { return ctx ? ctx->device_loop_runs : -1; }
 
+
 int globe_set_autotune(globe_ctx* ctx, int on) {
     if (!ctx) return GLOBE_ERR_ARG;
     if (on != 0 && on != 1) return set_err(ctx, GLOBE_ERR_ARG, "globe_set_autotune: on must be 0 or 1, got %d", on);
@@ -240,6 +263,19 @@ int64_t globe_autotune_log(const globe_ctx* ctx, char* buf, int64_t cap) {
         buf[n] = 0;
     }
     return (int64_t)s.size();
+}
+
+int globe_debug_bounds(uint32_t* first_code) {
+#ifdef GLOBE_CHECK_BOUNDS
+    unsigned c = 0;
+    const int r = globe::query_bounds_words(&c);
+    if (r < 0) return GLOBE_ERR_CUDA;
+    if (first_code) *first_code = r ? c : 0u;
+    return r;
+#else
+    if (first_code) *first_code = 0u;
+    return GLOBE_ERR_UNSUPPORTED;
+#endif
 }
 
 int globe_debug_force_splits(globe_ctx* ctx, int splits) {

@@ -219,6 +219,33 @@ struct ProfScope {
     ~ProfScope() { prof_end(c, h); }
 };
 
+// ---- bounds-checked debug build -------------------------------------------------
+// Built with -DGLOBE_CHECK_BOUNDS (e.g. GLOBE_BUILD_TAG=bounds GLOBE_NVCC_FLAGS=
+// -DGLOBE_CHECK_BOUNDS), the kernels check the indices they take from data (record
+// ranges, individual indices) before using them.  A failed check records its code in a
+// device word of its translation unit (the first one wins) and the access is skipped;
+// nothing traps.  globe_debug_bounds reads and clears the words.  Without the macro
+// GLOBE_BOUNDS(cond, code) is the constant true and the checks compile away.
+int register_bounds_word(int (*query)(unsigned* code, bool clear));
+int query_bounds_words(unsigned* first_code);   // 0: none failed, 1: a code, < 0: error
+#if defined(GLOBE_CHECK_BOUNDS) && defined(__CUDACC__)
+static __device__ unsigned g_bounds_code = 0u;   // one per translation unit
+__device__ __forceinline__ bool bounds_ok(bool ok, unsigned code) {
+    if (!ok) atomicCAS(&g_bounds_code, 0u, code);
+    return ok;
+}
+static int query_bounds_word_tu(unsigned* code, bool clear) {
+    if (cudaMemcpyFromSymbol(code, g_bounds_code, sizeof(unsigned)) != cudaSuccess) return -1;
+    const unsigned zero = 0u;
+    if (clear && cudaMemcpyToSymbol(g_bounds_code, &zero, sizeof(unsigned)) != cudaSuccess) return -1;
+    return 0;
+}
+static const int g_bounds_registered = register_bounds_word(&query_bounds_word_tu);
+#define GLOBE_BOUNDS(cond, code) ::globe::bounds_ok((cond), (code))
+#else
+#define GLOBE_BOUNDS(cond, code) true
+#endif
+
 // ---- kernels entry points (defined in the k_*.cu files) ----
 
 // k_bed.cu

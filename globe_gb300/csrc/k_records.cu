@@ -97,6 +97,7 @@ __global__ void k_block_moments(const int32_t* __restrict__ bstart, const double
     const int b = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
     if (b >= nblk) return;
     const int st = bstart[b], en = bstart[b + 1];
+    if (!GLOBE_BOUNDS(st >= 0 && st <= en, 0x0901u)) return;
     double s1 = 0, s2 = 0;
     for (int r = st + lane; r < en; r += 32) {
         double tr = t[r];
@@ -126,6 +127,7 @@ __global__ void k_build_H(int32_t nblk, const double* __restrict__ bn, const dou
                           const double* __restrict__ gdiag, double gconst, VC v, double* __restrict__ H) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nblk) return;
+    if (gdiag && !GLOBE_BOUNDS(bind[b] >= 0 && bind[b] < nblk, 0x0A01u)) return;
     double g = gdiag ? v.g * gdiag[bind[b]] : gconst;
     double c00 = v.b0 + g, c01 = v.b01, c11 = v.b1;
     double g00 = bn[b], g01 = bt[b], g11 = btt[b];
@@ -163,6 +165,7 @@ __global__ void k_seg_sums(int32_t nblk, int64_t ld, int32_t N, const int32_t* _
     const int b = bl ? bl[idx] : idx;
     const int st = bstart[b], en = bstart[b + 1];
     const int i = bind[b];
+    if (!GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld && i >= 0 && i < N, 0x0101u)) return;
     for (int c = 0; c < kact; ++c) {
         const int col = cols ? cols[c] : c;
         double* xc = x + (size_t)col * ld;
@@ -202,6 +205,7 @@ __global__ void k_seg_sums_t(int32_t nblk, int64_t ld, int32_t N, const int32_t*
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     const int st = bstart[b], en = bstart[b + 1];
+    if (!GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld && bind[b] >= 0 && bind[b] < N, 0x0201u)) return;
     if (en - st > SHORT_BLOCK) return;   // a warp per long block handles it
     double* xc = x + (size_t)col * ld;
     double s0 = 0, s1 = 0;
@@ -261,6 +265,7 @@ __global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t
     const int b = live ? (bl ? bl[idx] : idx) : 0;
     int st = 0, en = 0, i = 0;
     if (live) { st = bstart[b]; en = bstart[b + 1]; i = bind[b]; }
+    if (live && !GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld && i >= 0 && i < N, 0x0301u)) st = en = i = 0;
     for (int c = 0; c < kact; ++c) {
         const int col = cols ? cols[c] : c;
         double dot = 0;
@@ -296,7 +301,8 @@ __global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     double dot[1] = {0.0};
-    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK) {   // long blocks: a warp each
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK &&   // long blocks: a warp each
+        GLOBE_BOUNDS(bstart[b] >= 0 && bstart[b + 1] <= ld && bind[b] >= 0 && bind[b] < N, 0x0401u)) {
         const int st = bstart[b], en = bstart[b + 1], i = bind[b];
         const double s0 = Zi[i + (size_t)c * N], s1 = S1[i + (size_t)c * N];
         const double g = GZ ? GZ[i + (size_t)c * N] : 0.0;
@@ -362,6 +368,7 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
         h01 = H[4 * b + 1];
         h10 = H[4 * b + 2];
         h11 = H[4 * b + 3];
+        if (!GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld, 0x0501u)) st = en = 0;
     }
     for (int c = 0; c < kact; ++c) {
         const int col = cols ? cols[c] : c;
@@ -413,7 +420,8 @@ __global__ void k_pcg_update_t(int32_t nblk, int64_t ld, const int32_t* __restri
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     double acc[2] = {0.0, 0.0};   // |r|^2, r'z
-    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK) {
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK &&
+        GLOBE_BOUNDS(bstart[b] >= 0 && bstart[b + 1] <= ld, 0x0601u)) {
         const int st = bstart[b], en = bstart[b + 1];
         const double a = alpha[col];
         double* xc = x + (size_t)col * ld;
@@ -487,6 +495,7 @@ __global__ void k_precond_apply(int32_t nblk, int64_t ld, const int32_t* __restr
         h01 = H[4 * b + 1];
         h10 = H[4 * b + 2];
         h11 = H[4 * b + 3];
+        if (!GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld, 0x0701u)) st = en = 0;
     }
     for (int c = 0; c < kact; ++c) {
         const int col = cols ? cols[c] : c;
@@ -525,7 +534,8 @@ __global__ void k_precond_apply_t(int32_t nblk, int64_t ld, const int32_t* __res
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
     double rz[1] = {0.0};
-    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK) {
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK &&
+        GLOBE_BOUNDS(bstart[b] >= 0 && bstart[b + 1] <= ld, 0x0801u)) {
         const int st = bstart[b], en = bstart[b + 1];
         const double* rc = r + (size_t)col * ld;
         double s0 = 0, s1 = 0;

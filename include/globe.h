@@ -270,6 +270,15 @@ int globe_get_autotune(const globe_ctx* ctx);
 int64_t globe_autotune_log(const globe_ctx* ctx, char* buf, int64_t cap);
 int globe_debug_force_splits(globe_ctx* ctx, int splits);
 
+/* Bounds-checked debug build (the library compiled with -DGLOBE_CHECK_BOUNDS):
+ * the kernels check the indices they take from data -- each block of records
+ * inside [0, Nrec), each individual inside [0, N) -- and a failed check skips
+ * its access and records a code (kernel << 8 | check).  Returns 0 if no check
+ * failed since the last call, 1 if one did (first_code: its code), and clears;
+ * GLOBE_ERR_UNSUPPORTED in a library built without the checks.  No reference
+ * counterpart. */
+int globe_debug_bounds(uint32_t* first_code);
+
 /* Test hook for the tensor-core kernels' bounded waits: the next tensor-core
  * GRM product's first launch (genotype or dense) leaves its first stage
  * unloaded.  The MMA issuer's wait for it runs out after ~2 s, the CTA raises
