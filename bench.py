@@ -345,8 +345,10 @@ def headline_parity(G, ctx, theta, numMC, seed, X, y, tol=1e-5):
 
     evaluation: one AIREML gradient evaluation in each precision with the same probes and
     fresh solves as runAIREML makes them (fitMME from x0 = Q^-1 b, the probe solves, the AI
-    solve; PCG tolerance 1e-5).  Both take the same iterations; rounding separates their
-    Krylov paths by far less than the tolerance.  From each, the Newton step p = AI^-1 g:
+    solve; PCG tolerance 1e-5).  Rounding separates the two Krylov paths; where the solves
+    are ill-conditioned they may stop an iteration or two apart, each within the
+    tolerance, and the gradients then differ at the level the tolerance allows.  From
+    each, the Newton step p = AI^-1 g:
     the FP64 step's distance from the mixed one, relative to theta, is how far one FP64
     iteration from theta lands from the mixed iteration; the FP64 step's own size is how
     far theta is from the FP64 fixed point for these probes (Monte-Carlo noise at numMC)."""
