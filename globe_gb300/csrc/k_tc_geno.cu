@@ -58,7 +58,8 @@ namespace tc {
 #define TC_DEC_PRE 8     // 16-byte units a decoder warp decodes before it waits for its TMEM slot
 #endif
 #ifndef TC_STW
-#define TC_STW 16        // columns per tcgen05.st of a decoded unit (16, or 8 in two stores)
+#define TC_STW 16        // columns per tcgen05.st: 16 (a unit), 8 (a unit in two), 32 (a tile row's two
+                         // units; 1% slower at k = 5)
 #endif
 #ifndef TC_SLEEP_DEC
 #define TC_SLEEP_DEC 1   // decoders suspend in their waits too
@@ -296,7 +297,12 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
                     decode_word(v[i].z, o[i][8], o[i][9], o[i][10], o[i][11]);
                     decode_word(v[i].w, o[i][12], o[i][13], o[i][14], o[i][15]);
                 }
-                tmem_st_unit(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[i]);
+                if (TC_STW == 32 && G::UPW % 2 == 0) {
+                    // units i, i+1 are the two halves of one tile's row: one 32-column store
+                    if (h == 1) tmem_st32(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32), o[i - 1], o[i]);
+                } else {
+                    tmem_st_unit(tmem + lane_addr + (uint32_t)(ACOL0 + (ds * MT + m) * 32 + h * 16), o[i]);
+                }
             }
             tmem_wait_st();
             tc_before();
