@@ -470,6 +470,8 @@ def run_ours(args, cfg):
     torch.cuda.set_device(device)
     prec = G.PREC_MIXED if args.precision == "mixed" else G.PREC_FP64
     ctx = G.Context(device)
+    if args.no_autotune:
+        ctx.set_autotune(False)
     indiv, X, y, N = make_records(cfg, iid_genetic=False)
     Nrec = len(indiv)
     bps = (N + 3) // 4
@@ -715,6 +717,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the in-run FP64-plain comparison")
     ap.add_argument("--no-aireml", action="store_true", help="skip the AIREML time-to-converge runs")
     ap.add_argument("--no-grm-build", action="store_true", help="skip the GRM build (N=20k, M=50k) measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="the cost model's split counts and groupings only (profiling captures a fixed launch sequence)")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the mixed-vs-FP64 evaluation at the AIREML estimate on this workload")
     args = ap.parse_args()
