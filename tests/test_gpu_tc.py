@@ -36,7 +36,8 @@ def test_grm_apply_tc_matches_fp64(gctx, orc, name, spec):
     rng = np.random.default_rng(N)
     try:
         gctx.set_precision(G.PREC_MIXED)
-        for k in (1, 4, 5, 9, 22, 30):   # widths 16..256 and a two-group split (30 -> 15 + 15)
+        for k in (1, 4, 5, 9, 22, 30, 65):   # widths 16..256, a two-group split (30 -> 15 + 15), and the
+                                             # 65-column batching shape (17 + 16 + 16 + 16)
             Z = rng.standard_normal((N, k)) * np.logspace(-3, 2, k)
             got, ref = gctx.grm_apply(Z), s.grm_apply(Z)
             assert max(rel(got[:, c], ref[:, c]) for c in range(k)) < 1e-11, k
