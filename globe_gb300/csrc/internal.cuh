@@ -120,6 +120,10 @@ struct globe_ctx {
     // only (globe_set_autotune)
     int autotune = 1;
     int force_splits = 0;         // test hook: every tensor-core launch uses this split count
+    // host-side results that repeat every product of a shape: split-K candidates per
+    // (row blocks, K stages) and encoded tensor maps per (base, sizes, box, swizzle)
+    std::map<std::pair<int, int>, std::vector<int>> split_cache;
+    std::map<std::vector<uint64_t>, std::vector<uint8_t>> map_cache;
     std::string tune_log;         // this context's decisions, JSON objects, comma separated
     int nvc() const { return model == GLOBE_MODEL_NO_TIME ? 2 : 5; }
     bool precond_ok = false;      // H built for the current vc

@@ -34,6 +34,7 @@
 // Every mbarrier wait is bounded (globaltimer); on timeout the CTA records
 // an error bit, waits (bounded) for its issued copies / MMAs and frees TMEM.
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <cstdarg>
@@ -540,6 +541,9 @@ __global__ void k_blockify(const uint8_t* __restrict__ src, int64_t nrows, int64
 
 using namespace tc;
 
+static int encode_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer,
+                      uint32_t box_in, uint32_t box_out, bool sw128);
+
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -555,6 +559,21 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 int make_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint32_t box_in,
                     uint32_t box_out, bool sw128) {
+    // a map depends only on these values: reuse the encoding of an earlier call
+    const std::vector<uint64_t> key = {(uint64_t)(uintptr_t)base, inner, outer, box_in, box_out, sw128 ? 1u : 0u};
+    const auto hit = ctx->map_cache.find(key);
+    if (hit != ctx->map_cache.end()) {
+        std::memcpy(m, hit->second.data(), sizeof(CUtensorMap));
+        return GLOBE_OK;
+    }
+    GLOBE_RET(encode_map(ctx, m, base, inner, outer, box_in, box_out, sw128));
+    if (ctx->map_cache.size() > 256) ctx->map_cache.clear();
+    ctx->map_cache[key].assign(reinterpret_cast<const uint8_t*>(m), reinterpret_cast<const uint8_t*>(m) + sizeof(CUtensorMap));
+    return GLOBE_OK;
+}
+
+static int encode_map(globe_ctx* ctx, CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer,
+                      uint32_t box_in, uint32_t box_out, bool sw128) {
     auto fn = encode_fn();
     if (!fn) return set_err(ctx, GLOBE_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {inner, outer};
@@ -679,7 +698,13 @@ int eff_splits(int nchunks, int splits) {
 // counts whose estimate is within 25% of it, 3 in all (the autotuner times them).  Example: 196 row
 // blocks x 3907 stages gives 10 splits (1960 CTAs, 12.9 waves on 152 SMs) where aiming at ~8
 // waves gave 7 (1372 CTAs, 9.03 waves: a tenth wave of 4 CTAs).
-static std::vector<int> split_candidates(globe_ctx* ctx, int tiles, int nchunks) {
+static std::vector<int> split_candidates_model(globe_ctx* ctx, int tiles, int nchunks);
+static const std::vector<int>& split_candidates(globe_ctx* ctx, int tiles, int nchunks) {
+    auto& v = ctx->split_cache[{tiles, nchunks}];
+    if (v.empty()) v = split_candidates_model(ctx, tiles, nchunks);
+    return v;
+}
+static std::vector<int> split_candidates_model(globe_ctx* ctx, int tiles, int nchunks) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || sms < 1) sms = 152;
     constexpr int CTA_COST = 8;                       // fixed cost of a CTA, in stages
@@ -808,7 +833,8 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     const int64_t kpad2 = (int64_t)nch2 * BK;
     const int rpc = rows_per_cta(nmma);
     const int tiles1 = (int)((g.Mk + rpc - 1) / rpc), tiles2 = (N + rpc - 1) / rpc;
-    const std::vector<int> cand1 = split_candidates(ctx, tiles1, nch1), cand2 = split_candidates(ctx, tiles2, nch2);
+    const std::vector<int>& cand1 = split_candidates(ctx, tiles1, nch1);
+    const std::vector<int>& cand2 = split_candidates(ctx, tiles2, nch2);
     auto most = [&](const std::vector<int>& c, int nch) {   // partial slots for any count used below
         int m = std::max(ctx->force_splits, (nch + 4095) / 4096);
         for (int v : c) m = std::max(m, v);
