@@ -82,6 +82,9 @@ SIGNATURES = {
     "globe_set_device_loop": (C.c_int, [_vp, C.c_int]),
     "globe_get_device_loop": (C.c_int, [_vp]),
     "globe_device_loop_runs": (C.c_int64, [_vp]),
+    "globe_set_record_df": (C.c_int, [_vp, C.c_int]),
+    "globe_get_record_df": (C.c_int, [_vp]),
+    "globe_record_df_solves": (C.c_int64, [_vp]),
     "globe_set_autotune": (C.c_int, [_vp, C.c_int]),
     "globe_get_autotune": (C.c_int, [_vp]),
     "globe_autotune_log": (C.c_int64, [_vp, C.c_char_p, C.c_int64]),

@@ -198,6 +198,17 @@ class Context:
         """Solves that ran their iterations as the device-side loop."""
         return int(self._L.globe_device_loop_runs(self.h))
 
+    def set_record_df(self, on):
+        """Run the record kernels of mixed-precision solves in double-float (default on)."""
+        self._ck(self._L.globe_set_record_df(self.h, int(on)))
+
+    def get_record_df(self):
+        return bool(self._L.globe_get_record_df(self.h))
+
+    def record_df_solves(self):
+        """Solves that ran their record kernels in double-float."""
+        return int(self._L.globe_record_df_solves(self.h))
+
     def set_autotune(self, on):
         """Time split counts and column groupings of the tensor-core product on first use (default on)."""
         self._ck(self._L.globe_set_autotune(self.h, int(on)))

@@ -37,8 +37,8 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-I", os.path.join(ROOT, "include"), "-I", SRC,
           "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
-LIB_SOURCES = ["api.cu", "k_bed.cu", "k_records.cu", "k_grm_geno.cu", "k_grm_dense.cu", "k_tc_geno.cu", "solver.cu", "noalloc.cu", "ingest.cu",
-               "k_grm_build.cu", "k_tc_dense.cu",
+LIB_SOURCES = ["api.cu", "k_bed.cu", "k_records.cu", "k_records_df.cu", "k_grm_geno.cu", "k_grm_dense.cu", "k_tc_geno.cu",
+               "solver.cu", "noalloc.cu", "ingest.cu", "k_grm_build.cu", "k_tc_dense.cu",
                "aireml.cpp", "io.cpp"]
 # program -> (source, extra flags)
 CLI = {"runPCGsolver": ("cli_pcg.cpp", []), "runAIREML": ("cli_aireml.cpp", []),

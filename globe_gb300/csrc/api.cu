@@ -126,7 +126,7 @@ void prof_end(globe_ctx* ctx, int h) {
 static void free_cohort(globe_ctx* ctx) {
     auto& c = ctx->coh;
     for (void* p : {(void*)c.X, (void*)c.y, (void*)c.bstart, (void*)c.bind, (void*)c.rind, (void*)c.bn,
-                    (void*)c.bt, (void*)c.btt, (void*)c.lblk})
+                    (void*)c.bt, (void*)c.btt, (void*)c.lblk, (void*)c.tdf})
         dfree(ctx, p);
     c = Cohort();
     for (void* p : {(void*)ctx->vinv_X, (void*)ctx->vinv_r, (void*)ctx->uhat, (void*)ctx->f_theta}) dfree(ctx, p);
@@ -243,6 +243,17 @@ int globe_set_device_loop(globe_ctx* ctx, int on) {
 int globe_get_device_loop(const globe_ctx* ctx) { return ctx ? ctx->device_loop : -1; }
 
 int64_t globe_device_loop_runs(const globe_ctx* ctx) { return ctx ? ctx->device_loop_runs : -1; }
+
+int globe_set_record_df(globe_ctx* ctx, int on) {
+    if (!ctx) return GLOBE_ERR_ARG;
+    if (on != 0 && on != 1) return set_err(ctx, GLOBE_ERR_ARG, "globe_set_record_df: on must be 0 or 1, got %d", on);
+    ctx->record_df = on;
+    return GLOBE_OK;
+}
+
+int globe_get_record_df(const globe_ctx* ctx) { return ctx ? ctx->record_df : -1; }
+
+int64_t globe_record_df_solves(const globe_ctx* ctx) { return ctx ? ctx->record_df_runs : -1; }
 
 
 int globe_set_autotune(globe_ctx* ctx, int on) {
@@ -399,6 +410,12 @@ int globe_load_records(globe_ctx* ctx, int64_t Nrec, int32_t N, int32_t p, const
     GLOBE_CK(ctx, cudaMemcpyAsync(c.bind, bind.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, ctx->stream));
     GLOBE_CK(ctx, cudaMemcpyAsync(c.rind, rind.data(), sizeof(int32_t) * Nrec, cudaMemcpyHostToDevice, ctx->stream));
     GLOBE_RET(block_moments(ctx));
+    // the times as double-float pairs, for the double-float record kernels
+    double tmax = 0.0;
+    for (int64_t r = 0; r < Nrec; ++r) tmax = std::max(tmax, std::fabs(X[(int64_t)p * Nrec + r]));
+    c.tmax = tmax;
+    GLOBE_RET(dalloc(ctx, &c.tdf, (size_t)Nrec));
+    GLOBE_RET(to_df(ctx, c.times(), Nrec, c.tdf));
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return GLOBE_OK;
 }

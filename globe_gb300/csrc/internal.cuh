@@ -43,6 +43,8 @@ struct Cohort {
     int32_t max_block = 0;
     int32_t* lblk = nullptr;   // blocks with more than SHORT_BLOCK records (device list)
     int32_t nlong = 0;
+    float2* tdf = nullptr;     // times as double-float pairs (the double-float record kernels)
+    double tmax = 0;           // max |t|
     const double* times() const { return X + (size_t)p * Nrec; }
 };
 
@@ -85,7 +87,7 @@ enum SlotId {
     WS_R, WS_Z, WS_P, WS_VP, WS_ZI, WS_GZ, WS_S1, WS_PART, WS_SCAL, WS_COLS, WS_W,
     WS_GPART, WS_B, WS_TMP1, WS_TMP2, WS_TMP3, WS_TMP4, WS_H, WS_HSTAR, WS_PROBE,
     WS_UH, WS_SMALL, WS_IO1, WS_IO2, WS_BHAT, WS_FB, WS_FX,
-    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_LOOP, WS_COUNT
+    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_LOOP, WS_S0DF, WS_HDF, WS_COUNT
 };
 
 // Scalars kept on the device during a solve (per column, k entries each).
@@ -147,6 +149,10 @@ struct globe_ctx {
     cudaGraphExec_t pcg_loop = nullptr;
     int device_loop = 1;
     int64_t device_loop_runs = 0;
+    // record kernels of GLOBE_PREC_MIXED solves in double-float (k_records_df.cu), and how many
+    // solves ran them (globe_set_record_df)
+    int record_df = 1;
+    int64_t record_df_runs = 0;
     bool capturing = false;       // a stream capture is open: allocation is refused
     // event profiling (globe_prof_*)
     bool prof_on = false;
@@ -265,7 +271,7 @@ int synth_bed(globe_ctx* ctx, uint8_t* d_bed, int64_t M, int32_t N, int64_t stri
 
 // k_records.cu
 int block_moments(globe_ctx* ctx);
-int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H);
+int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H, float2* Hdf = nullptr);
 int seg_sums(globe_ctx* ctx, const double* x, const double* z, const double* beta, double* xout,
              const int32_t* cols, int kact, double* Zi, double* S1);
 int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double* Zi,
@@ -279,7 +285,8 @@ int precond_apply_scratch(globe_ctx* ctx, const double* H, const double* r, doub
                           size_t part_cap, double* rz);
 int col_dots(globe_ctx* ctx, const double* a, const double* b, int64_t n, int64_t lda, int64_t ldb,
              const int32_t* cols, int kact, double* out);
-int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int kact);
+int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int kact,
+               float2* out_df = nullptr);
 int xt_mat(globe_ctx* ctx, const double* X, int m1, const double* S, int m2, double* out);
 int sub_mat(globe_ctx* ctx, const double* A, const double* Bm, int m, const double* c, double* out,
             int kout);
@@ -289,6 +296,23 @@ int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, 
                  double* Y);
 int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double* TY, int numMC,
                 double* out);
+
+// k_records_df.cu: the iteration's record kernels on double-float vectors (float2 in the
+// place of each double); Zi, GZ, the partial sums and the scalars stay FP64
+int to_df(globe_ctx* ctx, const double* in, int64_t n, float2* out);
+struct DfCols {   // up to 4 (source, destination) column blocks; unused destinations null
+    const double* src[4] = {nullptr, nullptr, nullptr, nullptr};
+    double* dst[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+int cols_to_df(globe_ctx* ctx, const DfCols& v, int64_t n, int k, const double* bb, double* rz);
+int precond_apply_df(globe_ctx* ctx, const float2* H, const float2* r, float2* z, int k, double* rz);
+int cols_from_df(globe_ctx* ctx, double* v, int64_t n, int k, const double* bb);
+int seg_sums_df(globe_ctx* ctx, float2* x, const float2* z, const float2* beta, const int32_t* cols, int kact,
+                double* Zi, float2* S0, float2* S1);
+int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const float2* S0, const float2* S1,
+                   const int32_t* cols, int kact, float2* out, double* dot_out);
+int pcg_update_df(globe_ctx* ctx, const float2* H, const float2* alpha, float2* x, float2* r, const float2* p,
+                  const float2* Vp, float2* z, const int32_t* cols, int kact, double* rr, double* rz);
 
 // k_grm_geno.cu
 int geno_apply_f64(globe_ctx* ctx, const double* Z, int k, double scale, double* out);

@@ -17,32 +17,15 @@
 //         H = (sig2e I + C W'W)^-1 C, a 2x2 per individual.
 //
 // Reductions are deterministic: per-CTA partials, then a fixed-order reduce.
-#include "internal.cuh"
+#include "df.cuh"
+#include "records.cuh"
 
 namespace globe {
 
-constexpr int RB_THREADS = 256;  // 8 warps, one block of records per warp
-constexpr int RB_WARPS = RB_THREADS / 32;
-constexpr int TB_THREADS = 256;  // thread-per-block layout
 // limits of precond_apply_scratch, which may set no kernel attribute: columns are
 // grid rows (gridDim.y <= 65535), and dynamic shared memory stays at the default 48 KB
 constexpr int NOALLOC_MAX_COLS = 65535;
 constexpr size_t NOALLOC_SMEM_BYTES = 48 * 1024;
-
-// Launch shape of the record kernels: one thread per (block of <= SHORT_BLOCK records,
-// column) over all blocks -- nbt CTAs per column, longer blocks skipped -- and one
-// warp per longer block over the list coh.lblk (nbl CTAs).  Per-CTA partial sums of
-// both go to part[slot + q * S], thread-layout CTAs first.
-struct RecShape {
-    int nbt, nbl, S;
-};
-static RecShape rec_shape(const globe_ctx* ctx) {
-    RecShape r;
-    r.nbt = div_up(ctx->coh.N, TB_THREADS);
-    r.nbl = ctx->coh.nlong > 0 ? div_up(ctx->coh.nlong, RB_WARPS) : 0;
-    r.S = r.nbt + r.nbl;
-    return r;
-}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -124,7 +107,8 @@ int block_moments(globe_ctx* ctx) {
 // H_b = (sig2e I + C G)^-1 C,  C = [[b0 + g, b01], [b01, b1]],  G = [[n, St], [St, Stt]]
 __global__ void k_build_H(int32_t nblk, const double* __restrict__ bn, const double* __restrict__ bt,
                           const double* __restrict__ btt, const int32_t* __restrict__ bind,
-                          const double* __restrict__ gdiag, double gconst, VC v, double* __restrict__ H) {
+                          const double* __restrict__ gdiag, double gconst, VC v, double* __restrict__ H,
+                          float2* __restrict__ Hdf) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nblk) return;
     if (gdiag && !GLOBE_BOUNDS(bind[b] >= 0 && bind[b] < nblk, 0x0A01u)) return;
@@ -137,16 +121,19 @@ __global__ void k_build_H(int32_t nblk, const double* __restrict__ bn, const dou
     double m11 = v.e + c01 * g01 + c11 * g11;
     double det = m00 * m11 - m01 * m10;
     double i00 = m11 / det, i01 = -m01 / det, i10 = -m10 / det, i11 = m00 / det;
-    H[4 * b + 0] = i00 * c00 + i01 * c01;
-    H[4 * b + 1] = i00 * c01 + i01 * c11;
-    H[4 * b + 2] = i10 * c00 + i11 * c01;
-    H[4 * b + 3] = i10 * c01 + i11 * c11;
+    const double h[4] = {i00 * c00 + i01 * c01, i00 * c01 + i01 * c11, i10 * c00 + i11 * c01,
+                         i10 * c01 + i11 * c11};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        H[4 * b + j] = h[j];
+        if (Hdf) df::store(Hdf + 4 * b + j, df::from_double(h[j]));   // the double-float record kernels' copy
+    }
 }
 
-int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H) {
+int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H, float2* Hdf) {
     VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
     auto& c = ctx->coh;
-    k_build_H<<<div_up(c.N, 128), 128, 0, ctx->stream>>>(c.N, c.bn, c.bt, c.btt, c.bind, gdiag, gconst, v, H);
+    k_build_H<<<div_up(c.N, 128), 128, 0, ctx->stream>>>(c.N, c.bn, c.bt, c.btt, c.bind, gdiag, gconst, v, H, Hdf);
     GLOBE_LAUNCHED(ctx, "k_build_H");
     return GLOBE_OK;
 }
@@ -258,7 +245,7 @@ __global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t
                               const double* __restrict__ Zi, const double* __restrict__ S1,
                               const int32_t* __restrict__ cols, int kact, double* __restrict__ out,
                               double* __restrict__ part, const int32_t* __restrict__ bl, int slot0, int pstride) {
-    extern __shared__ double sm[];
+    __shared__ double sm[RCH * RB_WARPS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int idx = blockIdx.x * RB_WARPS + warp;
     const bool live = idx < nblk;
@@ -266,29 +253,33 @@ __global__ void k_vx_assemble(int32_t nblk, int64_t ld, int32_t N, const int32_t
     int st = 0, en = 0, i = 0;
     if (live) { st = bstart[b]; en = bstart[b + 1]; i = bind[b]; }
     if (live && !GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld && i >= 0 && i < N, 0x0301u)) st = en = i = 0;
-    for (int c = 0; c < kact; ++c) {
-        const int col = cols ? cols[c] : c;
-        double dot = 0;
-        if (live) {
-            const double s0 = Zi[i + (size_t)c * N], s1 = S1[i + (size_t)c * N];
-            const double g = GZ ? GZ[i + (size_t)c * N] : 0.0;
-            const double a0 = g + v.b0 * s0 + v.b01 * s1;
-            const double a1 = v.b01 * s0 + v.b1 * s1;
-            const double* xc = x + (size_t)col * ld;
-            double* oc = out + (size_t)col * ld;
-            for (int r = st + lane; r < en; r += 32) {
-                double xv = xc[r];
-                double o = a0 + t[r] * a1 + v.e * xv;
-                oc[r] = o;
-                dot += xv * o;
+    for (int c0 = 0; c0 < kact; c0 += RCH) {
+        const int nc = min(RCH, kact - c0);
+        for (int cc = 0; cc < nc; ++cc) {
+            const int c = c0 + cc;
+            const int col = cols ? cols[c] : c;
+            double dot = 0;
+            if (live) {
+                const double s0 = Zi[i + (size_t)c * N], s1 = S1[i + (size_t)c * N];
+                const double g = GZ ? GZ[i + (size_t)c * N] : 0.0;
+                const double a0 = g + v.b0 * s0 + v.b01 * s1;
+                const double a1 = v.b01 * s0 + v.b1 * s1;
+                const double* xc = x + (size_t)col * ld;
+                double* oc = out + (size_t)col * ld;
+                for (int r = st + lane; r < en; r += 32) {
+                    double xv = xc[r];
+                    double o = a0 + t[r] * a1 + v.e * xv;
+                    oc[r] = o;
+                    dot += xv * o;
+                }
+            }
+            if (part) {
+                dot = warp_sum(dot);
+                if (lane == 0) sm[cc * RB_WARPS + warp] = dot;
             }
         }
-        if (part) {
-            dot = warp_sum(dot);
-            if (lane == 0) sm[c * RB_WARPS + warp] = dot;
-        }
+        if (part) flush_chunk(sm, 1, nc, c0, kact, part, slot0 + blockIdx.x, pstride);
     }
-    if (part) cta_partials(sm, kact, part, slot0 + blockIdx.x, pstride);
 }
 
 __global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32_t* __restrict__ bstart,
@@ -335,8 +326,7 @@ int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double*
                                                                           v, x, GZ, Zi, S1, cols, out, part, rs.S);
     GLOBE_LAUNCHED(ctx, "k_vx_assemble_t");
     if (rs.nbl) {
-        const size_t sm = dot_out ? sizeof(double) * RB_WARPS * kact : 0;
-        k_vx_assemble<<<rs.nbl, RB_THREADS, sm, ctx->stream>>>(c.nlong, c.Nrec, c.N, c.bstart, c.bind, c.times(), v,
+        k_vx_assemble<<<rs.nbl, RB_THREADS, 0, ctx->stream>>>(c.nlong, c.Nrec, c.N, c.bstart, c.bind, c.times(), v,
                                                                 x, GZ, Zi, S1, cols, kact, out, part, c.lblk, rs.nbt,
                                                                 rs.S);
         GLOBE_LAUNCHED(ctx, "k_vx_assemble");
@@ -354,7 +344,7 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
                              const double* __restrict__ p, const double* __restrict__ Vp,
                              double* __restrict__ z, const int32_t* __restrict__ cols, int kact,
                              double* __restrict__ part, const int32_t* __restrict__ bl, int slot0, int pstride) {
-    extern __shared__ double sm[];
+    __shared__ double sm[2 * RCH * RB_WARPS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int idx = blockIdx.x * RB_WARPS + warp;
     const bool live = idx < nblk;
@@ -370,44 +360,48 @@ __global__ void k_pcg_update(int32_t nblk, int64_t ld, const int32_t* __restrict
         h11 = H[4 * b + 3];
         if (!GLOBE_BOUNDS(st >= 0 && st <= en && en <= ld, 0x0501u)) st = en = 0;
     }
-    for (int c = 0; c < kact; ++c) {
-        const int col = cols ? cols[c] : c;
-        double rr = 0, rz = 0;
-        if (live) {
-            const double a = alpha[col];
-            double* xc = x + (size_t)col * ld;
-            double* rc = r + (size_t)col * ld;
-            const double* pc = p + (size_t)col * ld;
-            const double* vc = Vp + (size_t)col * ld;
-            double s0 = 0, s1 = 0;
-            for (int q = st + lane; q < en; q += 32) {
-                xc[q] += a * pc[q];
-                double rn = rc[q] - a * vc[q];
-                rc[q] = rn;
-                rr += rn * rn;
-                s0 += rn;
-                s1 += t[q] * rn;
+    for (int c0 = 0; c0 < kact; c0 += RCH) {
+        const int nc = min(RCH, kact - c0);
+        for (int cc = 0; cc < nc; ++cc) {
+            const int c = c0 + cc;
+            const int col = cols ? cols[c] : c;
+            double rr = 0, rz = 0;
+            if (live) {
+                const double a = alpha[col];
+                double* xc = x + (size_t)col * ld;
+                double* rc = r + (size_t)col * ld;
+                const double* pc = p + (size_t)col * ld;
+                const double* vc = Vp + (size_t)col * ld;
+                double s0 = 0, s1 = 0;
+                for (int q = st + lane; q < en; q += 32) {
+                    xc[q] += a * pc[q];
+                    double rn = rc[q] - a * vc[q];
+                    rc[q] = rn;
+                    rr += rn * rn;
+                    s0 += rn;
+                    s1 += t[q] * rn;
+                }
+                s0 = warp_sum(s0);
+                s1 = warp_sum(s1);
+                const double g0 = h00 * s0 + h01 * s1, g1 = h10 * s0 + h11 * s1;
+                const double g0e = g0 * inv_e, g1e = g1 * inv_e;   // z = r/sig2e - (g0 + g1 t)/sig2e
+                double* zc = z + (size_t)col * ld;
+                for (int q = st + lane; q < en; q += 32) {
+                    double rn = rc[q];
+                    double zv = fma(rn, inv_e, -fma(g1e, t[q], g0e));
+                    zc[q] = zv;
+                    rz += rn * zv;
+                }
             }
-            s0 = warp_sum(s0);
-            s1 = warp_sum(s1);
-            const double g0 = h00 * s0 + h01 * s1, g1 = h10 * s0 + h11 * s1;
-            const double g0e = g0 * inv_e, g1e = g1 * inv_e;   // z = r/sig2e - (g0 + g1 t)/sig2e
-            double* zc = z + (size_t)col * ld;
-            for (int q = st + lane; q < en; q += 32) {
-                double rn = rc[q];
-                double zv = fma(rn, inv_e, -fma(g1e, t[q], g0e));
-                zc[q] = zv;
-                rz += rn * zv;
+            rr = warp_sum(rr);
+            rz = warp_sum(rz);
+            if (lane == 0) {
+                sm[cc * RB_WARPS + warp] = rr;
+                sm[(RCH + cc) * RB_WARPS + warp] = rz;
             }
         }
-        rr = warp_sum(rr);
-        rz = warp_sum(rz);
-        if (lane == 0) {
-            sm[c * RB_WARPS + warp] = rr;
-            sm[(kact + c) * RB_WARPS + warp] = rz;
-        }
+        flush_chunk(sm, 2, nc, c0, kact, part, slot0 + blockIdx.x, pstride);
     }
-    cta_partials(sm, 2 * kact, part, slot0 + blockIdx.x, pstride);
 }
 
 __global__ void k_pcg_update_t(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
@@ -464,8 +458,7 @@ int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, 
                                                                          cols, kact, part, rs.S);
     GLOBE_LAUNCHED(ctx, "k_pcg_update_t");
     if (rs.nbl) {
-        const size_t sm = sizeof(double) * RB_WARPS * kact * 2;
-        k_pcg_update<<<rs.nbl, RB_THREADS, sm, ctx->stream>>>(c.nlong, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0],
+        k_pcg_update<<<rs.nbl, RB_THREADS, 0, ctx->stream>>>(c.nlong, c.Nrec, c.bstart, c.times(), 1.0 / ctx->vc[0],
                                                                H, alpha, x, r, p, Vp, z, cols, kact, part, c.lblk,
                                                                rs.nbt, rs.S);
         GLOBE_LAUNCHED(ctx, "k_pcg_update");
@@ -682,13 +675,19 @@ int col_dots(globe_ctx* ctx, const double* a, const double* b, int64_t n, int64_
     return reduce_cols(ctx, part, nb, kact, cols, out);
 }
 
-__global__ void k_scal_div(const double* __restrict__ num, const double* __restrict__ den, double* out, int k) {
+// out = num / den (0 where den = 0), and its double-float copy when out_df is given
+__global__ void k_scal_div(const double* __restrict__ num, const double* __restrict__ den, double* out, int k,
+                           float2* __restrict__ out_df) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < k) out[c] = (den[c] != 0.0) ? num[c] / den[c] : 0.0;
+    if (c < k) {
+        const double q = (den[c] != 0.0) ? num[c] / den[c] : 0.0;
+        out[c] = q;
+        if (out_df) df::store(out_df + c, df::from_double(q));
+    }
 }
 
-int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int k) {
-    k_scal_div<<<div_up(k, 128), 128, 0, ctx->stream>>>(num, den, out, k);
+int scal_alpha(globe_ctx* ctx, const double* num, const double* den, double* out, int k, float2* out_df) {
+    k_scal_div<<<div_up(k, 128), 128, 0, ctx->stream>>>(num, den, out, k, out_df);
     GLOBE_LAUNCHED(ctx, "k_scal_div");
     return GLOBE_OK;
 }

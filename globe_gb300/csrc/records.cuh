@@ -1,0 +1,45 @@
+// records.cuh -- launch shape shared by the record kernels (k_records.cu, k_records_df.cu).
+#pragma once
+
+#include "internal.cuh"
+
+namespace globe {
+
+constexpr int RB_THREADS = 256;  // 8 warps, one block of records per warp
+constexpr int RB_WARPS = RB_THREADS / 32;
+constexpr int TB_THREADS = 256;  // thread-per-block layout
+
+// Launch shape of the record kernels: one thread per (block of <= SHORT_BLOCK records,
+// column) over all blocks -- nbt CTAs per column, longer blocks skipped -- and one
+// warp per longer block over the list coh.lblk (nbl CTAs).  Per-CTA partial sums of
+// both go to part[slot + q * S], thread-layout CTAs first.
+struct RecShape {
+    int nbt, nbl, S;
+};
+inline RecShape rec_shape(const globe_ctx* ctx) {
+    RecShape r;
+    r.nbt = div_up(ctx->coh.N, TB_THREADS);
+    r.nbl = ctx->coh.nlong > 0 ? div_up(ctx->coh.nlong, RB_WARPS) : 0;
+    r.S = r.nbt + r.nbl;
+    return r;
+}
+
+// The warp-per-block kernels stage per-warp partial sums of RCH columns at a time in static
+// shared memory, sm[(j * RCH + cc) * RB_WARPS + warp] for quantity j < nq and column c0 + cc,
+// so any number of columns fits.  flush_chunk sums them over the CTA's warps, in warp order,
+// into part[slot + (j * kact + c0 + cc) * stride]; every thread of the CTA calls it.
+constexpr int RCH = 32;
+__device__ __forceinline__ void flush_chunk(const double* sm, int nq, int nc, int c0, int kact, double* part, int slot,
+                                            int stride) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < nq * nc; e += blockDim.x) {
+        const int j = e / nc, cc = e - j * nc;
+        double a = 0.0;
+#pragma unroll
+        for (int w = 0; w < RB_WARPS; ++w) a += sm[(j * RCH + cc) * RB_WARPS + w];
+        part[slot + (size_t)(j * kact + c0 + cc) * stride] = a;
+    }
+    __syncthreads();
+}
+
+}  // namespace globe

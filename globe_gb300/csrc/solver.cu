@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "df.cuh"
 #include "internal.cuh"
 
 namespace globe {
@@ -45,8 +46,10 @@ int ensure_precond(globe_ctx* ctx) {
     if (ctx->precond_ok) return GLOBE_OK;
     GLOBE_RET(ensure_gdiag(ctx));
     double* H;
+    float2* Hdf;
     GLOBE_RET(ws(ctx, WS_H, (size_t)ctx->coh.N * 4, &H));
-    GLOBE_RET(build_H(ctx, ctx->gen.gdiag, 0.0, H));
+    GLOBE_RET(ws(ctx, WS_HDF, (size_t)ctx->coh.N * 4, &Hdf));
+    GLOBE_RET(build_H(ctx, ctx->gen.gdiag, 0.0, H, Hdf));
     ctx->precond_ok = true;
     return GLOBE_OK;
 }
@@ -164,7 +167,8 @@ __global__ void k_pcg_loop_arm(cudaGraphConditionalHandle h) { cudaGraphSetCondi
 // the host loop's stopping rule (pcg_run) on the device: one thread, after iteration st->it + 1
 __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restrict__ pvp,
                             const double* __restrict__ bb, const int32_t* __restrict__ cols, int kact, int k,
-                            double tol, int rule, int maxit, PcgLoopState* st, cudaGraphConditionalHandle h) {
+                            double tol, int rule, int maxit, int scaled, PcgLoopState* st,
+                            cudaGraphConditionalHandle h) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int it = st->it + 1;
     st->it = it;
@@ -184,7 +188,8 @@ __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restr
         double mx = 0.0;
         for (int j = 0; j < k; ++j) {
             const double nb = sqrt(bb[j]);
-            const double q = nb > small_b ? sqrt(rr[j]) / nb : 0.0;
+            const double u = scaled ? col_unscale(bb[j]) : 1.0;
+            const double q = nb > small_b ? sqrt(rr[j]) * u / nb : 0.0;
             if (q > mx) mx = q;
         }
         if (mx < tol) {
@@ -203,7 +208,7 @@ __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restr
     } else {
         bool all = true;
         for (int j = 0; j < k; ++j)
-            if (bb[j] > 0.0 && !(sqrt(rr[j]) < tol * sqrt(bb[j]))) {
+            if (bb[j] > 0.0 && !(sqrt(rr[j]) * (scaled ? col_unscale(bb[j]) : 1.0) < tol * sqrt(bb[j]))) {
                 all = false;
                 break;
             }
@@ -220,12 +225,15 @@ __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restr
 }
 
 // beta = r'z(new) / r'z(old) (0 where r'z(old) = 0, as k_scal_div), then r'z(old) = r'z(new)
+// (and beta's double-float copy when beta_df is given)
 __global__ void k_pcg_beta_shift(double* __restrict__ rz, const double* __restrict__ rz2, double* __restrict__ beta,
-                                 int k) {
+                                 float2* __restrict__ beta_df, int k) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < k) {
         const double o = rz[c], nw = rz2[c];
-        beta[c] = (o != 0.0) ? nw / o : 0.0;
+        const double bt = (o != 0.0) ? nw / o : 0.0;
+        beta[c] = bt;
+        if (beta_df) df::store(beta_df + c, df::from_double(bt));
         rz[c] = nw;
     }
 }
@@ -296,6 +304,17 @@ static int run_device_loop(globe_ctx* ctx, F&& body, int64_t* nlaunch, bool* ran
     return GLOBE_OK;
 }
 
+// Whether a GLOBE_PREC_MIXED solve may run its record kernels in double-float: with each
+// column scaled to a unit-size right-hand side, the variance components and times bound every
+// value of the iteration well inside FP32's exponent range.  Otherwise the FP64 kernels run.
+static bool df_records_ok(const globe_ctx* ctx) {
+    const double lo = std::ldexp(1.0, -30), hi = std::ldexp(1.0, 30);
+    if (!(ctx->vc[0] >= lo && ctx->vc[0] <= hi)) return false;
+    for (int j = 1; j < 5; ++j)
+        if (!(std::fabs(ctx->vc[j]) <= hi)) return false;
+    return ctx->coh.tdf != nullptr && ctx->coh.tmax <= hi;
+}
+
 static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o, globe_pcg_info* info) {
     GLOBE_RET(check_ready(ctx));
     if (k < 1) return set_err(ctx, GLOBE_ERR_ARG, "number of right-hand sides must be >= 1");
@@ -313,7 +332,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     GLOBE_RET(ws(ctx, WS_ZI, (size_t)N * k, &Zi));
     GLOBE_RET(ws(ctx, WS_GZ, (size_t)N * k, &GZ));
     GLOBE_RET(ws(ctx, WS_S1, (size_t)N * k, &S1));
-    GLOBE_RET(ws(ctx, WS_SCAL, (size_t)8 * k, &scal));
+    GLOBE_RET(ws(ctx, WS_SCAL, (size_t)10 * k, &scal));
     GLOBE_RET(ws(ctx, WS_COLS, (size_t)k, &dcols));
     GLOBE_RET(ws(ctx, WS_PART, (size_t)std::max<int64_t>(div_up(N, 8), 304) * k * 2, &part));
     PcgLoopState* dstate;
@@ -326,16 +345,38 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     double* beta = scal + 4 * k;
     double* rr = scal + 5 * k;
     double* bb = scal + 6 * k;
+    float2* alpha_df = reinterpret_cast<float2*>(scal + 8 * k);   // double-float copies of alpha, beta
+    float2* beta_df = reinterpret_cast<float2*>(scal + 9 * k);
     if ((size_t)4 * k > ctx->hpin_n) return set_err(ctx, GLOBE_ERR_ARG, "too many right-hand sides (%d)", k);
     double* h_rr = ctx->hpin;
     double* h_bb = ctx->hpin + k;
     double* h_pvp = ctx->hpin + 2 * k;
 
+    // Under GLOBE_PREC_MIXED the iterations run on double-float vectors (df_records_ok): x, r,
+    // z and p hold pairs, column c scaled by 1/unsc[c] (a power of two, col_unscale), and x is
+    // converted back when the loop ends, however it ends.  From x0 = 0 the set-up itself runs
+    // in double-float (r = b scaled, z = Q^-1 r); from another start point it runs in FP64 and
+    // x, r, z, p are converted in place.  r'z follows the scaling; the host and the device
+    // check unscale r'r exactly (sqrt(rr) unsc = sqrt(rr unsc^2)).
+    const bool df = ctx->prec == GLOBE_PREC_MIXED && ctx->record_df && df_records_ok(ctx);
+    const bool df_setup = df && o->x0mode == GLOBE_X0_ZERO;
+    float2* Hdf = reinterpret_cast<float2*>(ctx->ws[WS_HDF].p);
+    float2* S0df = nullptr;
+    if (df) GLOBE_RET(ws(ctx, WS_S0DF, (size_t)N * k, &S0df));
+    auto F = [](double* v) { return reinterpret_cast<float2*>(v); };
+
     GLOBE_RET(col_dots(ctx, B, B, n, n, n, nullptr, k, bb));
     switch (o->x0mode) {
         case GLOBE_X0_ZERO:
             GLOBE_CK(ctx, cudaMemsetAsync(X, 0, sizeof(double) * n * k, ctx->stream));
-            GLOBE_CK(ctx, cudaMemcpyAsync(r, B, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
+            if (df_setup) {
+                DfCols v;
+                v.src[0] = B;
+                v.dst[0] = r;
+                GLOBE_RET(cols_to_df(ctx, v, n, k, bb, nullptr));
+            } else {
+                GLOBE_CK(ctx, cudaMemcpyAsync(r, B, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
+            }
             break;
         case GLOBE_X0_PRECOND:
             GLOBE_RET(precond_apply(ctx, H, B, X, nullptr, k, nullptr));
@@ -349,12 +390,16 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
         default:
             return set_err(ctx, GLOBE_ERR_ARG, "unknown x0 mode %d", o->x0mode);
     }
-    GLOBE_RET(precond_apply(ctx, H, r, z, nullptr, k, rz));
+    if (df_setup) GLOBE_RET(precond_apply_df(ctx, Hdf, F(r), F(z), k, rz));
+    else GLOBE_RET(precond_apply(ctx, H, r, z, nullptr, k, rz));
     GLOBE_CK(ctx, cudaMemcpyAsync(p, z, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
-    GLOBE_RET(col_dots(ctx, r, r, n, n, n, nullptr, k, rr));
+    // from x0 = 0, r = b: r'r is b'b (the same kernel on the same values)
+    const bool r_is_b = o->x0mode == GLOBE_X0_ZERO;
+    if (!r_is_b) GLOBE_RET(col_dots(ctx, r, r, n, n, n, nullptr, k, rr));
     GLOBE_CK(ctx, cudaMemcpyAsync(h_bb, bb, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-    GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+    if (!r_is_b) GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
     GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (r_is_b) std::copy(h_bb, h_bb + k, h_rr);
 
     std::vector<double> nb(k), nr(k);
     for (int j = 0; j < k; ++j) {
@@ -376,6 +421,36 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     for (int j = 0; j < k; ++j)
         if (h_bb[j] > 0.0) cols.push_back(j);
         else GLOBE_CK(ctx, cudaMemsetAsync(X + (size_t)j * n, 0, sizeof(double) * n, ctx->stream));
+
+    std::vector<double> unsc(k, 1.0);
+    if (df) {
+        for (int j = 0; j < k; ++j) unsc[j] = col_unscale(h_bb[j]);
+        if (!df_setup) {   // x, r, z, p to double-float in place; r'z scaled with them
+            DfCols v;
+            double* vv[4] = {X, r, z, p};
+            for (int j = 0; j < 4; ++j) v.src[j] = v.dst[j] = vv[j];
+            GLOBE_RET(cols_to_df(ctx, v, n, k, bb, rz));
+        }
+        ctx->record_df_runs += 1;
+    }
+    // one iteration on the stream: the operator on p, alpha, and the updates up to r'r and r'z
+    auto iteration = [&](bool first, int kc) -> int {
+        if (df) {
+            GLOBE_RET(seg_sums_df(ctx, F(p), first ? nullptr : F(z), first ? nullptr : beta_df, dcols, kc, Zi, S0df,
+                                  F(S1)));
+            GLOBE_RET(grm_apply_dev(ctx, Zi, kc, GZ));
+            GLOBE_RET(vx_assemble_df(ctx, F(p), GZ, S0df, F(S1), dcols, kc, F(Vp), pvp));
+            GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k, alpha_df));
+            return pcg_update_df(ctx, Hdf, alpha_df, F(X), F(r), F(p), F(Vp), F(z), dcols, kc, rr, rz2);
+        }
+        if (!first) GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kc, Zi, S1));
+        else GLOBE_RET(seg_sums(ctx, p, nullptr, nullptr, nullptr, dcols, kc, Zi, S1));
+        GLOBE_RET(grm_apply_dev(ctx, Zi, kc, GZ));
+        GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kc, Vp, pvp));
+        GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
+        return pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kc, rr, rz2);
+    };
+
     std::vector<int32_t> uploaded;
     double last = max_ratio();
     const double stag_frac = (double)5e-3f;
@@ -386,120 +461,124 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     bool use_graph = ctx->graphs && !ctx->prof_on;   // profiling times each pass with events
     std::vector<int32_t> gcols[2];                   // column set each graph was captured for
     int64_t glaunch[2] = {0, 0};                     // kernels per replay
-    for (it = 0; it < o->maxit && !cols.empty(); ++it) {
-        const int kact = (int)cols.size();
-        ProfScope iter_scope(ctx, GLOBE_PROF_PCG_ITER);
-        if (cols != uploaded) {
-            GLOBE_CK(ctx, cudaMemcpyAsync(dcols, cols.data(), sizeof(int32_t) * kact, cudaMemcpyHostToDevice, ctx->stream));
-            uploaded = cols;
-        }
-        // the iteration's stream work, up to the copies of the two k-vectors the host checks
-        auto body = [&](bool first) -> int {
-            if (!first) GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kact, Zi, S1));
-            else GLOBE_RET(seg_sums(ctx, p, nullptr, nullptr, nullptr, dcols, kact, Zi, S1));
-            GLOBE_RET(grm_apply_dev(ctx, Zi, kact, GZ));
-            GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kact, Vp, pvp));
-            GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
-            GLOBE_RET(pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kact, rr, rz2));
-            GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-            GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-            return GLOBE_OK;
-        };
-        // The first iteration runs directly (it also builds what the products make on first
-        // use).  Later ones replay a graph of the body, captured once per call, parity of the
-        // swapped r'z buffers and column set; a failed capture falls back to direct launches.
-        bool ran = false;
-        if (it > 0 && use_graph) {
-            const int slot = rz == scal ? 0 : 1;
-            if (gcols[slot] != cols) {
-                gcols[slot].clear();
-                if (capture_body(ctx, slot, [&]() { return body(false); }, &glaunch[slot])) gcols[slot] = cols;
-                else use_graph = false;
+    auto iterate = [&]() -> int {
+        for (it = 0; it < o->maxit && !cols.empty(); ++it) {
+            const int kact = (int)cols.size();
+            ProfScope iter_scope(ctx, GLOBE_PROF_PCG_ITER);
+            if (cols != uploaded) {
+                GLOBE_CK(ctx, cudaMemcpyAsync(dcols, cols.data(), sizeof(int32_t) * kact, cudaMemcpyHostToDevice,
+                                              ctx->stream));
+                uploaded = cols;
             }
-            if (use_graph) {
-                GLOBE_CK(ctx, cudaGraphLaunch(ctx->pcg_graph[slot], ctx->stream));
-                ctx->launches += glaunch[slot];
-                ran = true;
-            }
-        }
-        if (!ran) GLOBE_RET(body(it == 0));
-        GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-        rhs_iters += kact;
-        for (int j : cols) {
-            if (!(h_pvp[j] > 0.0) || !std::isfinite(h_rr[j]))
-                return set_err(ctx, GLOBE_ERR_NUMERIC, "PCG breakdown in column %d at iteration %d (p'Vp = %g)", j,
-                               it + 1, h_pvp[j]);
-            nr[j] = std::sqrt(h_rr[j]);
-        }
-        if (o->rule == GLOBE_RULE_PCGSOLVER) {
-            double mx = max_ratio();
-            if (mx < o->tol) { converged = true; ++it; break; }
-            double impr = last - mx;
-            if (impr < stag_frac * last) ++stag;
-            else stag = 0;
-            last = mx;
-            if (stag >= 10) { stagnated = true; ++it; break; }
-        } else {
-            bool all = true;
-            for (int j = 0; j < k; ++j)
-                if (h_bb[j] > 0.0 && !(nr[j] < o->tol * nb[j])) { all = false; break; }
-            if (all) { converged = true; ++it; break; }
-        }
-        if (o->mask) {
-            std::vector<int32_t> keep;
-            for (int j : cols)
-                if (!(nr[j] < o->tol * nb[j])) keep.push_back(j);
-            if (keep.empty()) { converged = true; ++it; break; }
-            cols.swap(keep);
-        }
-        GLOBE_RET(scal_alpha(ctx, rz2, rz, beta, k));
-        std::swap(rz, rz2);
-        // after the first iteration, the rest as one device-side loop (no per-iteration
-        // synchronisation) when graphs are on and the column set cannot change
-        if (it == 0 && use_graph && ctx->device_loop && !o->mask && o->maxit > 1) {
-            const PcgLoopState st0{last, 0, 1, stag, 0, -1};
-            GLOBE_CK(ctx, cudaMemcpyAsync(dstate, &st0, sizeof st0, cudaMemcpyHostToDevice, ctx->stream));
-            const int kc = kact;
-            auto loop_body = [&](cudaGraphConditionalHandle h) -> int {
-                GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kc, Zi, S1));
-                GLOBE_RET(grm_apply_dev(ctx, Zi, kc, GZ));
-                GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kc, Vp, pvp));
-                GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
-                GLOBE_RET(pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kc, rr, rz2));
-                k_pcg_check<<<1, 32, 0, ctx->stream>>>(rr, pvp, bb, dcols, kc, k, o->tol, o->rule, o->maxit, dstate,
-                                                       h);
-                GLOBE_LAUNCHED(ctx, "k_pcg_check");
-                k_pcg_beta_shift<<<div_up(k, 128), 128, 0, ctx->stream>>>(rz, rz2, beta, k);
-                GLOBE_LAUNCHED(ctx, "k_pcg_beta_shift");
+            // the iteration's stream work, up to the copies of the two k-vectors the host checks
+            auto body = [&](bool first) -> int {
+                GLOBE_RET(iteration(first, kact));
+                GLOBE_CK(ctx, cudaMemcpyAsync(h_rr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+                GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
                 return GLOBE_OK;
             };
-            int64_t per_it = 0;
+            // The first iteration runs directly (it also builds what the products make on first
+            // use).  Later ones replay a graph of the body, captured once per call, parity of the
+            // swapped r'z buffers and column set; a failed capture falls back to direct launches.
             bool ran = false;
-            GLOBE_RET(run_device_loop(ctx, loop_body, &per_it, &ran));
-            if (ran) {
-                PcgLoopState st;
-                double* h_scr = ctx->hpin + 3 * k;   // k doubles: the final r'r
-                GLOBE_CK(ctx, cudaMemcpyAsync(&st, dstate, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
-                GLOBE_CK(ctx, cudaMemcpyAsync(h_scr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-                GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
-                GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
-                if (st.it > 1) {   // the loop ran (see run_device_loop)
-                    ctx->launches += per_it * (st.it - 1) + 1;
-                    ctx->device_loop_runs += 1;
-                    rhs_iters += st.rhs_iters;
-                    for (int j : cols) nr[j] = std::sqrt(h_scr[j]);
-                    if (st.status == 4)
-                        return set_err(ctx, GLOBE_ERR_NUMERIC, "PCG breakdown in column %d at iteration %d (p'Vp = %g)",
-                                       st.err_col, st.it, h_pvp[st.err_col]);
-                    converged = st.status == 1;
-                    stagnated = st.status == 2;
-                    it = st.it;
-                    break;
+            if (it > 0 && use_graph) {
+                const int slot = rz == scal ? 0 : 1;
+                if (gcols[slot] != cols) {
+                    gcols[slot].clear();
+                    if (capture_body(ctx, slot, [&]() { return body(false); }, &glaunch[slot])) gcols[slot] = cols;
+                    else use_graph = false;
+                }
+                if (use_graph) {
+                    GLOBE_CK(ctx, cudaGraphLaunch(ctx->pcg_graph[slot], ctx->stream));
+                    ctx->launches += glaunch[slot];
+                    ran = true;
                 }
             }
-            use_graph = use_graph && ran;
+            if (!ran) GLOBE_RET(body(it == 0));
+            GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+            rhs_iters += kact;
+            for (int j : cols) {
+                if (!(h_pvp[j] > 0.0) || !std::isfinite(h_rr[j]))
+                    return set_err(ctx, GLOBE_ERR_NUMERIC, "PCG breakdown in column %d at iteration %d (p'Vp = %g)", j,
+                                   it + 1, h_pvp[j] * unsc[j] * unsc[j]);
+                nr[j] = std::sqrt(h_rr[j]) * unsc[j];
+            }
+            if (o->rule == GLOBE_RULE_PCGSOLVER) {
+                double mx = max_ratio();
+                if (mx < o->tol) { converged = true; ++it; break; }
+                double impr = last - mx;
+                if (impr < stag_frac * last) ++stag;
+                else stag = 0;
+                last = mx;
+                if (stag >= 10) { stagnated = true; ++it; break; }
+            } else {
+                bool all = true;
+                for (int j = 0; j < k; ++j)
+                    if (h_bb[j] > 0.0 && !(nr[j] < o->tol * nb[j])) { all = false; break; }
+                if (all) { converged = true; ++it; break; }
+            }
+            if (o->mask) {
+                std::vector<int32_t> keep;
+                for (int j : cols)
+                    if (!(nr[j] < o->tol * nb[j])) keep.push_back(j);
+                if (keep.empty()) { converged = true; ++it; break; }
+                cols.swap(keep);
+            }
+            GLOBE_RET(scal_alpha(ctx, rz2, rz, beta, k, df ? beta_df : nullptr));
+            std::swap(rz, rz2);
+            // after the first iteration, the rest as one device-side loop (no per-iteration
+            // synchronisation) when graphs are on and the column set cannot change
+            if (it == 0 && use_graph && ctx->device_loop && !o->mask && o->maxit > 1) {
+                const PcgLoopState st0{last, 0, 1, stag, 0, -1};
+                GLOBE_CK(ctx, cudaMemcpyAsync(dstate, &st0, sizeof st0, cudaMemcpyHostToDevice, ctx->stream));
+                const int kc = kact;
+                auto loop_body = [&](cudaGraphConditionalHandle h) -> int {
+                    GLOBE_RET(iteration(false, kc));
+                    k_pcg_check<<<1, 32, 0, ctx->stream>>>(rr, pvp, bb, dcols, kc, k, o->tol, o->rule, o->maxit,
+                                                           df ? 1 : 0, dstate, h);
+                    GLOBE_LAUNCHED(ctx, "k_pcg_check");
+                    k_pcg_beta_shift<<<div_up(k, 128), 128, 0, ctx->stream>>>(rz, rz2, beta, df ? beta_df : nullptr, k);
+                    GLOBE_LAUNCHED(ctx, "k_pcg_beta_shift");
+                    return GLOBE_OK;
+                };
+                int64_t per_it = 0;
+                bool ran = false;
+                GLOBE_RET(run_device_loop(ctx, loop_body, &per_it, &ran));
+                if (ran) {
+                    PcgLoopState st;
+                    double* h_scr = ctx->hpin + 3 * k;   // k doubles: the final r'r
+                    GLOBE_CK(ctx, cudaMemcpyAsync(&st, dstate, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+                    GLOBE_CK(ctx, cudaMemcpyAsync(h_scr, rr, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+                    GLOBE_CK(ctx, cudaMemcpyAsync(h_pvp, pvp, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx->stream));
+                    GLOBE_CK(ctx, cudaStreamSynchronize(ctx->stream));
+                    if (st.it > 1) {   // the loop ran (see run_device_loop)
+                        ctx->launches += per_it * (st.it - 1) + 1;
+                        ctx->device_loop_runs += 1;
+                        rhs_iters += st.rhs_iters;
+                        for (int j : cols) nr[j] = std::sqrt(h_scr[j]) * unsc[j];
+                        if (st.status == 4)
+                            return set_err(ctx, GLOBE_ERR_NUMERIC,
+                                           "PCG breakdown in column %d at iteration %d (p'Vp = %g)", st.err_col, st.it,
+                                           h_pvp[st.err_col] * unsc[st.err_col] * unsc[st.err_col]);
+                        converged = st.status == 1;
+                        stagnated = st.status == 2;
+                        it = st.it;
+                        break;
+                    }
+                }
+                use_graph = use_graph && ran;
+            }
         }
+        return GLOBE_OK;
+    };
+    const int rc = iterate();
+    if (df) {   // x back to FP64, whatever ended the loop (an earlier error's message is kept)
+        const std::string e0 = ctx->err;
+        const int rc2 = cols_from_df(ctx, X, n, k, bb);
+        if (rc != GLOBE_OK) ctx->err = e0;
+        else if (rc2 != GLOBE_OK) return rc2;
     }
+    if (rc != GLOBE_OK) return rc;
     if (info) {
         info->iters = it;
         info->inner_iters = it;

@@ -247,6 +247,23 @@ int globe_set_device_loop(globe_ctx* ctx, int on);
 int globe_get_device_loop(const globe_ctx* ctx);
 int64_t globe_device_loop_runs(const globe_ctx* ctx);
 
+/* Double-float record kernels of GLOBE_PREC_MIXED solves (on = 1, the default;
+ * 0 = FP64).  The block PCG's record-level vectors (x, r, z, p, Vp) are held
+ * as pairs of FP32 numbers (about 48 significant bits) from the end of its
+ * FP64 set-up to the end of the solve, and the iteration's segment sums,
+ * operator assembly and update run on the FP32 pipe; the GRM product's input
+ * and output, the per-column scalars and the dot products past each CTA stay
+ * FP64.  Each column runs scaled by a power of two to a unit-size right-hand
+ * side (exact), and x is returned in FP64.  A solve keeps the FP64 kernels
+ * when sig2e lies outside [2^-30, 2^30], another component or a time exceeds
+ * 2^30 in magnitude, or a right-hand side is not finite.
+ * globe_record_df_solves counts the solves that used them.  FP64 solves
+ * (GLOBE_PREC_FP64) never do.  No reference counterpart: the reference's
+ * record loops run in its build's floating type (PCGsolver.cpp:1095-1266). */
+int globe_set_record_df(globe_ctx* ctx, int on);
+int globe_get_record_df(const globe_ctx* ctx);
+int64_t globe_record_df_solves(const globe_ctx* ctx);
+
 /* Autotuning of the tensor-core genotype product (on = 1, the default; 0 =
  * the analytic choices only).  On first use of a shape in the process --
  * outside graph capture and event profiling -- the product times its

@@ -192,15 +192,19 @@ void orc_grm_apply(orc_solver* s, const double* Z, int k, double* out) {
         const int64_t Mk = m->Mk;
         if (Mk == 0) return;
         double* W = (double*)calloc((size_t)Mk * k, sizeof(double));
+        /* columns in groups of 256 (the accumulator); each column's sum runs in i order */
+        for (int c0 = 0; c0 < k; c0 += 256) {
+            const int kc = k - c0 < 256 ? k - c0 : 256;
 #pragma omp parallel for schedule(dynamic, 64)
-        for (int64_t sn = 0; sn < Mk; ++sn) {
-            double acc[256];
-            for (int c = 0; c < k; ++c) acc[c] = 0.0;
-            for (int32_t i = 0; i < N; ++i) {
-                double z = zs_of(m, sn, i);
-                for (int c = 0; c < k; ++c) acc[c] += z * Z[(size_t)c * N + i];
+            for (int64_t sn = 0; sn < Mk; ++sn) {
+                double acc[256];
+                for (int c = 0; c < kc; ++c) acc[c] = 0.0;
+                for (int32_t i = 0; i < N; ++i) {
+                    double z = zs_of(m, sn, i);
+                    for (int c = 0; c < kc; ++c) acc[c] += z * Z[(size_t)(c0 + c) * N + i];
+                }
+                for (int c = 0; c < kc; ++c) W[(size_t)(c0 + c) * Mk + sn] = acc[c];
             }
-            for (int c = 0; c < k; ++c) W[(size_t)c * Mk + sn] = acc[c];
         }
         const double scale = s2g * (1.0 / (double)Mk);
 #pragma omp parallel

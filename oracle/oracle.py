@@ -217,6 +217,8 @@ def ref_vx_f32(indiv, times, packed_kept, maf_kept, vc, x, N):
     maf = np.ascontiguousarray(maf_kept, np.float32)
     v = np.ascontiguousarray(vc, np.float32)
     x = np.asfortranarray(np.atleast_2d(x.T).T, np.float32)
+    if x.shape[1] > 256:
+        raise ValueError("the FP32 reference-structure port takes at most 256 columns")
     out = np.zeros_like(x, order="F")
     lib().orc_ref_vx_f32(C.c_int32(N), C.c_int64(len(indiv)), _p(indiv, C.c_int32), _p(times, C.c_float),
                          _p(g, C.c_uint8), C.c_int64(g.shape[0]), C.c_int64(g.shape[1]), _p(maf, C.c_float),
