@@ -304,9 +304,10 @@ struct DfCols {   // up to 4 (source, destination) column blocks; unused destina
     const double* src[4] = {nullptr, nullptr, nullptr, nullptr};
     double* dst[4] = {nullptr, nullptr, nullptr, nullptr};
 };
-int cols_to_df(globe_ctx* ctx, const DfCols& v, int64_t n, int k, const double* bb, double* rz);
+int col_unscales(globe_ctx* ctx, const double* bb, int k, double* unsc);   // unsc[c] = col_unscale(bb[c])
+int cols_to_df(globe_ctx* ctx, const DfCols& v, int64_t n, int k, const double* unsc, double* rz);
 int precond_apply_df(globe_ctx* ctx, const float2* H, const float2* r, float2* z, int k, double* rz);
-int cols_from_df(globe_ctx* ctx, double* v, int64_t n, int k, const double* bb);
+int cols_from_df(globe_ctx* ctx, double* v, int64_t n, int k, const double* unsc);
 int seg_sums_df(globe_ctx* ctx, float2* x, const float2* z, const float2* beta, const int32_t* cols, int kact,
                 double* Zi, float2* S0, float2* S1);
 int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const float2* S0, const float2* S1,

@@ -26,7 +26,10 @@ using df::D;
 
 // records per step of the thread-per-block loops: their loads issue together, ahead of the
 // arithmetic, so that each thread keeps several loads in flight (the kernels wait on memory)
-constexpr int RU = 4;
+#ifndef REC_DF_RU
+#define REC_DF_RU 4
+#endif
+constexpr int RU = REC_DF_RU;
 
 struct VCdf {
     D e, b0, b01, b1;
@@ -62,15 +65,22 @@ __global__ void k_to_df(const double* __restrict__ in, int64_t n, float2* __rest
         df::store(out + e, df::from_double_scaled(in[e], 0));
 }
 
-// column c (n rows, grid.y) of each pair with a destination: dst <- df(src s_c), src == dst
-// allowed (each element is read and written by one thread); rz[c] *= s_c^2.  The scale
-// exponent is computed once per CTA.
-__global__ void k_cols_to_df(DfCols v, int64_t n, const double* __restrict__ bb, double* __restrict__ rz) {
+// unsc[c] = col_unscale(bb[c]), once per solve
+__global__ void k_col_unscale(const double* __restrict__ bb, int k, double* __restrict__ unsc) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < k) unsc[c] = col_unscale(bb[c]);
+}
+
+// 2^-e for the power of two u = 2^e, from its exponent bits
+__device__ __forceinline__ int neg_exp2(double u) {
+    return 1023 - (int)((__double_as_longlong(u) >> 52) & 0x7ff);
+}
+
+// column c (n rows, grid.y) of each pair with a destination: dst <- df(src / unsc[c]), src ==
+// dst allowed (each element is read and written by one thread); rz[c] /= unsc[c]^2
+__global__ void k_cols_to_df(DfCols v, int64_t n, const double* __restrict__ unsc, double* __restrict__ rz) {
     const int c = blockIdx.y;
-    __shared__ int sh_s;
-    if (threadIdx.x == 0) sh_s = -col_scale_exp(bb[c]);
-    __syncthreads();
-    const int sh = sh_s;
+    const int sh = neg_exp2(unsc[c]);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (!v.dst[j]) continue;
@@ -82,20 +92,18 @@ __global__ void k_cols_to_df(DfCols v, int64_t n, const double* __restrict__ bb,
     if (rz && blockIdx.x == 0 && threadIdx.x == 0) rz[c] = ldexp(rz[c], 2 * sh);
 }
 
-// in place, column c: v <- double(v) / s_c
-__global__ void k_cols_from_df(double* v, int64_t n, const double* __restrict__ bb) {
+// in place, column c: v <- double(v) unsc[c]
+__global__ void k_cols_from_df(double* v, int64_t n, const double* __restrict__ unsc) {
     const int c = blockIdx.y;
-    __shared__ double u_s;
-    if (threadIdx.x == 0) u_s = col_unscale(bb[c]);
-    __syncthreads();
-    const double u = u_s;
+    const double u = unsc[c];
     double* vc = v + (size_t)c * n;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         vc[e] = df::to_double(df::load(reinterpret_cast<const float2*>(vc + e))) * u;
 }
 
+// CTAs per column of the conversions: ~4 elements per thread
 static unsigned grid_for(int64_t n) {
-    const int64_t b = (n + 255) / 256;
+    const int64_t b = (n + 1023) / 1024;
     return (unsigned)(b < 1 ? 1 : (b > 1024 ? 1024 : b));
 }
 
@@ -106,14 +114,20 @@ int to_df(globe_ctx* ctx, const double* in, int64_t n, float2* out) {
     return GLOBE_OK;
 }
 
-int cols_to_df(globe_ctx* ctx, const DfCols& v, int64_t n, int k, const double* bb, double* rz) {
-    k_cols_to_df<<<dim3(grid_for(n), k), 256, 0, ctx->stream>>>(v, n, bb, rz);
+int col_unscales(globe_ctx* ctx, const double* bb, int k, double* unsc) {
+    k_col_unscale<<<div_up(k, 128), 128, 0, ctx->stream>>>(bb, k, unsc);
+    GLOBE_LAUNCHED(ctx, "k_col_unscale");
+    return GLOBE_OK;
+}
+
+int cols_to_df(globe_ctx* ctx, const DfCols& v, int64_t n, int k, const double* unsc, double* rz) {
+    k_cols_to_df<<<dim3(grid_for(n), k), 256, 0, ctx->stream>>>(v, n, unsc, rz);
     GLOBE_LAUNCHED(ctx, "k_cols_to_df");
     return GLOBE_OK;
 }
 
-int cols_from_df(globe_ctx* ctx, double* v, int64_t n, int k, const double* bb) {
-    k_cols_from_df<<<dim3(grid_for(n), k), 256, 0, ctx->stream>>>(v, n, bb);
+int cols_from_df(globe_ctx* ctx, double* v, int64_t n, int k, const double* unsc) {
+    k_cols_from_df<<<dim3(grid_for(n), k), 256, 0, ctx->stream>>>(v, n, unsc);
     GLOBE_LAUNCHED(ctx, "k_cols_from_df");
     return GLOBE_OK;
 }

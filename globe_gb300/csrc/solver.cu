@@ -167,7 +167,7 @@ __global__ void k_pcg_loop_arm(cudaGraphConditionalHandle h) { cudaGraphSetCondi
 // the host loop's stopping rule (pcg_run) on the device: one thread, after iteration st->it + 1
 __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restrict__ pvp,
                             const double* __restrict__ bb, const int32_t* __restrict__ cols, int kact, int k,
-                            double tol, int rule, int maxit, int scaled, PcgLoopState* st,
+                            double tol, int rule, int maxit, const double* __restrict__ unsc, PcgLoopState* st,
                             cudaGraphConditionalHandle h) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int it = st->it + 1;
@@ -188,7 +188,7 @@ __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restr
         double mx = 0.0;
         for (int j = 0; j < k; ++j) {
             const double nb = sqrt(bb[j]);
-            const double u = scaled ? col_unscale(bb[j]) : 1.0;
+            const double u = unsc ? unsc[j] : 1.0;
             const double q = nb > small_b ? sqrt(rr[j]) * u / nb : 0.0;
             if (q > mx) mx = q;
         }
@@ -208,7 +208,7 @@ __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restr
     } else {
         bool all = true;
         for (int j = 0; j < k; ++j)
-            if (bb[j] > 0.0 && !(sqrt(rr[j]) * (scaled ? col_unscale(bb[j]) : 1.0) < tol * sqrt(bb[j]))) {
+            if (bb[j] > 0.0 && !(sqrt(rr[j]) * (unsc ? unsc[j] : 1.0) < tol * sqrt(bb[j]))) {
                 all = false;
                 break;
             }
@@ -345,6 +345,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     double* beta = scal + 4 * k;
     double* rr = scal + 5 * k;
     double* bb = scal + 6 * k;
+    double* dunsc = scal + 7 * k;   // per-column unscale factors of a double-float solve
     float2* alpha_df = reinterpret_cast<float2*>(scal + 8 * k);   // double-float copies of alpha, beta
     float2* beta_df = reinterpret_cast<float2*>(scal + 9 * k);
     if ((size_t)4 * k > ctx->hpin_n) return set_err(ctx, GLOBE_ERR_ARG, "too many right-hand sides (%d)", k);
@@ -366,6 +367,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     auto F = [](double* v) { return reinterpret_cast<float2*>(v); };
 
     GLOBE_RET(col_dots(ctx, B, B, n, n, n, nullptr, k, bb));
+    if (df) GLOBE_RET(col_unscales(ctx, bb, k, dunsc));
     switch (o->x0mode) {
         case GLOBE_X0_ZERO:
             GLOBE_CK(ctx, cudaMemsetAsync(X, 0, sizeof(double) * n * k, ctx->stream));
@@ -373,7 +375,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
                 DfCols v;
                 v.src[0] = B;
                 v.dst[0] = r;
-                GLOBE_RET(cols_to_df(ctx, v, n, k, bb, nullptr));
+                GLOBE_RET(cols_to_df(ctx, v, n, k, dunsc, nullptr));
             } else {
                 GLOBE_CK(ctx, cudaMemcpyAsync(r, B, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, ctx->stream));
             }
@@ -429,7 +431,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
             DfCols v;
             double* vv[4] = {X, r, z, p};
             for (int j = 0; j < 4; ++j) v.src[j] = v.dst[j] = vv[j];
-            GLOBE_RET(cols_to_df(ctx, v, n, k, bb, rz));
+            GLOBE_RET(cols_to_df(ctx, v, n, k, dunsc, rz));
         }
         ctx->record_df_runs += 1;
     }
@@ -535,7 +537,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
                 auto loop_body = [&](cudaGraphConditionalHandle h) -> int {
                     GLOBE_RET(iteration(false, kc));
                     k_pcg_check<<<1, 32, 0, ctx->stream>>>(rr, pvp, bb, dcols, kc, k, o->tol, o->rule, o->maxit,
-                                                           df ? 1 : 0, dstate, h);
+                                                           df ? dunsc : nullptr, dstate, h);
                     GLOBE_LAUNCHED(ctx, "k_pcg_check");
                     k_pcg_beta_shift<<<div_up(k, 128), 128, 0, ctx->stream>>>(rz, rz2, beta, df ? beta_df : nullptr, k);
                     GLOBE_LAUNCHED(ctx, "k_pcg_beta_shift");
@@ -574,7 +576,7 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
     const int rc = iterate();
     if (df) {   // x back to FP64, whatever ended the loop (an earlier error's message is kept)
         const std::string e0 = ctx->err;
-        const int rc2 = cols_from_df(ctx, X, n, k, bb);
+        const int rc2 = cols_from_df(ctx, X, n, k, dunsc);
         if (rc != GLOBE_OK) ctx->err = e0;
         else if (rc2 != GLOBE_OK) return rc2;
     }
