@@ -55,7 +55,7 @@ __global__ void k_grm_table(const double* __restrict__ U4, const double* __restr
         double cv = 0.0;
         if (s < Mk) {
             long long I = __double2ll_rn(U4[x] * sc);
-            cv = 2.0 * f[s] * ((double)I * back);
+            cv = 2.0 * f[s] * ll_times_pow2(I, back);
             uint32_t b[NDIG];
             const int mult = geno_digit_mult(s);   // even SNPs: 4 d (their genotypes decode to 2^-9 g)
 #pragma unroll

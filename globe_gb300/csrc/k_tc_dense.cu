@@ -283,7 +283,7 @@ __global__ void k_dense_combine(const float* __restrict__ part, int nsplit, int 
         for (int q = 0; q < 3; ++q)
 #pragma unroll
             for (int m = 0; m < 5; ++m) C[q] = C[q] * 32 + (5 * q + m < NT ? T[5 * q + m] : 0);
-        const double v = s0 * ((double)C[0] + ldexp((double)C[1], -25) + ldexp((double)C[2], -50));
+        const double v = s0 * (ll_times_pow2(C[0], 1.0) + ll_times_pow2(C[1], 0x1p-25) + ll_times_pow2(C[2], 0x1p-50));
         out[i + c * ldo] = bad ? colinfo[2 * c + 1] : v;
     }
 }

@@ -361,7 +361,7 @@ __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld
     double mx = 0, sm = 0;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
         const double v = X[r + c * ld];
-        mx = fmax(mx, fabs(v));
+        mx = absmax_bits(mx, v);
         sm += v;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -428,7 +428,7 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
         const double iv = inv[s], fs = f[s];
         const double u = iv * iv * (gv - 2.0 * fs * Sc);
         U[s + c * rows] = u;
-        mx = fmax(mx, fabs(u));
+        mx = absmax_bits(mx, u);
         sm += 2.0 * fs * u;
     }
     for (int o = 16; o > 0; o >>= 1) {

@@ -81,6 +81,33 @@ __device__ __forceinline__ uint32_t e4m3_int(int d) {   // d in [-16, 16], or 4x
     return (uint32_t)__nv_cvt_float_to_fp8((float)d, __NV_SATFINITE, __NV_E4M3);
 }
 
+// Exact int64 -> FP64 conversion scaled by a power of two, from the bits: GB300's FP64 pipe,
+// which also runs its int64 -> FP64 conversion instruction, is small, and the recombinations
+// convert two or three integers per value.  It gives the bits of the FP64 route it replaces.
+// (The digit kernels' FP64 -> int64 rounding stays on the conversion instruction: an integer
+// form of it measured slower there.)
+
+// v s for |v| < 2^53 and s a power of two: (double)v * s, built from the bits when the result
+// is a normal double (both the conversion and the product are exact then), else computed so
+__device__ __forceinline__ double ll_times_pow2(long long v, double s) {
+    if (v == 0) return 0.0;
+    const int es = (int)((__double_as_longlong(s) >> 52) & 0x7ff);
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    const int msb = 63 - __clzll((long long)a);
+    const int ex = es + msb;   // biased exponent of v s
+    if (es == 0 || msb > 52 || ex <= 0 || ex >= 2047) return (double)v * s;
+    const unsigned long long mant = (a << (52 - msb)) & 0xfffffffffffffull;
+    return __longlong_as_double((long long)((v < 0 ? 0x8000000000000000ull : 0ull) | ((unsigned long long)ex << 52) |
+                                            mant));
+}
+
+// max(m, |v|) for m >= 0 by comparing bits (non-negative doubles order as integers; a NaN v
+// wins, where fmax would drop it -- the column sums carry NaN either way)
+__device__ __forceinline__ double absmax_bits(double m, double v) {
+    const long long a = __double_as_longlong(m), b = __double_as_longlong(v) & 0x7fffffffffffffffll;
+    return __longlong_as_double(a > b ? a : b);
+}
+
 // 2^e sum_j 32^-j P_j of one row of a genotype product, ND digits per column (rows c*ND + j
 // of the partials).  Every FP32 partial is an exact multiple of 2^-7 (|P| < 2^17), so it is
 // scaled to an integer, the split partials are summed in int64 and the digits combined in two
@@ -104,7 +131,7 @@ __device__ __forceinline__ double recombine(const float* __restrict__ part, int 
     for (int j = 0; j < NH; ++j) hi = hi * (1 << DBITS) + pj[j];
 #pragma unroll
     for (int j = NH; j < ND; ++j) lo = lo * (1 << DBITS) + pj[j];
-    return (double)hi * s_hi + (double)lo * s_lo;
+    return ll_times_pow2(hi, s_hi) + ll_times_pow2(lo, s_lo);
 }
 
 // scale factors of recombine<ND> for exponent e: 2^(e - 5 (ND_HI - 1)) and 2^(e - 5 (ND - 1))
