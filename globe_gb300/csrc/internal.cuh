@@ -274,8 +274,10 @@ int block_moments(globe_ctx* ctx);
 int build_H(globe_ctx* ctx, const double* gdiag, double gconst, double* H, float2* Hdf = nullptr);
 int seg_sums(globe_ctx* ctx, const double* x, const double* z, const double* beta, double* xout,
              const int32_t* cols, int kact, double* Zi, double* S1);
+// with dot_out and quot: also quot[col] = num[col] / dot_out[col] (the step length, fused)
 int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double* Zi,
-                const double* S1, const int32_t* cols, int kact, double* out, double* dot_out);
+                const double* S1, const int32_t* cols, int kact, double* out, double* dot_out,
+                const double* num = nullptr, double* quot = nullptr);
 int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, double* r,
                const double* p, const double* Vp, double* z, const int32_t* cols, int kact,
                double* rr, double* rz);
@@ -311,7 +313,8 @@ int cols_from_df(globe_ctx* ctx, double* v, int64_t n, int k, const double* unsc
 int seg_sums_df(globe_ctx* ctx, float2* x, const float2* z, const float2* beta, const int32_t* cols, int kact,
                 double* Zi, float2* S0, float2* S1);
 int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const float2* S0, const float2* S1,
-                   const int32_t* cols, int kact, float2* out, double* dot_out);
+                   const int32_t* cols, int kact, float2* out, double* dot_out, const double* num = nullptr,
+                   double* quot = nullptr, float2* quot_df = nullptr);
 int pcg_update_df(globe_ctx* ctx, const float2* H, const float2* alpha, float2* x, float2* r, const float2* p,
                   const float2* Vp, float2* z, const int32_t* cols, int kact, double* rr, double* rz);
 
@@ -347,5 +350,9 @@ int vx_dev(globe_ctx* ctx, const double* x, int k, double* out);
 int pcg_dev(globe_ctx* ctx, const double* B, double* X, int k, const globe_pcg_opts* o,
             globe_pcg_info* info);
 int reduce_cols(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out);
+int reduce_cols2(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out0,
+                 double* out1);
+int reduce_cols_div(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out,
+                    const double* num, double* quot, float2* quot_df);
 
 }  // namespace globe

@@ -316,7 +316,7 @@ __global__ void k_vx_assemble_t(int32_t nblk, int64_t ld, int32_t N, const int32
 }
 
 int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double* Zi, const double* S1,
-                const int32_t* cols, int kact, double* out, double* dot_out) {
+                const int32_t* cols, int kact, double* out, double* dot_out, const double* num, double* quot) {
     auto& c = ctx->coh;
     VC v{ctx->vc[0], ctx->vc[1], ctx->vc[2], ctx->vc[3], ctx->vc[4]};
     const RecShape rs = rec_shape(ctx);
@@ -331,7 +331,7 @@ int vx_assemble(globe_ctx* ctx, const double* x, const double* GZ, const double*
                                                                 rs.S);
         GLOBE_LAUNCHED(ctx, "k_vx_assemble");
     }
-    if (dot_out) GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, dot_out));
+    if (dot_out) GLOBE_RET(reduce_cols_div(ctx, part, rs.S, kact, cols, dot_out, num, quot, nullptr));
     return GLOBE_OK;
 }
 
@@ -463,9 +463,7 @@ int pcg_update(globe_ctx* ctx, const double* H, const double* alpha, double* x, 
                                                                rs.nbt, rs.S);
         GLOBE_LAUNCHED(ctx, "k_pcg_update");
     }
-    GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, rr));
-    GLOBE_RET(reduce_cols(ctx, part + (size_t)rs.S * kact, rs.S, kact, cols, rz));
-    return GLOBE_OK;
+    return reduce_cols2(ctx, part, rs.S, kact, cols, rr, rz);
 }
 
 // z = Q^-1 r (+ partial r'z)
@@ -611,12 +609,22 @@ int precond_apply_scratch(globe_ctx* ctx, const double* H, const double* r, doub
 // ---------------------------------------------------------------------------
 // Column reductions
 
-// part[j + c*nparts], j < nparts  ->  out[cols ? cols[c] : c]
-__global__ void k_reduce_cols(const double* __restrict__ part, int nparts, const int32_t* __restrict__ cols,
-                              double* __restrict__ out) {
+// Quantity y (grid.y) of column c (grid.x): part[y * qstride + j + c*nparts], j < nparts,
+// summed into o.out[y][cols ? cols[c] : c]; with o.quot, also o.quot[col] = o.num[col] / sum
+// (0 where the sum is 0) and its double-float copy o.quot_df -- the step length
+// alpha = r'z / p'Vp fused into the p'Vp reduction.
+struct ReduceOut {
+    double* out[2] = {nullptr, nullptr};
+    const double* num = nullptr;
+    double* quot = nullptr;
+    float2* quot_df = nullptr;
+};
+
+__global__ void k_reduce_cols(const double* __restrict__ part, int nparts, size_t qstride,
+                              const int32_t* __restrict__ cols, ReduceOut o) {
     __shared__ double sm[256];
     const int c = blockIdx.x;
-    const double* pc = part + (size_t)c * nparts;
+    const double* pc = part + blockIdx.y * qstride + (size_t)c * nparts;
     double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
     int j = threadIdx.x;
     for (; j + 3 * (int)blockDim.x < nparts; j += 4 * blockDim.x) {
@@ -632,12 +640,47 @@ __global__ void k_reduce_cols(const double* __restrict__ part, int nparts, const
         if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[cols ? cols[c] : c] = sm[0];
+    if (threadIdx.x == 0) {
+        const int col = cols ? cols[c] : c;
+        const double v = sm[0];
+        o.out[blockIdx.y][col] = v;
+        if (o.quot) {
+            const double q = (v != 0.0) ? o.num[col] / v : 0.0;
+            o.quot[col] = q;
+            if (o.quot_df) df::store(o.quot_df + col, df::from_double(q));
+        }
+    }
 }
 
 // out[cols ? cols[c] : c] = sum_j part[j + c*nparts]
 int reduce_cols(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out) {
-    k_reduce_cols<<<kact, 256, 0, ctx->stream>>>(part, nparts, cols, out);
+    ReduceOut o;
+    o.out[0] = out;
+    k_reduce_cols<<<kact, 256, 0, ctx->stream>>>(part, nparts, 0, cols, o);
+    GLOBE_LAUNCHED(ctx, "k_reduce_cols");
+    return GLOBE_OK;
+}
+
+// two quantities of kact columns each (the second's partials follow the first's), one launch
+int reduce_cols2(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out0,
+                 double* out1) {
+    ReduceOut o;
+    o.out[0] = out0;
+    o.out[1] = out1;
+    k_reduce_cols<<<dim3(kact, 2), 256, 0, ctx->stream>>>(part, nparts, (size_t)nparts * kact, cols, o);
+    GLOBE_LAUNCHED(ctx, "k_reduce_cols");
+    return GLOBE_OK;
+}
+
+// out as reduce_cols, and quot[col] = num[col] / out[col] (0 where out is 0), quot_df its copy
+int reduce_cols_div(globe_ctx* ctx, const double* part, int nparts, int kact, const int32_t* cols, double* out,
+                    const double* num, double* quot, float2* quot_df) {
+    ReduceOut o;
+    o.out[0] = out;
+    o.num = num;
+    o.quot = quot;
+    o.quot_df = quot_df;
+    k_reduce_cols<<<kact, 256, 0, ctx->stream>>>(part, nparts, 0, cols, o);
     GLOBE_LAUNCHED(ctx, "k_reduce_cols");
     return GLOBE_OK;
 }

@@ -352,7 +352,8 @@ static VCdf vc_df(const globe_ctx* ctx) {
 }
 
 int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const float2* S0, const float2* S1,
-                   const int32_t* cols, int kact, float2* out, double* dot_out) {
+                   const int32_t* cols, int kact, float2* out, double* dot_out, const double* num, double* quot,
+                   float2* quot_df) {
     auto& c = ctx->coh;
     const VCdf v = vc_df(ctx);
     const RecShape rs = rec_shape(ctx);
@@ -367,7 +368,7 @@ int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const floa
                                                                    rs.S);
         GLOBE_LAUNCHED(ctx, "k_vx_assemble_df");
     }
-    if (dot_out) GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, dot_out));
+    if (dot_out) GLOBE_RET(reduce_cols_div(ctx, part, rs.S, kact, cols, dot_out, num, quot, quot_df));
     return GLOBE_OK;
 }
 
@@ -523,9 +524,7 @@ int pcg_update_df(globe_ctx* ctx, const float2* H, const float2* alpha, float2* 
                                                                   r, p, Vp, z, cols, kact, part, c.lblk, rs.nbt, rs.S);
         GLOBE_LAUNCHED(ctx, "k_pcg_update_df");
     }
-    GLOBE_RET(reduce_cols(ctx, part, rs.S, kact, cols, rr));
-    GLOBE_RET(reduce_cols(ctx, part + (size_t)rs.S * kact, rs.S, kact, cols, rz));
-    return GLOBE_OK;
+    return reduce_cols2(ctx, part, rs.S, kact, cols, rr, rz);
 }
 
 // ---------------------------------------------------------------------------

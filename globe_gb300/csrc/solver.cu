@@ -145,8 +145,8 @@ static bool capture_body(globe_ctx* ctx, int slot, F&& body, int64_t* nlaunch) {
 //
 // One graph: a kernel that arms a WHILE conditional node, then the node, whose body is
 // one iteration (the same kernels, in the same order, as a host-driven iteration) followed
-// by k_pcg_check, which applies the stopping rule of the host loop below to the device
-// copies of r'r and p'Vp and sets the node's condition, and by the beta / r'z shift.
+// by k_pcg_check_shift, which applies the stopping rule of the host loop below to the device
+// copies of r'r and p'Vp, sets the node's condition, and shifts beta / r'z.
 // So the iterations run without a host synchronisation each, with bit-identical
 // results and iteration counts.  The condition's launch default is 0: only the arming
 // kernel opens the loop, so a condition that could not be set leaves the loop unrun
@@ -165,11 +165,10 @@ struct PcgLoopState {
 __global__ void k_pcg_loop_arm(cudaGraphConditionalHandle h) { cudaGraphSetConditional(h, 1u); }
 
 // the host loop's stopping rule (pcg_run) on the device: one thread, after iteration st->it + 1
-__global__ void k_pcg_check(const double* __restrict__ rr, const double* __restrict__ pvp,
-                            const double* __restrict__ bb, const int32_t* __restrict__ cols, int kact, int k,
-                            double tol, int rule, int maxit, const double* __restrict__ unsc, PcgLoopState* st,
-                            cudaGraphConditionalHandle h) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void pcg_check(const double* __restrict__ rr, const double* __restrict__ pvp,
+                          const double* __restrict__ bb, const int32_t* __restrict__ cols, int kact, int k,
+                          double tol, int rule, int maxit, const double* __restrict__ unsc, PcgLoopState* st,
+                          cudaGraphConditionalHandle h) {
     const int it = st->it + 1;
     st->it = it;
     st->rhs_iters += kact;
@@ -224,10 +223,17 @@ __global__ void k_pcg_check(const double* __restrict__ rr, const double* __restr
     cudaGraphSetConditional(h, stop ? 0u : 1u);
 }
 
-// beta = r'z(new) / r'z(old) (0 where r'z(old) = 0, as k_scal_div), then r'z(old) = r'z(new)
-// (and beta's double-float copy when beta_df is given)
-__global__ void k_pcg_beta_shift(double* __restrict__ rz, const double* __restrict__ rz2, double* __restrict__ beta,
-                                 float2* __restrict__ beta_df, int k) {
+// The end of a device-loop iteration, one launch: thread 0 applies the stopping rule
+// (pcg_check); every column c < k takes beta = r'z(new) / r'z(old) (0 where r'z(old) = 0, as
+// k_scal_div) and its double-float copy when beta_df is given, then r'z(old) = r'z(new).
+// The check reads r'r and p'Vp only, so the two parts are independent.
+__global__ void k_pcg_check_shift(const double* __restrict__ rr, const double* __restrict__ pvp,
+                                  const double* __restrict__ bb, const int32_t* __restrict__ cols, int kact, int k,
+                                  double tol, int rule, int maxit, const double* __restrict__ unsc, PcgLoopState* st,
+                                  cudaGraphConditionalHandle h, double* __restrict__ rz,
+                                  const double* __restrict__ rz2, double* __restrict__ beta,
+                                  float2* __restrict__ beta_df) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) pcg_check(rr, pvp, bb, cols, kact, k, tol, rule, maxit, unsc, st, h);
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < k) {
         const double o = rz[c], nw = rz2[c];
@@ -441,15 +447,13 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
             GLOBE_RET(seg_sums_df(ctx, F(p), first ? nullptr : F(z), first ? nullptr : beta_df, dcols, kc, Zi, S0df,
                                   F(S1)));
             GLOBE_RET(grm_apply_dev(ctx, Zi, kc, GZ));
-            GLOBE_RET(vx_assemble_df(ctx, F(p), GZ, S0df, F(S1), dcols, kc, F(Vp), pvp));
-            GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k, alpha_df));
+            GLOBE_RET(vx_assemble_df(ctx, F(p), GZ, S0df, F(S1), dcols, kc, F(Vp), pvp, rz, alpha, alpha_df));
             return pcg_update_df(ctx, Hdf, alpha_df, F(X), F(r), F(p), F(Vp), F(z), dcols, kc, rr, rz2);
         }
         if (!first) GLOBE_RET(seg_sums(ctx, p, z, beta, p, dcols, kc, Zi, S1));
         else GLOBE_RET(seg_sums(ctx, p, nullptr, nullptr, nullptr, dcols, kc, Zi, S1));
         GLOBE_RET(grm_apply_dev(ctx, Zi, kc, GZ));
-        GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kc, Vp, pvp));
-        GLOBE_RET(scal_alpha(ctx, rz, pvp, alpha, k));
+        GLOBE_RET(vx_assemble(ctx, p, GZ, Zi, S1, dcols, kc, Vp, pvp, rz, alpha));   // alpha = r'z / p'Vp
         return pcg_update(ctx, H, alpha, X, r, p, Vp, z, dcols, kc, rr, rz2);
     };
 
@@ -536,11 +540,10 @@ static int pcg_run(globe_ctx* ctx, const double* B, double* X, int k, const glob
                 const int kc = kact;
                 auto loop_body = [&](cudaGraphConditionalHandle h) -> int {
                     GLOBE_RET(iteration(false, kc));
-                    k_pcg_check<<<1, 32, 0, ctx->stream>>>(rr, pvp, bb, dcols, kc, k, o->tol, o->rule, o->maxit,
-                                                           df ? dunsc : nullptr, dstate, h);
-                    GLOBE_LAUNCHED(ctx, "k_pcg_check");
-                    k_pcg_beta_shift<<<div_up(k, 128), 128, 0, ctx->stream>>>(rz, rz2, beta, df ? beta_df : nullptr, k);
-                    GLOBE_LAUNCHED(ctx, "k_pcg_beta_shift");
+                    k_pcg_check_shift<<<div_up(k, 128), 128, 0, ctx->stream>>>(
+                        rr, pvp, bb, dcols, kc, k, o->tol, o->rule, o->maxit, df ? dunsc : nullptr, dstate, h, rz, rz2,
+                        beta, df ? beta_df : nullptr);
+                    GLOBE_LAUNCHED(ctx, "k_pcg_check_shift");
                     return GLOBE_OK;
                 };
                 int64_t per_it = 0;
