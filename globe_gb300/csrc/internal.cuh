@@ -87,7 +87,7 @@ enum SlotId {
     WS_R, WS_Z, WS_P, WS_VP, WS_ZI, WS_GZ, WS_S1, WS_PART, WS_SCAL, WS_COLS, WS_W,
     WS_GPART, WS_B, WS_TMP1, WS_TMP2, WS_TMP3, WS_TMP4, WS_H, WS_HSTAR, WS_PROBE,
     WS_UH, WS_SMALL, WS_IO1, WS_IO2, WS_BHAT, WS_FB, WS_FX,
-    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_LOOP, WS_S0DF, WS_HDF, WS_COUNT
+    WS_TC_D1, WS_TC_D2, WS_TC_P1, WS_TC_P2, WS_TC_U, WS_TC_SCAL, WS_TC_ERR, WS_LOOP, WS_S0DF, WS_HDF, WS_TC_CNT, WS_COUNT
 };
 
 // Scalars kept on the device during a solve (per column, k entries each).
@@ -339,6 +339,7 @@ int load_bed_rows(globe_ctx* ctx, const uint8_t* d_bed, int64_t M, int64_t strid
 int geno_apply_tc(globe_ctx* ctx, const double* Z, int k, double scale, double* out);
 int tc_err_word(globe_ctx* ctx, unsigned** err);   // the kernels' timeout word (cleared when created)
 int tc_check_error(globe_ctx* ctx);                 // reads and clears it: GLOBE_ERR_CUDA if set
+int tc_counters(globe_ctx* ctx, size_t n, unsigned** cnt);   // >= n zeroed per-column arrival counts
 // rc of a call at `precision`, or the tensor-core timeout behind it (the root cause) if one was set
 int with_tc_check(globe_ctx* ctx, int precision, int rc);
 

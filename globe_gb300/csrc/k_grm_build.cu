@@ -354,7 +354,7 @@ static int grm_build_tc(globe_ctx* ctx, float* lt) {
     k_grm_u4<<<(unsigned)std::min<int64_t>(div_up(4 * g.Mk, 256), 4096), 256, 0, ctx->stream>>>(g.zs, g.inv, g.Mk,
                                                                                                  U4);
     GLOBE_LAUNCHED(ctx, "k_grm_u4");
-    k_col_maxsum<<<dim3(nbr, 1), 256, 0, ctx->stream>>>(U4, 4 * g.Mk, 4 * g.Mk, pm, ps);
+    k_col_maxsum<<<dim3(nbr, 1), 256, 0, ctx->stream>>>(U4, 4 * g.Mk, 4 * g.Mk, pm, ps, nullptr, nullptr);
     GLOBE_LAUNCHED(ctx, "k_col_maxsum");
     k_col_finish<<<1, 128, 0, ctx->stream>>>(pm, ps, nbr, 1, info);
     GLOBE_LAUNCHED(ctx, "k_col_finish");

@@ -432,10 +432,10 @@ static int dense_group(globe_ctx* ctx, const double* Z, int kg, double scale, do
     GLOBE_RET(make_map(ctx, &mA, g.adig, (uint64_t)np, (uint64_t)rows, BK, BM, true));
     GLOBE_RET(make_map(ctx, &mB, D, (uint64_t)np, (uint64_t)nmma, BK, (uint32_t)nmma, true));
     const int nz = col_parts(N);
-    k_col_maxsum<<<dim3(nz, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
+    unsigned* cnt;
+    GLOBE_RET(tc_counters(ctx, kg, &cnt));
+    k_col_maxsum<<<dim3(nz, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps, cnt, col);
     GLOBE_LAUNCHED(ctx, "k_col_maxsum");
-    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nz, kg, col);
-    GLOBE_LAUNCHED(ctx, "k_col_finish");
     if (nmma > kg * ND)   // digit rows past the kg columns stay zero
         GLOBE_CK(ctx, cudaMemsetAsync(D + (size_t)kg * ND * np, 0, (size_t)(nmma - kg * ND) * np, ctx->stream));
     k_digits<ND, false><<<dim3((unsigned)std::min<int64_t>(div_up(np / 4, 256), 1024), kg), 256, 0, ctx->stream>>>(

@@ -353,9 +353,65 @@ __global__ void __launch_bounds__(Geo<NMMA>::NTHREADS, 1)
 
 
 
-// per-column max |x| and sum over n rows (partials per CTA)
+// colinfo = {scale exponent e (as double), column sum} of one column from its nparts partials;
+// one warp (the lanes read the partials through L2, so a CTA that did not write them sees
+// them once their writers' fences are past)
+__device__ __forceinline__ void col_finish_warp(const double* __restrict__ pm, const double* __restrict__ ps,
+                                                int nparts, double* __restrict__ colinfo) {
+    const int lane = threadIdx.x & 31;
+    double mx = 0, sm = 0;
+    for (int j = lane; j < nparts; j += 32) {
+        mx = fmax(mx, __ldcg(pm + j));
+        sm += __ldcg(ps + j);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    }
+    if (lane == 0) {
+        // A column holding NaN or +-Inf has a non-finite sum (fmax drops NaN, the sum keeps it).
+        // It is marked by a NaN sum and a zero exponent: k_digits gives it zero digits, and every
+        // epilogue writes NaN for it (through the centring term, or explicitly), as FP64 would.
+        const bool bad = !isfinite(sm) || !isfinite(mx);
+        int E = 0;
+        if (!bad && mx > 0) frexp(mx, &E);
+        colinfo[0] = bad ? 0.0 : (double)(E - (DBITS - 1));  // |x 2^-e| < 16
+        colinfo[1] = bad ? __longlong_as_double(0x7ff8000000000000ll) : sm;
+    }
+}
+
+// colinfo[c] = {scale exponent e_c (as double), column sum} from partials; one warp per column
+__global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
+                             double* __restrict__ colinfo) {
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= k) return;
+    col_finish_warp(pmax + (size_t)c * nparts, psum + (size_t)c * nparts, nparts, colinfo + 2 * c);
+}
+
+// The same inside the kernel that wrote the partials: the last of the column's gridDim.x CTAs
+// to finish (a per-column arrival count, which that CTA resets for the next launch) forms
+// colinfo[c], in the same order as k_col_finish.  Every thread of the CTA calls it, after
+// thread 0 wrote the CTA's partials.
+__device__ __forceinline__ void col_finish_last(const double* __restrict__ pmax, const double* __restrict__ psum,
+                                                int c, unsigned* __restrict__ cnt, double* __restrict__ colinfo) {
+    __shared__ bool last;
+    const int nparts = (int)gridDim.x;
+    if (threadIdx.x == 0) {
+        __threadfence();   // this CTA's partials, then its arrival
+        last = atomicAdd(&cnt[c], 1u) == (unsigned)nparts - 1u;
+    }
+    __syncthreads();
+    if (last && threadIdx.x < 32) {
+        __threadfence();
+        col_finish_warp(pmax + (size_t)c * nparts, psum + (size_t)c * nparts, nparts, colinfo + 2 * c);
+        if (threadIdx.x == 0) cnt[c] = 0u;
+    }
+}
+
+// per-column max |x| and sum over n rows (partials per CTA); with colinfo, the last CTA of
+// each column also forms colinfo[c] (col_finish_last)
 __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld, double* __restrict__ pmax,
-                             double* __restrict__ psum) {
+                             double* __restrict__ psum, unsigned* __restrict__ cnt, double* __restrict__ colinfo) {
     __shared__ double smx[32], ssm[32];
     const int c = blockIdx.y;
     double mx = 0, sm = 0;
@@ -382,41 +438,16 @@ __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld
         pmax[blockIdx.x + (size_t)c * gridDim.x] = a;
         psum[blockIdx.x + (size_t)c * gridDim.x] = b;
     }
+    if (colinfo) col_finish_last(pmax, psum, c, cnt, colinfo);
 }
 
-// colinfo[c] = {scale exponent e_c (as double), column sum} from partials; one warp per column
-__global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
-                             double* __restrict__ colinfo) {
-    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (c >= k) return;
-    double mx = 0, sm = 0;
-    for (int j = lane; j < nparts; j += 32) {
-        mx = fmax(mx, pmax[j + (size_t)c * nparts]);
-        sm += psum[j + (size_t)c * nparts];
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        sm += __shfl_xor_sync(0xffffffffu, sm, o);
-    }
-    if (lane == 0) {
-        // A column holding NaN or +-Inf has a non-finite sum (fmax drops NaN, the sum keeps it).
-        // It is marked by a NaN sum and a zero exponent: k_digits gives it zero digits, and every
-        // epilogue writes NaN for it (through the centring term, or explicitly), as FP64 would.
-        const bool bad = !isfinite(sm) || !isfinite(mx);
-        int E = 0;
-        if (!bad && mx > 0) frexp(mx, &E);
-        colinfo[2 * c] = bad ? 0.0 : (double)(E - (DBITS - 1));  // |x 2^-e| < 16
-        colinfo[2 * c + 1] = bad ? __longlong_as_double(0x7ff8000000000000ll) : sm;
-    }
-}
-
-
-// pass-1 epilogue in FP64: u[s,c] = inv_s^2 (2^e_c sum_j 32^-j P1 - 2 f_s S_c); partial max|u|, sum 2 f u
+// pass-1 epilogue in FP64: u[s,c] = inv_s^2 (2^e_c sum_j 32^-j P1 - 2 f_s S_c); partial max|u|, sum 2 f u,
+// and from the column's last CTA colinfo2[c]
 template <int ND>
 __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int64_t rows, int k,
                            const double* __restrict__ colinfo, const double* __restrict__ f,
                            const double* __restrict__ inv, double* __restrict__ U, double* __restrict__ pmax,
-                           double* __restrict__ psum) {
+                           double* __restrict__ psum, unsigned* __restrict__ cnt, double* __restrict__ colinfo2) {
     __shared__ double smx[32], ssm[32];
     const int c = blockIdx.y;
     double s_hi, s_lo;
@@ -449,6 +480,7 @@ __global__ void k_combine1(const float* __restrict__ part, int nsplit, int nmma,
         pmax[blockIdx.x + (size_t)c * gridDim.x] = a;
         psum[blockIdx.x + (size_t)c * gridDim.x] = b;
     }
+    col_finish_last(pmax, psum, c, cnt, colinfo2);   // u's digit scale and centring sum
 }
 
 // pass-2 epilogue: out[i,c] = scale (2^e_c sum_j 32^-j P2 - C2_c)
@@ -863,10 +895,10 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
     GLOBE_RET(make_map(ctx, &mB2, D2, (uint64_t)kpad2, (uint64_t)nmma, BK, (uint32_t)nmma, true));
     // ---- digits of Z
     const int nz = col_parts(N);
-    k_col_maxsum<<<dim3(nz, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps);
+    unsigned* cnt;
+    GLOBE_RET(tc_counters(ctx, 2 * kg, &cnt));
+    k_col_maxsum<<<dim3(nz, kg), 256, 0, ctx->stream>>>(Z, N, N, pm, ps, cnt, col1);
     GLOBE_LAUNCHED(ctx, "k_col_maxsum");
-    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nz, kg, col1);
-    GLOBE_LAUNCHED(ctx, "k_col_finish");
     // digit rows past the kg columns stay zero
     if (nmma > kg * ND)
         GLOBE_CK(ctx, cudaMemsetAsync(D1 + (size_t)kg * ND * kpad1, 0, (size_t)(nmma - kg * ND) * kpad1,
@@ -885,10 +917,9 @@ static int tc_group(globe_ctx* ctx, const double* Z, int kg, double scale, doubl
         GLOBE_RET(gemm_dispatch(ctx, nmma, g.blk1, g.ntiles1, mB1, (int)g.Mk, nch1, sp1, P1, ldp1, err, zg));
     }
     const int sp1e = eff_splits(nch1, sp1);
-    k_combine1<ND><<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps);
+    k_combine1<ND><<<dim3(nbr, kg), 256, 0, ctx->stream>>>(P1, sp1e, nmma, ldp1, g.Mk, kg, col1, g.f, g.inv, U, pm, ps,
+                                                           cnt + kg, col2);
     GLOBE_LAUNCHED(ctx, "k_combine1");
-    k_col_finish<<<div_up(kg, 4), 128, 0, ctx->stream>>>(pm, ps, nbr, kg, col2);
-    GLOBE_LAUNCHED(ctx, "k_col_finish");
     // ---- digits of u, pass 2
     if (nmma > kg * ND)
         GLOBE_CK(ctx, cudaMemsetAsync(D2 + (size_t)kg * ND * kpad2, 0, (size_t)(nmma - kg * ND) * kpad2,
@@ -980,6 +1011,16 @@ int tc_err_word(globe_ctx* ctx, unsigned** err) {
     const bool fresh = ctx->ws[WS_TC_ERR].p == nullptr;
     GLOBE_RET(ws(ctx, WS_TC_ERR, 4, err));
     if (fresh) GLOBE_CK(ctx, cudaMemsetAsync(*err, 0, 4 * sizeof(unsigned), ctx->stream));
+    return GLOBE_OK;
+}
+
+// per-column arrival counts of col_finish_last, zero between launches: (re)created zeroed when
+// more are needed (never inside a capture, where allocation is refused; every shape's first
+// product runs outside one)
+int tc_counters(globe_ctx* ctx, size_t n, unsigned** cnt) {
+    const bool fresh = ctx->ws[WS_TC_CNT].bytes < n * sizeof(unsigned);
+    GLOBE_RET(ws(ctx, WS_TC_CNT, n, cnt));
+    if (fresh) GLOBE_CK(ctx, cudaMemsetAsync(*cnt, 0, ctx->ws[WS_TC_CNT].bytes, ctx->stream));
     return GLOBE_OK;
 }
 

@@ -150,9 +150,10 @@ __host__ __forceinline__ int col_parts(int64_t n) {
 
 // per-column max |x| and sum over n rows (partials per CTA); colinfo[c] = {exponent e with
 // max |x 2^-e| < 16, column sum} from those partials, or {0, NaN} for a column holding a
-// NaN or an infinity (k_tc_geno.cu)
+// NaN or an infinity (k_tc_geno.cu).  k_col_maxsum forms colinfo itself when given it and
+// zeroed per-column counts cnt (tc_counters), in its last CTA per column; else k_col_finish.
 __global__ void k_col_maxsum(const double* __restrict__ X, int64_t n, int64_t ld, double* __restrict__ pmax,
-                             double* __restrict__ psum);
+                             double* __restrict__ psum, unsigned* __restrict__ cnt, double* __restrict__ colinfo);
 __global__ void k_col_finish(const double* __restrict__ pmax, const double* __restrict__ psum, int nparts, int k,
                              double* __restrict__ colinfo);
 
