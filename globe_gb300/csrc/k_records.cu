@@ -624,25 +624,9 @@ __global__ void k_reduce_cols(const double* __restrict__ part, int nparts, size_
                               const int32_t* __restrict__ cols, ReduceOut o) {
     __shared__ double sm[256];
     const int c = blockIdx.x;
-    const double* pc = part + blockIdx.y * qstride + (size_t)c * nparts;
-    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    int j = threadIdx.x;
-    for (; j + 3 * (int)blockDim.x < nparts; j += 4 * blockDim.x) {
-        a0 += pc[j];
-        a1 += pc[j + blockDim.x];
-        a2 += pc[j + 2 * blockDim.x];
-        a3 += pc[j + 3 * blockDim.x];
-    }
-    for (; j < nparts; j += blockDim.x) a0 += pc[j];
-    sm[threadIdx.x] = (a0 + a1) + (a2 + a3);
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
-        __syncthreads();
-    }
+    const double v = cta_reduce_256(part + blockIdx.y * qstride + (size_t)c * nparts, nparts, sm);   // 256 threads
     if (threadIdx.x == 0) {
         const int col = cols ? cols[c] : c;
-        const double v = sm[0];
         o.out[blockIdx.y][col] = v;
         if (o.quot) {
             const double q = (v != 0.0) ? o.num[col] / v : 0.0;

@@ -57,6 +57,47 @@ __device__ __forceinline__ void cta_sums_df(const D (&v)[NQ], const int (&q)[NQ]
     }
 }
 
+// A column reduction finished inside a thread-per-block kernel when no warp-per-block launch
+// contributes partials (no individual has more than SHORT_BLOCK records): the last of column
+// c's CTAs (a per-column arrival count, zero between launches, reset by that CTA) sums the
+// partials of quantity y < nq, part[y * S * kact + c * S + j], j < S, as k_reduce_cols would,
+// into out[y][cols[c]]; with quot, quot[col] = num[col] / out[0][col] (0 where it is 0) and
+// its double-float copy.
+struct Fin {
+    unsigned* cnt = nullptr;   // null: the host launches k_reduce_cols instead
+    const int32_t* cols = nullptr;
+    double* out[2] = {nullptr, nullptr};
+    const double* num = nullptr;
+    double* quot = nullptr;
+    float2* quot_df = nullptr;
+};
+
+// every thread of the CTA calls it, after the CTA's partials are written
+__device__ __forceinline__ void fin_last(const Fin& f, const double* part, int nq, int kact, int S) {
+    __shared__ bool last;
+    __shared__ double sm[256];
+    const int c = blockIdx.y;
+    __threadfence();   // this CTA's partials (written by threads 0 .. nq-1), then its arrival
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&f.cnt[c], 1u) == gridDim.x - 1u;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int col = f.cols ? f.cols[c] : c;
+    for (int y = 0; y < nq; ++y) {
+        const double v = cta_reduce_256(part + (size_t)y * S * kact + (size_t)c * S, S, sm);
+        if (threadIdx.x == 0) {
+            f.out[y][col] = v;
+            if (y == 0 && f.quot) {
+                const double q = (v != 0.0) ? f.num[col] / v : 0.0;
+                f.quot[col] = q;
+                if (f.quot_df) df::store(f.quot_df + col, df::from_double(q));
+            }
+        }
+    }
+    if (threadIdx.x == 0) f.cnt[c] = 0u;
+}
+
 // ---------------------------------------------------------------------------
 // Conversions
 
@@ -260,7 +301,7 @@ __global__ void k_vx_assemble_df_t(int32_t nblk, int64_t ld, int32_t N, const in
                                    const float2* __restrict__ x, const double* __restrict__ GZ,
                                    const float2* __restrict__ S0, const float2* __restrict__ S1,
                                    const int32_t* __restrict__ cols, float2* __restrict__ out,
-                                   double* __restrict__ part, int pstride) {
+                                   double* __restrict__ part, int pstride, Fin fin) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
@@ -295,6 +336,7 @@ __global__ void k_vx_assemble_df_t(int32_t nblk, int64_t ld, int32_t N, const in
     if (part) {
         const int q[1] = {c};
         cta_sums_df<1>(dot, q, part, pstride);
+        if (fin.cnt) fin_last(fin, part, 1, 0, pstride);
     }
 }
 
@@ -359,8 +401,18 @@ int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const floa
     const RecShape rs = rec_shape(ctx);
     double* part = nullptr;
     if (dot_out) GLOBE_RET(ws(ctx, WS_PART, (size_t)rs.S * kact * 2, &part));
+    Fin fin;   // no long blocks: the p'Vp reduction (and alpha) finish in the kernel
+    if (dot_out && rs.nbl == 0) {
+        GLOBE_RET(tc_counters(ctx, (size_t)kact, &fin.cnt));
+        fin.cols = cols;
+        fin.out[0] = dot_out;
+        fin.num = num;
+        fin.quot = quot;
+        fin.quot_df = quot_df;
+    }
     k_vx_assemble_df_t<<<dim3(rs.nbt, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.tdf,
-                                                                             v, x, GZ, S0, S1, cols, out, part, rs.S);
+                                                                             v, x, GZ, S0, S1, cols, out, part, rs.S,
+                                                                             fin);
     GLOBE_LAUNCHED(ctx, "k_vx_assemble_df_t");
     if (rs.nbl) {
         k_vx_assemble_df<<<rs.nbl, RB_THREADS, 0, ctx->stream>>>(c.nlong, c.Nrec, c.N, c.bstart, c.bind, c.tdf, v, x,
@@ -368,7 +420,7 @@ int vx_assemble_df(globe_ctx* ctx, const float2* x, const double* GZ, const floa
                                                                    rs.S);
         GLOBE_LAUNCHED(ctx, "k_vx_assemble_df");
     }
-    if (dot_out) GLOBE_RET(reduce_cols_div(ctx, part, rs.S, kact, cols, dot_out, num, quot, quot_df));
+    if (dot_out && !fin.cnt) GLOBE_RET(reduce_cols_div(ctx, part, rs.S, kact, cols, dot_out, num, quot, quot_df));
     return GLOBE_OK;
 }
 
@@ -380,7 +432,7 @@ __global__ void k_pcg_update_df_t(int32_t nblk, int64_t ld, const int32_t* __res
                                   const float2* __restrict__ alpha, float2* __restrict__ x, float2* __restrict__ r,
                                   const float2* __restrict__ p, const float2* __restrict__ Vp,
                                   float2* __restrict__ z, const int32_t* __restrict__ cols, int kact,
-                                  double* __restrict__ part, int pstride) {
+                                  double* __restrict__ part, int pstride, Fin fin) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     const int c = blockIdx.y;
     const int col = cols ? cols[c] : c;
@@ -440,6 +492,7 @@ __global__ void k_pcg_update_df_t(int32_t nblk, int64_t ld, const int32_t* __res
     }
     const int qi[2] = {c, kact + c};
     cta_sums_df<2>(acc, qi, part, pstride);
+    if (fin.cnt) fin_last(fin, part, 2, kact, pstride);
 }
 
 __global__ void k_pcg_update_df(int32_t nblk, int64_t ld, const int32_t* __restrict__ bstart,
@@ -515,15 +568,23 @@ int pcg_update_df(globe_ctx* ctx, const float2* H, const float2* alpha, float2* 
     const D inv_e = df::from_double_host(1.0 / ctx->vc[0]);
     double* part;
     GLOBE_RET(ws(ctx, WS_PART, (size_t)rs.S * kact * 2, &part));
+    Fin fin;   // no long blocks: the r'r and r'z reductions finish in the kernel
+    if (rs.nbl == 0) {
+        GLOBE_RET(tc_counters(ctx, (size_t)kact, &fin.cnt));
+        fin.cols = cols;
+        fin.out[0] = rr;
+        fin.out[1] = rz;
+    }
     k_pcg_update_df_t<<<dim3(rs.nbt, kact), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.bstart, c.tdf, inv_e, H,
                                                                             alpha, x, r, p, Vp, z, cols, kact, part,
-                                                                            rs.S);
+                                                                            rs.S, fin);
     GLOBE_LAUNCHED(ctx, "k_pcg_update_df_t");
     if (rs.nbl) {
         k_pcg_update_df<<<rs.nbl, RB_THREADS, 0, ctx->stream>>>(c.nlong, c.Nrec, c.bstart, c.tdf, inv_e, H, alpha, x,
                                                                   r, p, Vp, z, cols, kact, part, c.lblk, rs.nbt, rs.S);
         GLOBE_LAUNCHED(ctx, "k_pcg_update_df");
     }
+    if (fin.cnt) return GLOBE_OK;
     return reduce_cols2(ctx, part, rs.S, kact, cols, rr, rz);
 }
 

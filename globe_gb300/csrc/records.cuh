@@ -24,6 +24,30 @@ inline RecShape rec_shape(const globe_ctx* ctx) {
     return r;
 }
 
+// Sum of one column's nparts partials by a CTA of 256 threads: four strided accumulators per
+// thread, then a tree in sm (256 doubles); every thread returns the sum.  k_reduce_cols and the
+// reductions that the record kernels' last CTAs finish both use it, so the order is one.
+__device__ __forceinline__ double cta_reduce_256(const double* __restrict__ pc, int nparts, double* sm) {
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int j = threadIdx.x;
+    for (; j + 3 * 256 < nparts; j += 4 * 256) {
+        a0 += __ldcg(pc + j);
+        a1 += __ldcg(pc + j + 256);
+        a2 += __ldcg(pc + j + 2 * 256);
+        a3 += __ldcg(pc + j + 3 * 256);
+    }
+    for (; j < nparts; j += 256) a0 += __ldcg(pc + j);
+    sm[threadIdx.x] = (a0 + a1) + (a2 + a3);
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] += sm[threadIdx.x + s];
+        __syncthreads();
+    }
+    const double v = sm[0];
+    __syncthreads();   // sm may be reused
+    return v;
+}
+
 // The warp-per-block kernels stage per-warp partial sums of RCH columns at a time in static
 // shared memory, sm[(j * RCH + cc) * RB_WARPS + warp] for quantity j < nq and column c0 + cc,
 // so any number of columns fits.  flush_chunk sums them over the CTA's warps, in warp order,
