@@ -294,8 +294,9 @@ int sub_mat(globe_ctx* ctx, const double* A, const double* Bm, int m, const doub
             int kout);
 int bhat_kernel(globe_ctx* ctx, const double* vr, double* bhat);
 int ftheta_kernel(globe_ctx* ctx, const double* vr, const double* uh, double* fth);
-int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen,
-                 double* Y);
+// gen: normals from the stream of seed (zi: 3 N numMC doubles of scratch); else from draws
+int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen, double* Y,
+                 double* zi);
 int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double* TY, int numMC,
                 double* out);
 

@@ -843,9 +843,9 @@ __device__ __forceinline__ uint64_t pmix(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-// standard normal number `idx` of stream `seed` (Box-Muller on two 53-bit uniforms)
-__device__ double stream_normal(uint64_t seed, uint64_t idx) {
-    uint64_t pair = idx >> 1;
+// standard normal numbers 2 pair and 2 pair + 1 of stream `seed` (Box-Muller on two 53-bit
+// uniforms): the cosine and sine halves of one draw
+__device__ void stream_normal_pair(uint64_t seed, uint64_t pair, double& even, double& odd) {
     uint64_t h1 = pmix(seed ^ pmix(2 * pair + 1));
     uint64_t h2 = pmix(seed ^ pmix(2 * pair + 2));
     double u1 = ((double)(h1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
@@ -853,50 +853,91 @@ __device__ double stream_normal(uint64_t seed, uint64_t idx) {
     double rad = sqrt(-2.0 * log(u1));
     double s, c;
     sincospi(2.0 * u2, &s, &c);
-    return (idx & 1) ? rad * s : rad * c;
+    even = rad * c;
+    odd = rad * s;
 }
 
-__global__ void k_probes(int64_t n, int32_t N, const int32_t* __restrict__ rind, const double* __restrict__ t,
-                         double sg, double se, double L00, double L10, double L11,
-                         const double* __restrict__ draws, uint64_t seed, int numMC, int no_time,
-                         double* __restrict__ Y) {
+// standard normal number `idx` of stream `seed`
+__device__ double stream_normal(uint64_t seed, uint64_t idx) {
+    double e, o;
+    stream_normal_pair(seed, idx >> 1, e, o);
+    return (idx & 1) ? o : e;
+}
+
+// the per-individual normals of probe j (grid.y) in generated mode, once per individual rather
+// than once per record: stream indices base .. base + L - 1 (base = j per, L = N or 3 N), i.e.
+// z1 of individual i at base + i and, with time effects, z2a / z2b at base + N + 2 i (+ 1),
+// into zi[3 j N + i], zi[(3 j + 1) N + i], zi[(3 j + 2) N + i]; one Box-Muller pair per step
+__global__ void k_probe_ind(int32_t N, uint64_t seed, int no_time, size_t per, double* __restrict__ zi) {
     const int j = blockIdx.y;
-    const size_t per = (no_time ? 1 : 3) * (size_t)N + n;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        const int i = rind[r];
-        double z1, z2a, z2b, z3;
-        if (no_time) {   // Y = sqrt(sig2g) Z1 + sqrt(sig2e) Z3 (varCompEst_reducedModel_noTime.cpp:563-577)
-            if (draws) {
-                const double* d = draws + (size_t)j * per;
-                z1 = d[i];
-                z3 = d[(size_t)N + r];
+    const uint64_t b = (uint64_t)j * per, L = (no_time ? 1u : 3u) * (uint64_t)N;
+    const uint64_t p0 = b >> 1, p1 = (b + L - 1) >> 1;
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (uint64_t)gridDim.x * blockDim.x;
+    double* z = zi + 3 * (size_t)j * N;
+    for (uint64_t p = p0 + tid; p <= p1; p += nth) {
+        double ze, zo;
+        stream_normal_pair(seed, p, ze, zo);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int64_t m = (int64_t)(2 * p + h) - (int64_t)b;
+            if (m < 0 || m >= (int64_t)L) continue;
+            const double v = h ? zo : ze;
+            if (m < N) {
+                z[m] = v;
             } else {
-                const uint64_t base = (uint64_t)j * per;
-                z1 = stream_normal(seed, base + i);
-                z3 = stream_normal(seed, base + (uint64_t)N + r);
+                const int64_t m2 = m - N;
+                z[(1 + (m2 & 1)) * (size_t)N + (m2 >> 1)] = v;
             }
-            Y[r + (size_t)j * n] = sg * z1 + se * z3;
-            continue;
         }
-        if (draws) {
-            const double* d = draws + (size_t)j * per;
-            z1 = d[i];
-            z2a = d[N + 2 * i];
-            z2b = d[N + 2 * i + 1];
-            z3 = d[3 * (size_t)N + r];
-        } else {
-            const uint64_t base = (uint64_t)j * per;
-            z1 = stream_normal(seed, base + i);
-            z2a = stream_normal(seed, base + N + 2 * i);
-            z2b = stream_normal(seed, base + N + 2 * i + 1);
-            z3 = stream_normal(seed, base + 3 * (uint64_t)N + r);
-        }
-        const double tr = t[r];
-        Y[r + (size_t)j * n] = sg * z1 + se * z3 + z2a * (L00 + L10 * tr) + z2b * L11 * tr;
     }
 }
 
-int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen, double* Y) {
+// probe Y_j = sqrt(sig2g) Z1 + sqrt(sig2e) Z3 + the random-regression term (varCompEst.cpp:816-837;
+// without time effects varCompEst_reducedModel_noTime.cpp:563-577), record r of probe j
+__device__ __forceinline__ double probe_value(int no_time, double sg, double se, double L00, double L10, double L11,
+                                              double z1, double z2a, double z2b, double z3, double tr) {
+    if (no_time) return sg * z1 + se * z3;
+    return sg * z1 + se * z3 + z2a * (L00 + L10 * tr) + z2b * L11 * tr;
+}
+
+// draws given: the normals of probe j at draws[j * per ...]; generated: the per-individual ones
+// from k_probe_ind and the per-record one z3 (index base + N0 + r, N0 = N or 3 N) by Box-Muller
+// pairs, one pair per thread step (both halves are records of the probe, except at its ends)
+__global__ void k_probes(int64_t n, int32_t N, const int32_t* __restrict__ rind, const double* __restrict__ t,
+                         double sg, double se, double L00, double L10, double L11,
+                         const double* __restrict__ draws, const double* __restrict__ zi, uint64_t seed, int numMC,
+                         int no_time, double* __restrict__ Y) {
+    const int j = blockIdx.y;
+    const size_t per = (no_time ? 1 : 3) * (size_t)N + n;
+    const size_t N0 = (no_time ? 1 : 3) * (size_t)N;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+    if (draws) {
+        const double* d = draws + (size_t)j * per;
+        for (int64_t r = tid; r < n; r += nth) {
+            const int i = rind[r];
+            const double z2a = no_time ? 0.0 : d[N + 2 * (size_t)i], z2b = no_time ? 0.0 : d[N + 2 * (size_t)i + 1];
+            Y[r + (size_t)j * n] = probe_value(no_time, sg, se, L00, L10, L11, d[i], z2a, z2b, d[N0 + r], t[r]);
+        }
+        return;
+    }
+    const uint64_t b3 = (uint64_t)j * per + N0;   // stream index of record 0's z3
+    const uint64_t p0 = b3 >> 1, p1 = (b3 + (uint64_t)n - 1) >> 1;
+    const double* z1s = zi + (3 * (size_t)j) * N;
+    for (uint64_t p = p0 + (uint64_t)tid; p <= p1; p += (uint64_t)nth) {
+        double ze, zo;
+        stream_normal_pair(seed, p, ze, zo);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int64_t r = (int64_t)(2 * p + h) - (int64_t)b3;
+            if (r < 0 || r >= n) continue;
+            const int i = rind[r];
+            const double z2a = no_time ? 0.0 : z1s[N + i], z2b = no_time ? 0.0 : z1s[2 * (size_t)N + i];
+            Y[r + (size_t)j * n] = probe_value(no_time, sg, se, L00, L10, L11, z1s[i], z2a, z2b, h ? zo : ze, t[r]);
+        }
+    }
+}
+
+int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, bool gen, double* Y, double* zi) {
     auto& c = ctx->coh;
     const double* v = ctx->vc;
     // compute_chol_2x2 (varCompEst.cpp:800-813); unused without time effects
@@ -909,69 +950,112 @@ int probes_build(globe_ctx* ctx, const double* draws, int numMC, uint64_t seed, 
         if (d11 < 0) d11 = 0;
         L11 = sqrt(d11);
     }
+    if (gen) {
+        const size_t per = (no_time ? 1 : 3) * (size_t)c.N + (size_t)c.Nrec;
+        const int nbi = div_up(c.N, 256) < 1216 ? div_up(c.N, 256) : 1216;
+        k_probe_ind<<<dim3(nbi, numMC), 256, 0, ctx->stream>>>(c.N, seed, no_time, per, zi);
+        GLOBE_LAUNCHED(ctx, "k_probe_ind");
+    }
     int nb = div_up(c.Nrec, 256);
     if (nb > 1216) nb = 1216;
     k_probes<<<dim3(nb, numMC), 256, 0, ctx->stream>>>(c.Nrec, c.N, c.rind, c.times(), sqrt(v[1]), sqrt(v[0]),
-                                                       L00, L10, L11, gen ? nullptr : draws, seed, numMC, no_time, Y);
+                                                       L00, L10, L11, gen ? nullptr : draws, zi, seed, numMC, no_time,
+                                                       Y);
     GLOBE_LAUNCHED(ctx, "k_probes");
     return GLOBE_OK;
 }
 
 // trace terms: for probe j, f~_k from (VR_j, UH_j) and dot with TY_j
-// (estimateTrace_PdV, varCompEst.cpp:955-968).  out[j*5 + k].
+// (estimateTrace_PdV, varCompEst.cpp:955-968).  out[j*5 + k].  The launch shape of the record
+// kernels: a thread per (individual of at most SHORT_BLOCK records, probe) -- grid.y = probe --
+// and a warp per longer individual over every probe, partials part[slot + (5 j + k) * S].
+
+// the five terms of probe j over one individual's records [st, en)
+__device__ __forceinline__ void trace_block(const double* __restrict__ vr, const double* __restrict__ ty,
+                                            const double* __restrict__ t, double u, int st, int en, int step,
+                                            double (&acc)[5], bool warp) {
+    double w = 0, tw = 0;
+    for (int r = st; r < en; r += step) {
+        w += vr[r];
+        tw += t[r] * vr[r];
+    }
+    if (warp) {
+        w = warp_sum(w);
+        tw = warp_sum(tw);
+    }
+    for (int r = st; r < en; r += step) {
+        const double y = ty[r], tr = t[r];
+        acc[0] += vr[r] * y;
+        acc[1] += u * y;
+        acc[2] += w * y;
+        acc[3] += (tr * w + tw) * y;
+        acc[4] += tw * tr * y;
+    }
+}
+
+__global__ void k_trace_terms_t(int32_t nblk, int64_t n, int32_t N, const int32_t* __restrict__ bstart,
+                                const int32_t* __restrict__ bind, const double* __restrict__ t, double inv_g,
+                                const double* __restrict__ VR, const double* __restrict__ UH,
+                                const double* __restrict__ TY, double* __restrict__ part, int pstride) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    double acc[5] = {0, 0, 0, 0, 0};
+    if (b < nblk && bstart[b + 1] - bstart[b] <= SHORT_BLOCK &&   // long blocks: a warp each
+        GLOBE_BOUNDS(bstart[b] >= 0 && bstart[b + 1] <= n && bind[b] >= 0 && bind[b] < N, 0x1301u)) {
+        const int i = bind[b];
+        trace_block(VR + (size_t)j * n, TY + (size_t)j * n, t, UH[i + (size_t)j * N] * inv_g, bstart[b], bstart[b + 1],
+                    1, acc, false);
+    }
+    const int q[5] = {5 * j, 5 * j + 1, 5 * j + 2, 5 * j + 3, 5 * j + 4};
+    cta_sums<5>(acc, q, part, pstride);
+}
+
 __global__ void k_trace_terms(int32_t nblk, int64_t n, int32_t N, const int32_t* __restrict__ bstart,
                               const int32_t* __restrict__ bind, const double* __restrict__ t, double inv_g,
                               const double* __restrict__ VR, const double* __restrict__ UH,
-                              const double* __restrict__ TY, int numMC, double* __restrict__ part) {
+                              const double* __restrict__ TY, int numMC, double* __restrict__ part,
+                              const int32_t* __restrict__ bl, int slot0, int pstride) {
     extern __shared__ double sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int b = blockIdx.x * RB_WARPS + warp;
-    const bool live = b < nblk;
+    const int idx = blockIdx.x * RB_WARPS + warp;
+    const bool live = idx < nblk;
+    const int b = live ? (bl ? bl[idx] : idx) : 0;
     int st = 0, en = 0, i = 0;
     if (live) { st = bstart[b]; en = bstart[b + 1]; i = bind[b]; }
+    if (live && !GLOBE_BOUNDS(st >= 0 && st <= en && en <= n && i >= 0 && i < N, 0x1401u)) st = en = i = 0;
     for (int j = 0; j < numMC; ++j) {
         double acc[5] = {0, 0, 0, 0, 0};
-        if (live) {
-            const double* vr = VR + (size_t)j * n;
-            const double* ty = TY + (size_t)j * n;
-            double w = 0, tw = 0;
-            for (int r = st + lane; r < en; r += 32) {
-                w += vr[r];
-                tw += t[r] * vr[r];
-            }
-            w = warp_sum(w);
-            tw = warp_sum(tw);
-            const double u = UH[i + (size_t)j * N] * inv_g;
-            for (int r = st + lane; r < en; r += 32) {
-                const double y = ty[r], tr = t[r];
-                acc[0] += vr[r] * y;
-                acc[1] += u * y;
-                acc[2] += w * y;
-                acc[3] += (tr * w + tw) * y;
-                acc[4] += tw * tr * y;
-            }
-        }
+        if (live)
+            trace_block(VR + (size_t)j * n, TY + (size_t)j * n, t, UH[i + (size_t)j * N] * inv_g, st + lane, en, 32, acc,
+                        true);
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             double s = warp_sum(acc[k]);
             if (lane == 0) sm[(j * 5 + k) * RB_WARPS + warp] = s;
         }
     }
-    cta_partials(sm, numMC * 5, part, blockIdx.x, gridDim.x);
+    cta_partials(sm, numMC * 5, part, slot0 + blockIdx.x, pstride);
 }
 
 int trace_terms(globe_ctx* ctx, const double* VR, const double* UH, const double* TY, int numMC, double* out) {
     auto& c = ctx->coh;
-    int nb = div_up(c.N, RB_WARPS);
+    const RecShape rs = rec_shape(ctx);
     double* part;
-    GLOBE_RET(ws(ctx, WS_GPART, (size_t)nb * numMC * 5, &part));
-    size_t sm = sizeof(double) * RB_WARPS * numMC * 5;
-    if (sm > 48 * 1024)
-        GLOBE_CK(ctx, cudaFuncSetAttribute(k_trace_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_trace_terms<<<nb, RB_THREADS, sm, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind, c.times(),
-                                                       1.0 / ctx->vc[1], VR, UH, TY, numMC, part);
-    GLOBE_LAUNCHED(ctx, "k_trace_terms");
-    return reduce_cols(ctx, part, nb, numMC * 5, nullptr, out);
+    GLOBE_RET(ws(ctx, WS_GPART, (size_t)rs.S * numMC * 5, &part));
+    k_trace_terms_t<<<dim3(rs.nbt, numMC), TB_THREADS, 0, ctx->stream>>>(c.N, c.Nrec, c.N, c.bstart, c.bind,
+                                                                           c.times(), 1.0 / ctx->vc[1], VR, UH, TY,
+                                                                           part, rs.S);
+    GLOBE_LAUNCHED(ctx, "k_trace_terms_t");
+    if (rs.nbl) {
+        const size_t sm = sizeof(double) * RB_WARPS * numMC * 5;
+        if (sm > 48 * 1024)
+            GLOBE_CK(ctx, cudaFuncSetAttribute(k_trace_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_trace_terms<<<rs.nbl, RB_THREADS, sm, ctx->stream>>>(c.nlong, c.Nrec, c.N, c.bstart, c.bind, c.times(),
+                                                                1.0 / ctx->vc[1], VR, UH, TY, numMC, part, c.lblk,
+                                                                rs.nbt, rs.S);
+        GLOBE_LAUNCHED(ctx, "k_trace_terms");
+    }
+    return reduce_cols(ctx, part, rs.S, numMC * 5, nullptr, out);
 }
 
 }  // namespace globe

@@ -862,9 +862,11 @@ static int grad_probes(globe_ctx* ctx, const double* probes, int numMC, uint64_t
         size_t cnt = (size_t)numMC * ((ctx->model == GLOBE_MODEL_NO_TIME ? 1 : 3) * (size_t)N + n);
         GLOBE_RET(ws(ctx, WS_PROBE, cnt, &dd));
         GLOBE_CK(ctx, cudaMemcpyAsync(dd, probes, sizeof(double) * cnt, cudaMemcpyHostToDevice, ctx->stream));
-        GLOBE_RET(probes_build(ctx, dd, numMC, seed, false, pb.Y));
+        GLOBE_RET(probes_build(ctx, dd, numMC, seed, false, pb.Y, nullptr));
     } else {
-        GLOBE_RET(probes_build(ctx, nullptr, numMC, seed, true, pb.Y));
+        double* zi;   // per-individual normals (the injected-draws buffer is free in this mode)
+        GLOBE_RET(ws(ctx, WS_PROBE, (size_t)3 * N * numMC, &zi));
+        GLOBE_RET(probes_build(ctx, nullptr, numMC, seed, true, pb.Y, zi));
     }
     // V*^-1 Y by the Woodbury block inverse with g = sig2g (varCompEst.cpp:839-862)
     GLOBE_RET(build_H(ctx, nullptr, ctx->vc[1], pb.Hs));
