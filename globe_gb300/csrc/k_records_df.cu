@@ -77,7 +77,7 @@ __device__ __forceinline__ void fin_last(const Fin& f, const double* part, int n
     __shared__ bool last;
     __shared__ double sm[256];
     const int c = blockIdx.y;
-    __threadfence();   // this CTA's partials (written by threads 0 .. nq-1), then its arrival
+    if (threadIdx.x < nq) __threadfence();   // this CTA's partials (written by threads 0 .. nq-1), then its arrival
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(&f.cnt[c], 1u) == gridDim.x - 1u;
     __syncthreads();
