@@ -47,6 +47,44 @@ def test_device_probes_are_reproducible(gctx, case):
     assert np.array_equal(a, b) and not np.array_equal(a, c)
 
 
+def _device_stream_normals(seed, n):
+    """The device probe stream, restated: normal m = Box-Muller on the splitmix hashes of
+    pair m // 2 (cosine half for even m, sine half for odd m)."""
+    M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+    def pmix(z):
+        with np.errstate(over="ignore"):
+            z = z + np.uint64(0x9E3779B97F4A7C15)
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            return (z ^ (z >> np.uint64(31))) & M64
+
+    idx = np.arange(n, dtype=np.uint64)
+    pair = idx >> np.uint64(1)
+    s = np.uint64(seed)
+    with np.errstate(over="ignore"):
+        h1 = pmix(s ^ pmix(np.uint64(2) * pair + np.uint64(1)))
+        h2 = pmix(s ^ pmix(np.uint64(2) * pair + np.uint64(2)))
+    u1 = ((h1 >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+    u2 = ((h2 >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+    rad = np.sqrt(-2.0 * np.log(u1))
+    return np.where((idx & np.uint64(1)) == 1, rad * np.sin(2.0 * np.pi * u2), rad * np.cos(2.0 * np.pi * u2))
+
+
+def test_device_probes_are_the_stream_injected(gctx, case):
+    """Probes drawn on the device from a seed (per-individual normals once, Box-Muller pairs)
+    equal the same stream's normals passed in as injected draws, at their draw positions."""
+    th = case["ref"]["theta0"]
+    gctx.set_vc(th)
+    gctx.mme(tol=1e-10, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND)
+    numMC, seed = 6, 1234567
+    per = 3 * case["N"] + len(case["indiv"])
+    gen = gctx.aireml_grad(numMC, seed=seed, tol=1e-10)
+    inj = gctx.aireml_grad(numMC, probes=_device_stream_normals(seed, numMC * per), tol=1e-10)
+    for key in ("grad", "trace", "first"):
+        assert rel(gen[key], inj[key]) < 1e-11, key
+
+
 def test_loop_follows_reference_trajectory(gctx, case, tmp_path):
     ref = case["ref"]
     probes, per = aireml_probes(case, 60)
