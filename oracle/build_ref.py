@@ -59,7 +59,7 @@ def _write(p, s):
 
 
 def _fp64(src):
-    """Type substitution: every float becomes double (survey recipe)."""
+    """Type substitution: every float becomes double, and the float Eigen types their double forms."""
     s = re.sub(r"\bfloat\b", "double", src)
     s = re.sub(r"Eigen::MatrixXf|\bMatrixXf\b", "MatT", s)
     s = re.sub(r"Eigen::VectorXf|\bVectorXf\b", "VecT", s)
