@@ -87,22 +87,27 @@ def _load(gctx):
 
 
 @pytest.mark.gpu
-def test_first_evaluation_matches_reference(gctx):
+@pytest.mark.parametrize("prec,tol_ref", [(G.PREC_FP64, 1e-8), (G.PREC_MIXED, 1e-7)], ids=["fp64", "mixed"])
+def test_first_evaluation_matches_reference(gctx, prec, tol_ref):
+    """Score and AI of the reduced model against the FP64 reference run; mixed precision runs
+    the tensor-core dense product and the double-float record kernels (sig2b* = 0)."""
     ref = _ref()
     try:
         _load(gctx)
         probes, per = _probes(ref, 1)
         gctx.set_vc(list(ref["theta0"]) + [0.0, 0.0, 0.0])
         tol = ref["pcg_tol"]
-        gctx.mme(tol=tol, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND)
-        g = gctx.aireml_grad(ref["numMC"], probes=probes, tol=tol)
-        ai = gctx.aireml_ai(tol=tol)
+        gctx.mme(tol=tol, rule=G.RULE_AIREML, x0mode=G.X0_PRECOND, precision=prec)
+        n0 = gctx.record_df_solves()
+        g = gctx.aireml_grad(ref["numMC"], probes=probes, tol=tol, precision=prec)
+        ai = gctx.aireml_ai(tol=tol, precision=prec)
+        assert (gctx.record_df_solves() > n0) == (prec == G.PREC_MIXED)
         it1 = ref["iterations"][0]
-        assert rel(g["grad"][:2], it1["gradients"][0]) < 1e-8
+        assert rel(g["grad"][:2], it1["gradients"][0]) < tol_ref
         assert np.all(g["grad"][2:] == 0)
-        assert rel(ai[:2, :2], np.array(it1["ai"][0])) < 1e-8
-        f = gctx.aireml_eval(ref["numMC"], probes=probes, tol=tol)     # one block solve: same score
-        assert rel(f["grad"][:2], it1["gradients"][0]) < 1e-8
+        assert rel(ai[:2, :2], np.array(it1["ai"][0])) < tol_ref
+        f = gctx.aireml_eval(ref["numMC"], probes=probes, tol=tol, precision=prec)   # one block solve: same score
+        assert rel(f["grad"][:2], it1["gradients"][0]) < tol_ref
     finally:
         gctx.set_model(G.MODEL_FULL)
 
