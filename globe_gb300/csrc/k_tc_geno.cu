@@ -492,7 +492,7 @@ __global__ void k_combine2(const float* __restrict__ part, int nsplit, int nmma,
     recombine_scales<ND>((int)colinfo[2 * c], s_hi, s_lo);
     const double C2 = colinfo[2 * c + 1];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-        out[i + c * ldo] = scale * (recombine<ND>(part, nsplit, nmma, ldp, c, i, s_hi, s_lo) - C2);
+        out[i + c * ldo] = scale * (recombine<ND, 4>(part, nsplit, nmma, ldp, c, i, s_hi, s_lo) - C2);
     }
 }
 

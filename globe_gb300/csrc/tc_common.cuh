@@ -113,18 +113,40 @@ __device__ __forceinline__ double absmax_bits(double m, double v) {
 // scaled to an integer, the split partials are summed in int64 and the digits combined in two
 // exact int64 halves (hi = digits 0..ND_HI-1, lo = the rest); the only rounding is the final
 // FP64 addition.
-template <int ND>
+// With YU > 1, YU splits' ND loads issue together: k_combine2 reads 10 splits and waits on
+// them; k_combine1 reads 2, holds more registers, and runs faster one split at a time.
+template <int ND, int YU = 1>
 __device__ __forceinline__ double recombine(const float* __restrict__ part, int nsplit, int nmma, int64_t ldp, int c,
                                            int64_t row, double s_hi, double s_lo) {
     constexpr int NH = (ND + 1) / 2;
     long long pj[ND];
-#pragma unroll
-    for (int j = 0; j < ND; ++j)
-        pj[j] = (long long)__float2int_rn(part[((int64_t)c * ND + j) * ldp + row] * GENO_UNIT_INV);
-    for (int y = 1; y < nsplit; ++y) {
+    if constexpr (YU == 1) {
 #pragma unroll
         for (int j = 0; j < ND; ++j)
-            pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * ND + j) * ldp + row] * GENO_UNIT_INV);
+            pj[j] = (long long)__float2int_rn(part[((int64_t)c * ND + j) * ldp + row] * GENO_UNIT_INV);
+        for (int y = 1; y < nsplit; ++y) {
+#pragma unroll
+            for (int j = 0; j < ND; ++j)
+                pj[j] += (long long)__float2int_rn(part[((int64_t)y * nmma + c * ND + j) * ldp + row] * GENO_UNIT_INV);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < ND; ++j) pj[j] = 0;
+        for (int y0 = 0; y0 < nsplit; y0 += YU) {
+            float v[YU][ND];
+#pragma unroll
+            for (int u = 0; u < YU; ++u)
+                if (y0 + u < nsplit) {
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) v[u][j] = part[((int64_t)(y0 + u) * nmma + c * ND + j) * ldp + row];
+                }
+#pragma unroll
+            for (int u = 0; u < YU; ++u)
+                if (y0 + u < nsplit) {
+#pragma unroll
+                    for (int j = 0; j < ND; ++j) pj[j] += (long long)__float2int_rn(v[u][j] * GENO_UNIT_INV);
+                }
+        }
     }
     long long hi = 0, lo = 0;
 #pragma unroll
