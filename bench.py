@@ -666,7 +666,8 @@ def run_ours(args, cfg):
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
             "dtype": ("f64" if prec == G.PREC_FP64 else
-                      "e4m3 x e4m3 -> f32 (exact digits of A and Z), f64 PCG"),
+                      "e4m3 x e4m3 -> f32 (exact digits of A and Z); PCG vectors in double-float f32 pairs, "
+                      "scalars and dot products f64"),
             "data": "synthetic (GPU counter-based genotypes%s, seeded numpy records)" % (
                 ", GRM built from them" if dense else ""),
             "config": common_config(args, cfg, k, Nrec),
