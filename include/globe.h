@@ -45,7 +45,7 @@ extern "C" {
 #define GLOBE_ERR_NUMERIC (-7)     /* breakdown (non-finite or zero curvature) */
 #define GLOBE_ERR_UNSUPPORTED (-8) /* option not available for this input */
 
-/* precision of the GRM product inside the solver */
+/* precision of the GRM product and the solve's record arithmetic */
 #define GLOBE_PREC_FP64 0   /* plain FP64 everywhere (the drop-in path) */
 #define GLOBE_PREC_MIXED 1  /* genotype GRM product on the FP8 tensor cores with exact
                                base-32 digit slicing of the right-hand sides (9 digits =
@@ -55,7 +55,10 @@ extern "C" {
                                one fixed-point grid (7 N^2 bytes; A within 2^-34
                                max|A|), or in double-float FP32 arithmetic (~48 bits)
                                when the planes do not fit in free device memory or
-                               A has a non-finite entry */
+                               A has a non-finite entry; inside PCG / MME / AIREML solves
+                               the record-level vectors run in double-float FP32 pairs
+                               and the scalars and dot products in FP64
+                               (globe_set_record_df) */
 
 /* models (globe_set_model) */
 #define GLOBE_MODEL_FULL 0     /* random intercept and slope per individual (runAIREML) */
