@@ -70,7 +70,10 @@ def test_zero_rhs_column_and_cap(setup):
     assert info3["iters"] == 3 and not info3["converged"]
 
 
-def test_dense_and_odd_sizes(gctx, orc):
+@pytest.mark.parametrize("precision,tol_o", [(G.PREC_FP64, 1e-9), (G.PREC_MIXED, 1e-8)], ids=["fp64", "mixed"])
+def test_dense_and_odd_sizes(gctx, orc, precision, tol_o):
+    """Dense GRM, N = 131 individuals of 1-6 records; mixed precision runs the tensor-core
+    dense product (A to 2^-34 max|A|) and the double-float record kernels."""
     from globe_gb300 import synth
     coh = cohort(21, 131, 257, recs=("uniform", 1, 6), miss=0.03)
     grm = synth.grm_from_packed(coh["packed"], 131)
@@ -80,9 +83,9 @@ def test_dense_and_odd_sizes(gctx, orc):
     s = orc.Solver(coh["indiv"], coh["X"], coh["y"], 131, VC_F, grm_lt=grm)
     s.precond_build()
     B = np.column_stack([coh["X"], coh["y"]])
-    X, info = gctx.pcg(B, tol=1e-12, rule=G.RULE_PCGSOLVER)
+    X, info = gctx.pcg(B, tol=1e-12, rule=G.RULE_PCGSOLVER, precision=precision)
     Xo, it = s.pcg(B, 1e-12, rule=0)
-    assert rel(X, Xo) < 1e-9
+    assert info["converged"] and rel(X, Xo) < tol_o
 
 
 @pytest.mark.parametrize("precision", [G.PREC_FP64, G.PREC_MIXED])
